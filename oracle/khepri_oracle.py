@@ -1,0 +1,533 @@
+"""CPU oracle for the Crystal RCWA solve path — TEST INFRASTRUCTURE ONLY.
+
+This module restates, in plain numpy complex128 with LAPACK-backed dense solves and
+``numpy.linalg.eig``, the algorithm the reference (Kaeryv/Khepri) runs for
+``Crystal.solve`` + ``poynting_flux_end`` + ``fields_volume``.  Every function names the
+reference lines it follows (paths relative to the reference project root).
+
+Who may use it: ``tests/``, ``__graft_entry__.smoke()`` (as the checker) and ``bench.py``
+(its ``cpu_baseline`` leg and ``--impl reference`` arm).  The product package
+``khepri_gb300`` never imports it.
+
+Parity pinning: the oracle is checked (tests/test_oracle_golden.py) against golden vectors
+produced by running the reference itself on the same inputs (tests/golden/make_golden.py),
+and against the reference's own known-answer test, the thin-film Fresnel check of
+test/integration/test_complex_eps.py:13-42.
+
+The arithmetic underneath lives in numpy/LAPACK (zgesv, zgeev, zgemm) and numpy's FFT
+(pocketfft), exactly as in the reference; numpy versions there are unpinned
+(requirements.txt:1-5).
+"""
+from __future__ import annotations
+
+import cmath
+import math
+from types import SimpleNamespace
+
+import numpy as np
+
+TWOPI = 2.0 * math.pi
+
+
+# ---------------------------------------------------------------------------------------
+# Basis: harmonic indices, reciprocal lattice, k-vectors
+# ---------------------------------------------------------------------------------------
+def expansion_indices(pw):
+    """Integer harmonic pairs (m, n), m varying fastest: flat index k = j*Px + i.
+
+    Follows khepri/expansion.py:4-16 (odd pw asserted; meshgrid(m, n) flattened).
+    """
+    px, py = pw
+    if px % 2 != 1 or py % 2 != 1:
+        raise AssertionError("harmonic counts must be odd")
+    m = np.arange(-(px - 1) // 2, (px - 1) // 2 + 1)
+    n = np.arange(-(py - 1) // 2, (py - 1) // 2 + 1)
+    mm, nn = np.meshgrid(m, n)
+    return np.vstack([mm.ravel(), nn.ravel()])
+
+
+def reciprocal_basis(lattice):
+    """(b1, b2) with b_i . a_j = 2*pi*delta_ij; khepri/tools.py:64-69."""
+    a1, a2 = np.asarray(lattice[0], dtype=float), np.asarray(lattice[1], dtype=float)
+    det = a1[0] * a2[1] - a1[1] * a2[0]
+    s = TWOPI / det
+    b1 = np.array([a2[1] * s, -a2[0] * s])
+    b2 = np.array([-a1[1] * s, a1[0] * s])
+    return np.stack([b1, b2])
+
+
+def lattice_vectors(lattice="square", pitch=1.0):
+    """khepri/crystal.py:60-74."""
+    if isinstance(lattice, str):
+        if lattice == "square":
+            return pitch * np.asarray([[1.0, 0.0], [0.0, 1.0]])
+        if lattice == "hexagonal":
+            return pitch * np.asarray([[math.sqrt(3) / 2, 0.5], [math.sqrt(3) / 2, -0.5]])
+        raise NotImplementedError(f"This {lattice} magic-string is not emplemented.")
+    return np.asarray(lattice)
+
+
+def g_vectors(pw, lattice):
+    """G = m*b1 + n*b2 for every harmonic, shape [2, Nh]; khepri/expansion.py:37-40."""
+    rec = reciprocal_basis(lattice)
+    idx = expansion_indices(pw)
+    return rec[0][:, None] * idx[0][None, :] + rec[1][:, None] * idx[1][None, :]
+
+
+def k_vectors(gvec, kp, wavelength, eps=1.0):
+    """Normalised (Kx, Ky, Kz) = (kp + G, kz)/k0; kz = conj(sqrt(k0^2 conj(eps) - kx^2 - ky^2)).
+
+    Follows khepri/expansion.py:43-50 and kz_from_kplanar expansion.py:19-26.
+    """
+    k0 = TWOPI / wavelength
+    kx = np.asarray(kp[0], dtype=complex) + gvec[0]
+    ky = np.asarray(kp[1], dtype=complex) + gvec[1]
+    kz = np.conj(np.sqrt((k0 ** 2 * np.conj(eps) - kx ** 2 - ky ** 2).astype(complex)))
+    return kx / k0, ky / k0, kz / k0
+
+
+def compute_kplanar(eps_inc, wavelength, theta_deg=0.0, phi_deg=0.0):
+    """In-plane wavevector of the incident plane wave; khepri/tools.py:17-21."""
+    phi, theta = np.deg2rad(phi_deg), np.deg2rad(theta_deg)
+    direction = np.array([np.cos(phi), np.sin(phi)], dtype=complex)
+    return direction * cmath.sqrt(eps_inc) * TWOPI / wavelength * np.sin(theta)
+
+
+# ---------------------------------------------------------------------------------------
+# Convolution (Toeplitz) matrix
+# ---------------------------------------------------------------------------------------
+def fourier_coefficients(eps_map):
+    """fftshift(fft2(eps)) / (Nx*Ny); khepri/tools.py:33-35."""
+    eps_map = np.asarray(eps_map)
+    return np.fft.fftshift(np.fft.fft2(eps_map)) / eps_map.size
+
+
+def convolution_matrix_fourier(coefs, pw):
+    """C[r, c] = coefs[g0x + p_r - p_c, g0y + q_r - q_c] with r = q*Px + p.
+
+    Vectorised form of the double loop in khepri/tools.py:38-56 (g0 = floor(N/2)).
+    """
+    px, py = pw
+    nx, ny = coefs.shape
+    r = np.arange(px * py)
+    p, q = r % px, r // px
+    ix = nx // 2 + p[:, None] - p[None, :]
+    iy = ny // 2 + q[:, None] - q[None, :]
+    return coefs[ix, iy].astype(complex)
+
+
+def convolution_matrix(eps_map, pw):
+    """khepri/tools.py:33-35."""
+    return convolution_matrix_fourier(fourier_coefficients(eps_map), pw)
+
+
+# ---------------------------------------------------------------------------------------
+# Per-layer eigenmodes and S-matrices (khepri/alternative.py)
+# ---------------------------------------------------------------------------------------
+def _branch_kz(arg):
+    """kz with the uniform/free-space branch: Re(arg) < 0 -> -i*sqrt(-arg), else sqrt(arg).
+
+    alternative.py:92-96 and 145-149.
+    """
+    arg = np.asarray(arg, dtype=complex).copy()
+    neg = arg.real < 0
+    out = np.empty_like(arg)
+    out[neg] = -1j * np.sqrt(-arg[neg])
+    out[~neg] = np.sqrt(arg[~neg])
+    return out
+
+
+def _block_diag4(a, b, c, d):
+    """[[diag(a), diag(b)], [diag(c), diag(d)]] as a dense 2N x 2N matrix."""
+    return np.block([[np.diag(a), np.diag(b)], [np.diag(c), np.diag(d)]])
+
+
+def free_space_eigenmodes(kx, ky):
+    """Gap medium (eps = 1): W0 = I, V0 = Q0 / (i kz0) column-wise; alternative.py:84-99."""
+    nh = len(kx)
+    q0 = _block_diag4(kx * ky, 1 - kx ** 2, ky ** 2 - 1, -ky * kx)
+    kz = _branch_kz(1 - kx ** 2 - ky ** 2)
+    lam = np.concatenate([1j * kz, 1j * kz])
+    return np.eye(2 * nh, dtype=complex), q0 / lam[None, :]
+
+
+def solve_uniform_layer(kx, ky, eps):
+    """Analytic modes of a homogeneous layer: W = I, lambda = i kz, V = Q / lambda.
+
+    alternative.py:130-156 (mu_r = 1).
+    """
+    nh = len(kx)
+    q = _block_diag4(kx * ky, eps - kx ** 2, ky ** 2 - eps, -ky * kx)
+    kz = _branch_kz(eps - kx ** 2 - ky ** 2)
+    lam = np.concatenate([1j * kz, 1j * kz])
+    return np.eye(2 * nh, dtype=complex), q / lam[None, :], lam
+
+
+def solve_structured_layer(kx, ky, conv):
+    """Modes of a patterned layer: eig(P Q), lambda = principal sqrt, V = Q W / lambda.
+
+    alternative.py:158-178.  P uses C^-1 K products (solve(C, K)), Q uses C.
+    """
+    nh = len(kx)
+    eye = np.eye(nh, dtype=complex)
+    ic_kx = np.linalg.solve(conv, np.diag(kx))
+    ic_ky = np.linalg.solve(conv, np.diag(ky))
+    dkx, dky = np.diag(kx), np.diag(ky)
+    p = np.block([[dkx @ ic_ky, eye - dkx @ ic_kx], [dky @ ic_ky - eye, -dky @ ic_kx]])
+    q = np.block([[dkx @ dky, conv - dkx @ dkx], [dky @ dky - conv, -dky @ dkx]])
+    lam2, w = np.linalg.eig(p @ q)
+    lam = np.sqrt(lam2 + 0j)
+    v = (q @ w) / lam[None, :]
+    return w, v, lam
+
+
+def build_scatmat(w, v, w0, v0, lam, depth, k0):
+    """Symmetric-layer S-matrix with propagator X = diag(exp(-lambda k0 d)).
+
+    alternative.py:181-195: A = W^-1 W0 + V^-1 V0, B = W^-1 W0 - V^-1 V0,
+    T = A - X B A^-1 X B, S11 = S22 = T^-1 (X B A^-1 X A - B), S12 = S21 = T^-1 X (A - B A^-1 B).
+    """
+    t1 = np.linalg.solve(w, w0)
+    t2 = np.linalg.solve(v, v0)
+    a, b = t1 + t2, t1 - t2
+    x = np.diag(np.exp(-lam * depth * k0))
+    ainv_x = np.linalg.solve(a, x)
+    t = a - x @ b @ ainv_x @ b
+    s11 = np.linalg.solve(t, x @ b @ ainv_x @ a - b)
+    s12 = np.linalg.solve(t, x @ (a - b @ np.linalg.solve(a, b)))
+    return np.array([[s11, s12], [s12, s11]])
+
+
+def _half_space_blocks(kx, ky, w0, v0, eps):
+    """Shared part of the two half-space S-matrices; alternative.py:32-56, 59-82."""
+    q = _block_diag4(kx * ky, eps - kx ** 2, ky ** 2 - eps, -ky * kx)
+    kz = np.conj(np.sqrt((eps - kx ** 2 - ky ** 2).astype(complex)))
+    lam = np.concatenate([1j * kz, 1j * kz])
+    w = np.eye(2 * len(kx), dtype=complex)
+    v = q / lam[None, :]
+    a = np.linalg.solve(w0, w) + np.linalg.solve(v0, v)
+    b = np.linalg.solve(w0, w) - np.linalg.solve(v0, v)
+    return a, b, w, v, lam
+
+
+def scattering_reflection(kx, ky, w0, v0, eps):
+    """Incidence half-space: S11 = -A^-1 B, S12 = 2A^-1, S21 = (A - B A^-1 B)/2, S22 = B A^-1.
+
+    alternative.py:32-56.
+    """
+    a, b, w, v, lam = _half_space_blocks(kx, ky, w0, v0, eps)
+    ainv = np.linalg.inv(a)
+    s = np.array([[-np.linalg.solve(a, b), 2 * ainv],
+                  [0.5 * (a - b @ np.linalg.solve(a, b)), b @ ainv]])
+    return s, w, v, lam
+
+
+def scattering_transmission(kx, ky, w0, v0, eps):
+    """Emergence half-space: S11 = B A^-1, S12 = (A - B A^-1 B)/2, S21 = 2A^-1, S22 = -A^-1 B.
+
+    alternative.py:59-82.
+    """
+    a, b, w, v, lam = _half_space_blocks(kx, ky, w0, v0, eps)
+    ainv = np.linalg.inv(a)
+    s = np.array([[b @ ainv, 0.5 * (a - b @ np.linalg.solve(a, b))],
+                  [2 * ainv, -np.linalg.solve(a, b)]])
+    return s, w, v, lam
+
+
+def scattering_identity(n):
+    """[[0, I], [I, 0]]; alternative.py:220-232 (block form)."""
+    eye = np.eye(n, dtype=complex)
+    zero = np.zeros((n, n), dtype=complex)
+    return np.array([[zero, eye], [eye, zero]])
+
+
+def redheffer_product(sa, sb):
+    """Star product SA * SB with four separate solves; alternative.py:19-30."""
+    eye = np.eye(sa.shape[-1], dtype=complex)
+    d = eye - sb[0, 0] @ sa[1, 1]
+    f = eye - sa[1, 1] @ sb[0, 0]
+    s11 = sa[0, 0] + sa[0, 1] @ np.linalg.solve(d, sb[0, 0]) @ sa[1, 0]
+    s12 = sa[0, 1] @ np.linalg.solve(d, sb[0, 1])
+    s21 = sb[1, 0] @ np.linalg.solve(f, sa[1, 0])
+    s22 = sb[1, 1] + sb[1, 0] @ np.linalg.solve(f, sa[1, 1]) @ sb[0, 1]
+    return np.array([[s11, s12], [s21, s22]])
+
+
+def stack_layers(smats, mask):
+    """Forward chain I*S_0*...*S_L (copies where mask) and the reverse chain; layer.py:35-60."""
+    n = smats[0].shape[-1]
+    stot = scattering_identity(n)
+    forward = []
+    for s, keep in zip(smats, mask):
+        stot = redheffer_product(stot, s)
+        forward.append(stot.copy() if keep else None)
+    srev = scattering_identity(n)
+    rmask = list(reversed(mask[1:]))
+    reverse = []
+    for i, s in enumerate(reversed(smats[1:])):
+        reverse.append(srev.copy() if rmask[i] else None)
+        srev = redheffer_product(s.copy(), srev)
+    reverse.append(srev.copy())
+    return forward, list(reversed(reverse)), stot
+
+
+# ---------------------------------------------------------------------------------------
+# Source and fluxes
+# ---------------------------------------------------------------------------------------
+def incident(pw, te, tm, k_vector):
+    """Plane-wave source vector [ex, ey] with a delta at harmonic (Nh-1)//2.
+
+    alternative.py:101-128: (te, tm) normalised; aTE = -(z_dev x kbar)/|.|, aTM = aTE x kbar/|.|,
+    with z_dev = (0, 0, -1); at normal incidence aTE = x, aTM = y.
+    """
+    norm = math.hypot(abs(te), abs(tm))
+    te, tm = te / norm, tm / norm
+    kvec = np.asarray(k_vector, dtype=complex)
+    kp_norm = np.linalg.norm(kvec[:2])
+    kbar = kvec / np.linalg.norm(kvec)
+    if abs(kp_norm) < 1e-8:
+        a_te = np.array([1.0, 0.0, 0.0], dtype=complex)
+        a_tm = np.array([0.0, 1.0, 0.0], dtype=complex)
+    else:
+        z_dev = np.array([0.0, 0.0, -1.0], dtype=complex)
+        a_te = -np.cross(z_dev, kbar)
+        a_te = a_te / np.linalg.norm(a_te)
+        a_tm = np.cross(a_te, kbar)
+        a_tm = a_tm / np.linalg.norm(a_tm)
+    nh = pw[0] * pw[1]
+    pol = te * a_te + tm * a_tm
+    out = np.zeros(2 * nh, dtype=complex)
+    out[(nh - 1) // 2] = pol[0]
+    out[nh + (nh - 1) // 2] = pol[1]
+    return out
+
+
+def poynting_fluxes(gvec, c_out, kp, wavelength, epsi, eps_medium):
+    """Per-order power t_g = Re(kz_g)/Re(kzi) (|sx|^2+|sy|^2+|sz|^2), sz = -(kx sx + ky sy)/kz.
+
+    alternative.py:235-245 (kz in the exit medium, kzi in the incidence medium).
+    """
+    k0 = TWOPI / wavelength
+    kzi = np.conj(cmath.sqrt(k0 ** 2 * epsi - kp[0] ** 2 - kp[1] ** 2)) / k0
+    nh = len(c_out) // 2
+    sx, sy = c_out[:nh], c_out[nh:]
+    kx, ky, kz = k_vectors(gvec, kp, wavelength, eps_medium)
+    sz = -(kx * sx + ky * sy) / kz
+    t = kz.real / np.real(kzi) * (np.abs(sx) ** 2 + np.abs(sy) ** 2 + np.abs(sz) ** 2)
+    return np.sum(t), t
+
+
+# ---------------------------------------------------------------------------------------
+# Fields (khepri/fields.py, khepri/fourier.py:136-142)
+# ---------------------------------------------------------------------------------------
+def eigenbasis_matrix(w, v):
+    """[[W, W], [-V, V]]; fields.py:46-51."""
+    return np.block([[w, w], [-v, v]])
+
+
+def translate_mode_amplitudes(sl, sr, c1p):
+    """c+ = (I - Sl22 Sr11)^-1 Sl21 c1p, c- = Sr11 c+; fields.py:18-27."""
+    f = np.eye(len(c1p)) - sl[1, 1] @ sr[0, 0]
+    cp = np.linalg.solve(f, sl[1, 0] @ c1p)
+    return cp, sr[0, 0] @ cp
+
+
+def fourier_fields(ri, lam, r0, amps, zbar):
+    """RI (L o RI^-1 R0 c) with L = [exp(lam zbar), exp(-lam zbar)] clamped at |L| <= 1e14.
+
+    fields.py:53-62.
+    """
+    prop = np.concatenate([np.exp(lam * zbar), np.exp(-lam * zbar)])
+    big = np.abs(prop) > 1e14
+    prop[big] = prop[big] / (np.abs(prop[big]) / 1e14)
+    out = ri @ (prop * np.linalg.solve(ri, r0 @ np.concatenate(amps)))
+    return np.split(out, 4)
+
+
+def longitudinal_fields(sx, sy, ux, uy, kx, ky, ic):
+    """uz = -i(kx sy - ky sx); sz = -i IC (kx uy - ky ux); fields.py:68-76."""
+    uz = -1j * (kx * sy - ky * sx)
+    if np.ndim(ic) == 0:
+        sz = -1j * ic * (kx * uy - ky * ux)
+    else:
+        sz = -1j * ic @ (kx * uy - ky * ux)
+    return sz, uz
+
+
+def idft(coefs, kx, ky, x, y):
+    """sum_g c_g exp(i (kx_g x + ky_g y)) on the points (x, y); fourier.py:136-142."""
+    phase = np.exp(1j * (kx[:, None] * x.ravel()[None, :] + ky[:, None] * y.ravel()[None, :]))
+    return (coefs[:, None] * phase).sum(axis=0).reshape(x.shape)
+
+
+# ---------------------------------------------------------------------------------------
+# Crystal restatement (khepri/crystal.py)
+# ---------------------------------------------------------------------------------------
+class OracleCrystal:
+    """Stateful solver with the reference's Crystal method names and semantics.
+
+    khepri/crystal.py:42-400 (square / hexagonal / explicit lattices; uniform and pixmap layers;
+    half-space media epsi/epse).  Layers are solved once per unique name (crystal.py:183-186).
+    """
+
+    def __init__(self, pw, lattice="square", lattice_pitch=1, void=False, epsi=1, epse=1):
+        self.pw = tuple(pw)
+        self.lattice = lattice_vectors(lattice, lattice_pitch)
+        self.gvec = g_vectors(self.pw, self.lattice)
+        self.nh = self.pw[0] * self.pw[1]
+        self.void = void
+        self.epsi, self.epse = epsi, epse
+        self.layers = {}
+        self.source = None
+        self.S = None
+
+    def add_layer_uniform(self, name, epsilon, depth):
+        self.layers[name] = SimpleNamespace(kind="uniform", eps=epsilon, depth=depth, fields=False)
+
+    def add_layer_pixmap(self, name, epsilon, depth):
+        self.layers[name] = SimpleNamespace(kind="pixmap", eps=epsilon, depth=depth, fields=False)
+
+    def set_device(self, layers_stack, fields_mask=False):
+        """crystal.py:131-164."""
+        self.device_stack = list(layers_stack)
+        self.global_stacking = ([] if self.void else ["Sref"]) + list(layers_stack) + ([] if self.void else ["Strans"])
+        if not self.void:
+            self.layers.setdefault("Sref", SimpleNamespace(kind="inc", eps=self.epsi, depth=0, fields=True))
+            self.layers.setdefault("Strans", SimpleNamespace(kind="trn", eps=self.epse, depth=0, fields=True))
+        if isinstance(fields_mask, bool):
+            fields_mask = [fields_mask] * len(layers_stack)
+        self.stack_retain_mask = [True] + list(fields_mask) + [True]
+        for name, keep in zip(self.global_stacking, self.stack_retain_mask):
+            self.layers[name].fields |= keep
+
+    @property
+    def depth(self):
+        return sum(self.layers[n].depth for n in self.device_stack)
+
+    def set_source(self, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, kp=None):
+        """crystal.py:345-360."""
+        self.source = SimpleNamespace(te=te, tm=tm, theta=theta, phi=phi, wavelength=wavelength)
+        if kp is not None:
+            self.kp = (kp[0], kp[1])
+        else:
+            self.kp = tuple(compute_kplanar(self.epsi, wavelength, theta, phi))
+        self.k0 = TWOPI / wavelength
+        self.kzi = np.conj(cmath.sqrt(self.k0 ** 2 * self.epsi - self.kp[0] ** 2 - self.kp[1] ** 2))
+
+    def _solve_layer(self, layer, kx, ky, w0, v0, k0):
+        """layer.py:145-194."""
+        if layer.kind == "pixmap":
+            conv = convolution_matrix(layer.eps, self.pw)
+            layer.IC = np.linalg.inv(conv)
+            layer.W, layer.V, layer.L = solve_structured_layer(kx, ky, conv)
+            layer.S = build_scatmat(layer.W, layer.V, w0, v0, layer.L, layer.depth, k0)
+        elif layer.kind == "uniform":
+            layer.W, layer.V, layer.L = solve_uniform_layer(kx, ky, layer.eps)
+            layer.S = build_scatmat(layer.W, layer.V, w0, v0, layer.L, layer.depth, k0)
+            layer.IC = 1 / layer.eps
+        elif layer.kind == "inc":
+            layer.S, layer.W, layer.V, layer.L = scattering_reflection(kx, ky, w0, v0, layer.eps)
+            layer.IC = 1 / layer.eps
+        else:
+            layer.S, layer.W, layer.V, layer.L = scattering_transmission(kx, ky, w0, v0, layer.eps)
+            layer.IC = 1 / layer.eps
+
+    def solve(self):
+        """crystal.py:180-206."""
+        assert self.source is not None, "Call set_source before solving."
+        wl = self.source.wavelength
+        kx, ky, _ = k_vectors(self.gvec, self.kp, wl)
+        w0, v0 = free_space_eigenmodes(kx, ky)
+        for name in set(self.global_stacking):
+            self._solve_layer(self.layers[name], kx, ky, w0, v0, TWOPI / wl)
+        stacked = [self.layers[n] for n in self.global_stacking]
+        pos = list(np.cumsum([l.depth for l in stacked]))
+        pos[-1] = np.inf
+        if not self.void:
+            pos.insert(0, -np.inf)
+        self.stack_positions = pos
+        self.stacking_matrices, self.stacking_reverse_matrices, self.Stot = stack_layers(
+            [l.S for l in stacked], self.stack_retain_mask)
+        self.S = self.Stot
+
+    def poynting_flux_end(self, only_total=True):
+        """crystal.py:363-396 (W_ref = I, so c1p = inc)."""
+        assert self.S is not None, "Call solve first"
+        wl = self.source.wavelength
+        inc = incident(self.pw, self.source.te, self.source.tm, (self.kp[0], self.kp[1], self.kzi))
+        w_ref, w_trn = self.layers["Sref"].W, self.layers["Strans"].W
+        c1p = np.linalg.inv(w_ref) @ inc
+        t = poynting_fluxes(self.gvec, w_trn @ self.Stot[1, 0] @ c1p, self.kp, wl, self.epsi, self.epse)
+        r = poynting_fluxes(self.gvec, w_ref @ self.Stot[0, 0] @ c1p, self.kp, wl, self.epsi, self.epsi)
+        if only_total:
+            return r[0].real, t[0].real
+        return r, t
+
+    # -- fields -------------------------------------------------------------------------
+    def _locate(self, z):
+        """crystal.py:208-232."""
+        idx = int(np.searchsorted(self.stack_positions, z)) - 1
+        zr = z if z <= 0 else z - self.stack_positions[idx]
+        return self.layers[self.global_stacking[idx]], idx, zr
+
+    def _fourier_fields(self, z, inc_fields):
+        """crystal.py:234-279."""
+        layer, idx, zr = self._locate(z)
+        assert layer.fields, f"Layer at {z} did not store eigenspace."
+        wl = self.source.wavelength
+        k0 = TWOPI / wl
+        kx, ky, _ = k_vectors(self.gvec, self.kp, wl)
+        w0, v0 = free_space_eigenmodes(kx, ky)
+        ri = eigenbasis_matrix(layer.W, layer.V)
+        r0 = eigenbasis_matrix(w0, v0)
+        rref = eigenbasis_matrix(self.layers["Sref"].W, self.layers["Sref"].V)
+        n = 2 * self.nh
+        c1p = np.linalg.solve(rref, inc_fields)[:n]
+        cp, cm = translate_mode_amplitudes(self.stacking_matrices[idx], self.stacking_reverse_matrices[idx], c1p)
+        sx, sy, ux, uy = fourier_fields(ri, layer.L, r0, (cp, cm), k0 * (layer.depth - zr))
+        sz, uz = longitudinal_fields(sx, sy, ux, uy, kx, ky, layer.IC)
+        return sx, sy, sz, ux, uy, uz
+
+    def source_fields(self):
+        """crystal.py:281-295: (E, H) source vectors with H = 0."""
+        e = incident(self.pw, self.source.te, self.source.tm, (self.kp[0], self.kp[1], self.kzi))
+        return e, np.zeros_like(e)
+
+    def fields_coords_xy(self, x, y, z, incident_fields=None):
+        """crystal.py:297-333."""
+        x, y = np.asarray(x), np.asarray(y)
+        assert x.shape == y.shape and x.ndim == 2, "x and y must be 2D meshgrids"
+        assert self.S is not None, "Call solve first."
+        if incident_fields is None:
+            incident_fields = np.concatenate(self.source_fields())
+        elif isinstance(incident_fields, tuple):
+            incident_fields = np.concatenate(incident_fields)
+        wl = self.source.wavelength
+        k0 = TWOPI / wl
+        kx, ky, _ = k_vectors(self.gvec, self.kp, wl)
+        ff = self._fourier_fields(z, incident_fields)
+        out = np.asarray([idft(s, k0 * kx, k0 * ky, x, y) for s in ff])
+        return out[:3], out[3:]
+
+    def fields_volume(self, x, y, z, incident_fields=None):
+        """crystal.py:335-343: E, H of shape [Nz, 3, X, Y]."""
+        if incident_fields is None:
+            incident_fields = self.source_fields()
+        inc = np.concatenate(incident_fields)
+        res = [self.fields_coords_xy(x, y, zi, inc) for zi in z]
+        return np.asarray([r[0] for r in res]), np.asarray([r[1] for r in res])
+
+
+def solve_rt(pw, layers, stack, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, kp=None,
+             lattice="square", epsi=1, epse=1, only_total=True):
+    """Convenience wrapper: build a Crystal, solve once, return poynting_flux_end()."""
+    cl = OracleCrystal(pw, lattice=lattice, epsi=epsi, epse=epse)
+    for name, (kind, eps, depth) in layers.items():
+        if kind == "uniform":
+            cl.add_layer_uniform(name, eps, depth)
+        else:
+            cl.add_layer_pixmap(name, eps, depth)
+    cl.set_device(stack, False)
+    cl.set_source(wavelength, te, tm, theta, phi, kp)
+    cl.solve()
+    return cl.poynting_flux_end(only_total)

@@ -1,0 +1,192 @@
+"""Generate golden vectors by running the reference (Kaeryv/Khepri) on seeded inputs.
+
+Run in a container where the reference source is available (read-only):
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference imports numba at module load; ``tests/golden/_shim`` provides an identity
+``njit`` (the decorated functions are not on the Crystal solve path).  Inputs come from
+``khepri_gb300.workloads`` (deterministic, seeded) or are stored in the fixture itself; each
+fixture holds the reference's outputs for them.  The fixtures are small (< 1 MB each) and are
+the pins for the oracle (tests/test_oracle_golden.py) and for the GPU parity tests.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def _import_reference(ref_root):
+    sys.path.insert(0, os.path.join(HERE, "_shim"))
+    sys.path.insert(0, ref_root)
+    from khepri.crystal import Crystal  # noqa: E402
+    from khepri.draw import Drawing  # noqa: E402
+    from khepri import tools  # noqa: E402
+    return Crystal, Drawing, tools
+
+
+def _crystal(Crystal, st_pw, layers, stack, mask=False, lattice="square", epsi=1, epse=1):
+    cl = Crystal(st_pw, lattice=lattice, epsi=epsi, epse=epse)
+    for name, (kind, eps, depth) in layers.items():
+        if kind == "uniform":
+            cl.add_layer_uniform(name, eps, depth)
+        else:
+            cl.add_layer_pixmap(name, eps, depth)
+    cl.set_device(stack, mask)
+    return cl
+
+
+def main(ref_root):
+    sys.path.insert(0, ROOT)
+    from khepri_gb300 import workloads as wk
+
+    Crystal, Drawing, tools = _import_reference(ref_root)
+    t0 = time.time()
+
+    # A. thin lossy film, test/integration/test_complex_eps.py:13-42 (1x1 harmonics).
+    c, e0, sigma, h = 299792458, 8.85418782e-12, 0.01e6, 1.2
+    wls = np.linspace(0.7, 2.0)
+    R, T, EPS = [], [], []
+    for wl in wls:
+        omega = np.pi * 2 * (c / 1e-6) / wl
+        eps = 1.6 ** 2 - 1j * sigma / omega / e0
+        cl = Crystal((1, 1))
+        cl.add_layer_uniform("1", eps, h)
+        cl.set_device(["1"])
+        cl.set_source(wl, 1, 1)
+        cl.solve()
+        r, t = cl.poynting_flux_end()
+        R.append(r); T.append(t); EPS.append(eps)
+    np.savez_compressed(os.path.join(HERE, "fresnel_1x1.npz"), wavelength=wls, eps=np.array(EPS),
+                        depth=h, R=np.array(R), T=np.array(T))
+
+    # B. plain 5x5 sweep, 151 frequencies (examples/crystal_api/test_crystal.py:23-43 at 128^2).
+    d = Drawing((128, 128), 12)
+    d.disc((0.0, 0.0), 0.4, 1.0)
+    canvas = d.canvas()
+    sw = wk.plain_sweep()
+    assert np.array_equal(canvas, sw.structure.layers["Scyl"][1]), "disc_canvas disagrees with Drawing"
+    cl = _crystal(Crystal, (5, 5), sw.structure.layers, sw.structure.stack, [True] * 3)
+    R, T = [], []
+    stots = {}
+    for i, wl in enumerate(sw.wavelengths):
+        cl.set_source(wl, 1.0, 0, 0.0, 0.0)
+        cl.solve()
+        r, t = cl.poynting_flux_end()
+        R.append(r); T.append(t)
+        if i in (0, 75):
+            stots[i] = cl.Stot.copy()
+            if i == 75:
+                s_cyl = cl.layers["Scyl"].S.copy()
+                lam_cyl = cl.layers["Scyl"].L.copy()
+                s_u = cl.layers["S1"].S.copy()
+                s_ref = cl.layers["Sref"].S.copy()
+                s_trn = cl.layers["Strans"].S.copy()
+    np.savez_compressed(os.path.join(HERE, "plain_5x5.npz"), wavelength=sw.wavelengths, R=np.array(R),
+                        T=np.array(T), stot_0=stots[0], stot_75=stots[75], s_cyl_75=s_cyl, lam_cyl_75=lam_cyl,
+                        s_uniform_75=s_u, s_ref_75=s_ref, s_trn_75=s_trn)
+
+    # C. fields of the plain structure at wl = 2.04 (examples/crystal_api/test_crystal.py:49-57).
+    cl.set_source(2.04, 1.0, 0.0, 0, 0)
+    cl.solve()
+    xs = np.linspace(0, 1, 6)
+    ys = np.linspace(0, 1, 5)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    Z = np.array([-0.3, 0.0, 0.2, 0.55, 0.9, 1.65, 2.0, 2.4])
+    E, H = cl.fields_volume(X, Y, Z)
+    np.savez_compressed(os.path.join(HERE, "fields_5x5.npz"), wavelength=2.04, x=X, y=Y, z=Z, E=E, H=H)
+
+    # D. oblique incidence, both polarisations, per-order output, multi-disc map, non-unit media.
+    rng = np.random.default_rng(7)
+    emap = wk.multi_disc_map(rng, n=48)
+    layers = {"P1": ("pixmap", emap, 0.31), "U1": ("uniform", 2.2, 0.45), "P2": ("pixmap", emap, 0.27),
+              "U2": ("uniform", 3.1 - 0.05j, 0.2), "P3": ("pixmap", emap, 0.6)}
+    stack = ["P1", "U1", "P2", "U2", "P3"]
+    cases = []
+    for (epsi, epse) in [(1.0, 1.0), (2.25, 1.5)]:
+        cl = _crystal(Crystal, (5, 5), layers, stack, False, epsi=epsi, epse=epse)
+        for (wl, te, tm, theta, phi) in [(1.9, 1.0, 0.0, 0.0, 0.0), (1.9, 0.0, 1.0, 0.0, 0.0),
+                                         (2.3, 1.0, 0.0, 17.0, 30.0), (2.3, 0.0, 1.0, 17.0, 30.0),
+                                         (1.6, 0.6, 0.8, 35.0, -60.0)]:
+            cl.set_source(wl, te, tm, theta, phi)
+            cl.solve()
+            (r, ro), (t, to) = cl.poynting_flux_end(only_total=False)
+            cases.append((epsi, epse, wl, te, tm, theta, phi, r.real, t.real, ro.real, to.real))
+    arr = lambda k: np.array([cs[k] for cs in cases])
+    np.savez_compressed(os.path.join(HERE, "oblique_5x5.npz"), eps_map=emap,
+                        depths=np.array([0.31, 0.45, 0.27, 0.2, 0.6]), eps_u=np.array([2.2, 3.1 - 0.05j]),
+                        epsi=arr(0), epse=arr(1), wavelength=arr(2), te=arr(3), tm=arr(4), theta=arr(5),
+                        phi=arr(6), R=arr(7), T=arr(8), r_orders=arr(9), t_orders=arr(10))
+
+    # E. hexagonal lattice, 3x3, explicit kp.
+    dh = Drawing((64, 64), 4.0)
+    dh.disc((0.0, 0.0), 0.3, 1.0)
+    cl = _crystal(Crystal, (3, 3), {"H": ("pixmap", dh.canvas(), 0.4)}, ["H"], False, lattice="hexagonal")
+    hx = []
+    for wl, kp in [(1.4, (0.0, 0.0)), (1.2, (0.5, -0.3)), (0.95, (1.1, 0.4))]:
+        cl.set_source(wl, 1.0, 1.0, kp=kp)
+        cl.solve()
+        hx.append((wl, kp[0], kp[1]) + tuple(cl.poynting_flux_end()))
+    hx = np.array(hx)
+    np.savez_compressed(os.path.join(HERE, "hex_3x3.npz"), eps_map=dh.canvas(), wavelength=hx[:, 0],
+                        kp=hx[:, 1:3], R=hx[:, 3], T=hx[:, 4])
+
+    # F. uneven batch, small maps (lossy, absorption = 1 - R - T).
+    structs = wk.uneven_structures(8, seed=3, n_pix=32, max_pw=9, max_layers=4)
+    out = {}
+    for i, (st, wl, kp) in enumerate(structs):
+        cl = _crystal(Crystal, st.pw, st.layers, st.stack, False)
+        cl.set_source(wl, 1.0, 1.0, kp=tuple(kp))
+        cl.solve()
+        r, t = cl.poynting_flux_end()
+        out[f"R_{i}"] = r; out[f"T_{i}"] = t
+    np.savez_compressed(os.path.join(HERE, "uneven_small.npz"), count=8, seed=3, n_pix=32, max_pw=9,
+                        max_layers=4, R=np.array([out[f"R_{i}"] for i in range(8)]),
+                        T=np.array([out[f"T_{i}"] for i in range(8)]))
+
+    # G. the 11x11 batched-sweep structure (seed 0, full 256^2 map), a few (f, k) problems.
+    st = wk.batched_structure(0)
+    wl_all, kp_all = wk.batched_problems()
+    pick = np.array([16 * 32 + 16, 20 * 1024 + 15 * 32 + 17, 40 * 1024 + 300, 63 * 1024 + 1023])
+    cl = _crystal(Crystal, st.pw, st.layers, st.stack, False)
+    Rte, Tte, Rtm, Ttm = [], [], [], []
+    for p in pick:
+        for (te, tm, RR, TT) in [(1.0, 0.0, Rte, Tte), (0.0, 1.0, Rtm, Ttm)]:
+            cl.set_source(wl_all[p], te, tm, kp=tuple(kp_all[p]))
+            cl.solve()
+            r, t = cl.poynting_flux_end()
+            RR.append(r); TT.append(t)
+    np.savez_compressed(os.path.join(HERE, "batched_11x11.npz"), seed=0, problems=pick,
+                        map_sum=st.layers["P1"][1].sum(), R_te=np.array(Rte), T_te=np.array(Tte),
+                        R_tm=np.array(Rtm), T_tm=np.array(Ttm))
+
+    # H. convolution matrix of a non-square complex map, non-square harmonic set.
+    rng = np.random.default_rng(11)
+    cmap = rng.uniform(1, 5, size=(20, 14)) - 1j * rng.uniform(0, 0.2, size=(20, 14))
+    conv = tools.convolution_matrix(cmap, (5, 3))
+    np.savez_compressed(os.path.join(HERE, "convmat.npz"), eps_map=cmap, pw=np.array([5, 3]), C=conv)
+
+    # I. inverse-design structures (9x9), zeroth-order transmission.
+    thetas, dstructs, freqs = wk.inverse_design(2, seed=0)
+    res = []
+    for st in dstructs:
+        cl = _crystal(Crystal, st.pw, st.layers, st.stack, False)
+        for f in freqs[[0, 7, 15]]:
+            cl.set_source(1.0 / f, 1.0, 0.0, 0.0, 0.0)
+            cl.solve()
+            (r, ro), (t, to) = cl.poynting_flux_end(only_total=False)
+            res.append((f, r.real, t.real, to[(81 - 1) // 2].real))
+    res = np.array(res)
+    np.savez_compressed(os.path.join(HERE, "design_9x9.npz"), count=2, seed=0, freq=res[:, 0], R=res[:, 1],
+                        T=res[:, 2], t0=res[:, 3])
+    print(f"golden vectors written in {time.time() - t0:.1f} s")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,143 @@
+"""Pin the CPU oracle to golden vectors made by running the reference on the same inputs."""
+import numpy as np
+import pytest
+
+from oracle import khepri_oracle as ko
+from khepri_gb300 import workloads as wk
+
+
+def _solve(pw, layers, stack, wl, te, tm, theta=0.0, phi=0.0, kp=None, lattice="square", epsi=1, epse=1,
+           only_total=True):
+    return ko.solve_rt(pw, layers, stack, wl, te, tm, theta, phi, kp, lattice, epsi, epse, only_total)
+
+
+def test_fresnel_film_known_answer(golden):
+    """The reference's own known-answer test (test/integration/test_complex_eps.py:13-42)."""
+    g = golden("fresnel_1x1")
+    R = []
+    for wl, eps in zip(g["wavelength"], g["eps"]):
+        r, t = _solve((1, 1), {"1": ("uniform", eps, float(g["depth"]))}, ["1"], wl, 1, 1)
+        R.append(r)
+    R = np.array(R)
+    np.testing.assert_allclose(R, g["R"], rtol=1e-10, atol=1e-13)
+    wls = g["wavelength"]
+    eps_c = np.conj(g["eps"])
+    n2 = np.conj(np.sqrt(eps_c))
+    r12 = (1 - n2) / (1 + n2)
+    r23 = (n2 - 1) / (n2 + 1)
+    ph = np.exp(-2j * 2 * np.pi / wls * n2 * float(g["depth"]))
+    fres = np.abs((r12 + r23 * ph) / (1 + r12 * r23 * ph)) ** 2
+    np.testing.assert_allclose(R, fres, rtol=1e-7)
+
+
+def test_convolution_matrix(golden):
+    g = golden("convmat")
+    C = ko.convolution_matrix(g["eps_map"], tuple(g["pw"]))
+    np.testing.assert_allclose(C, g["C"], rtol=0, atol=1e-14)
+
+
+def test_plain_sweep_rt(golden):
+    g = golden("plain_5x5")
+    sw = wk.plain_sweep()
+    cl = ko.OracleCrystal((5, 5))
+    for name, (kind, eps, depth) in sw.structure.layers.items():
+        (cl.add_layer_uniform if kind == "uniform" else cl.add_layer_pixmap)(name, eps, depth)
+    cl.set_device(sw.structure.stack, [True] * 3)
+    idx = np.arange(0, 151, 10)
+    for i in idx:
+        cl.set_source(sw.wavelengths[i], 1.0, 0, 0.0, 0.0)
+        cl.solve()
+        r, t = cl.poynting_flux_end()
+        assert abs(r - g["R"][i]) < 1e-10 and abs(t - g["T"][i]) < 1e-10
+        if i == 0:
+            np.testing.assert_allclose(cl.Stot, g["stot_0"], atol=1e-10)
+    np.testing.assert_allclose(g["R"] + g["T"], 1.0, atol=1e-10)
+
+
+def test_plain_layer_smatrices(golden):
+    g = golden("plain_5x5")
+    sw = wk.plain_sweep()
+    cl = ko.OracleCrystal((5, 5))
+    for name, (kind, eps, depth) in sw.structure.layers.items():
+        (cl.add_layer_uniform if kind == "uniform" else cl.add_layer_pixmap)(name, eps, depth)
+    cl.set_device(sw.structure.stack, [True] * 3)
+    cl.set_source(sw.wavelengths[75], 1.0, 0, 0.0, 0.0)
+    cl.solve()
+    np.testing.assert_allclose(cl.layers["Scyl"].S, g["s_cyl_75"], atol=1e-10)
+    np.testing.assert_allclose(cl.layers["S1"].S, g["s_uniform_75"], atol=1e-12)
+    np.testing.assert_allclose(cl.layers["Sref"].S, g["s_ref_75"], atol=1e-12)
+    np.testing.assert_allclose(cl.layers["Strans"].S, g["s_trn_75"], atol=1e-12)
+    np.testing.assert_allclose(np.sort_complex(cl.layers["Scyl"].L), np.sort_complex(g["lam_cyl_75"]), atol=1e-10)
+    np.testing.assert_allclose(cl.Stot, g["stot_75"], atol=1e-10)
+
+
+def test_fields(golden):
+    g = golden("fields_5x5")
+    sw = wk.plain_sweep()
+    cl = ko.OracleCrystal((5, 5))
+    for name, (kind, eps, depth) in sw.structure.layers.items():
+        (cl.add_layer_uniform if kind == "uniform" else cl.add_layer_pixmap)(name, eps, depth)
+    cl.set_device(sw.structure.stack, [True] * 3)
+    cl.set_source(float(g["wavelength"]), 1.0, 0.0, 0, 0)
+    cl.solve()
+    E, H = cl.fields_volume(g["x"], g["y"], g["z"])
+    scale = np.abs(g["E"]).max()
+    np.testing.assert_allclose(E, g["E"], atol=1e-9 * scale)
+    np.testing.assert_allclose(H, g["H"], atol=1e-9 * np.abs(g["H"]).max())
+
+
+def test_oblique_orders(golden):
+    g = golden("oblique_5x5")
+    emap, d, eu = g["eps_map"], g["depths"], g["eps_u"]
+    layers = {"P1": ("pixmap", emap, d[0]), "U1": ("uniform", eu[0], d[1]), "P2": ("pixmap", emap, d[2]),
+              "U2": ("uniform", eu[1], d[3]), "P3": ("pixmap", emap, d[4])}
+    stack = ["P1", "U1", "P2", "U2", "P3"]
+    for i in range(len(g["R"])):
+        (r, ro), (t, to) = _solve((5, 5), layers, stack, g["wavelength"][i], g["te"][i], g["tm"][i],
+                                  g["theta"][i], g["phi"][i], epsi=g["epsi"][i], epse=g["epse"][i],
+                                  only_total=False)
+        assert abs(r - g["R"][i]) < 1e-10 and abs(t - g["T"][i]) < 1e-10
+        np.testing.assert_allclose(ro, g["r_orders"][i], atol=1e-10)
+        np.testing.assert_allclose(to, g["t_orders"][i], atol=1e-10)
+
+
+def test_hexagonal(golden):
+    g = golden("hex_3x3")
+    for i in range(len(g["R"])):
+        r, t = _solve((3, 3), {"H": ("pixmap", g["eps_map"], 0.4)}, ["H"], g["wavelength"][i], 1.0, 1.0,
+                      kp=tuple(g["kp"][i]), lattice="hexagonal")
+        assert abs(r - g["R"][i]) < 1e-10 and abs(t - g["T"][i]) < 1e-10
+
+
+def test_uneven_lossy(golden):
+    g = golden("uneven_small")
+    structs = wk.uneven_structures(int(g["count"]), seed=int(g["seed"]), n_pix=int(g["n_pix"]),
+                                   max_pw=int(g["max_pw"]), max_layers=int(g["max_layers"]))
+    for i, (st, wl, kp) in enumerate(structs):
+        r, t = _solve(st.pw, st.layers, st.stack, wl, 1.0, 1.0, kp=tuple(kp))
+        assert abs(r - g["R"][i]) < 1e-9 and abs(t - g["T"][i]) < 1e-9
+        assert r + t < 1.0  # lossy: Im eps < 0
+
+
+def test_inverse_design_zeroth_order(golden):
+    g = golden("design_9x9")
+    _, structs, freqs = wk.inverse_design(int(g["count"]), seed=int(g["seed"]))
+    k = 0
+    for st in structs:
+        for f in freqs[[0, 7, 15]]:
+            (r, _), (t, to) = _solve(st.pw, st.layers, st.stack, 1.0 / f, 1.0, 0.0, only_total=False)
+            assert abs(f - g["freq"][k]) < 1e-15
+            assert abs(r - g["R"][k]) < 1e-9 and abs(t - g["T"][k]) < 1e-9
+            assert abs(to[40] - g["t0"][k]) < 1e-9
+            k += 1
+
+
+@pytest.mark.slow
+def test_batched_11x11_points(golden):
+    g = golden("batched_11x11")
+    st = wk.batched_structure(int(g["seed"]))
+    assert abs(st.layers["P1"][1].sum() - float(g["map_sum"])) == 0
+    wl, kp = wk.batched_problems()
+    for j, p in enumerate(g["problems"][:2]):
+        r, t = _solve(st.pw, st.layers, st.stack, wl[p], 1.0, 0.0, kp=tuple(kp[p]))
+        assert abs(r - g["R_te"][j]) < 1e-9 and abs(t - g["T_te"][j]) < 1e-9
