@@ -1,0 +1,171 @@
+/*
+ * khepri_gb300.h — C ABI of libkhp, the GB300 (sm_103a) kernels of the Crystal RCWA solve.
+ *
+ * Conventions
+ *   - Complex numbers are pairs of doubles (re, im): the memory layout of numpy / torch
+ *     complex128.  A "complex pointer" below is a `double*` to such pairs.
+ *   - Matrices are row-major and contiguous; batches are contiguous along the leading axis.
+ *     n = 2 * nh, nh = px * py harmonics.  An S-matrix is [2][2][n][n] (S11, S12, S21, S22),
+ *     the layout of the reference's np.array([[S11, S12], [S21, S22]]).
+ *   - Every pointer is a DEVICE pointer.  Every call is asynchronous on `stream` (a
+ *     cudaStream_t, NULL = legacy default stream) and returns 0 (KHP_OK) or an error code;
+ *     khp_status_string() names it.  Per-problem status words (int32, OR-ed flags
+ *     1 = singular pivot, 2 = eigensolver not converged, 4 = non-finite value) are written
+ *     to device arrays and are never turned into traps.
+ *   - No call allocates device memory: scratch comes from the caller through `workspace`
+ *     (size from the matching *_workspace function, 256-byte aligned base).
+ *   - Calls are reentrant per stream and hold no host-global state.
+ *
+ * The reference (Kaeryv/Khepri) is a numpy library; each entry point below replaces the
+ * reference function named beside it (file:line in that project).
+ */
+#ifndef KHEPRI_GB300_H
+#define KHEPRI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KHP_OK 0
+#define KHP_ERR_INVALID_ARG 1
+#define KHP_ERR_WORKSPACE 2
+#define KHP_ERR_CUDA 3
+#define KHP_ERR_SINGULAR 4
+#define KHP_ERR_NOT_CONVERGED 5
+#define KHP_ERR_NONFINITE 6
+#define KHP_ERR_TOO_LARGE 7
+
+/* Library version as major*10000 + minor*100 + patch. */
+int khp_version(void);
+/* Static description of an error code or of a per-problem status word. */
+const char* khp_status_string(int code);
+
+/*
+ * Convolution (Toeplitz) matrices of pixmaps.  Replaces tools.convolution_matrix
+ * (khepri/tools.py:33-56): C[r][c] = eps_hat(p_r - p_c, q_r - q_c) with r = q*px + p and
+ * eps_hat(dx, dy) = (1/(nx*ny)) sum_{x,y} eps[x][y] exp(-2 pi i (dx x/nx + dy y/ny)),
+ * the fftshift(fft2(eps))/(nx*ny) coefficients the reference gathers.
+ *   eps:  complex [nmaps][nx][ny] (axis 0 = x);  conv: complex [nmaps][nh][nh].
+ * Requires nx >= 2*px - 1 and ny >= 2*py - 1 (the reference's index range), ny <= 8192.
+ */
+size_t khp_convmat_workspace(int64_t nmaps, int32_t px, int32_t py);
+int khp_convmat(int64_t nmaps, int64_t nx, int64_t ny, const double* eps, int32_t px, int32_t py, double* conv,
+                void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Per-structure preparation of a patterned layer (done once, reused for every wavelength and
+ * k-point): ic = C^-1 (the reference's Layer.IC, khepri/layer.py:158) and the products
+ * hx = C^-1 diag(gx) C, hy = C^-1 diag(gy) C that make P*Q assemble in O(n^2) per problem.
+ *   conv, ic, hx, hy: complex [nmaps][nh][nh];  gx, gy: real [nh] (G vectors, absolute units).
+ */
+size_t khp_structure_prep_workspace(int64_t nmaps, int32_t nh);
+int khp_structure_prep(int64_t nmaps, int32_t nh, const double* conv, const double* gx, const double* gy, double* ic,
+                       double* hx, double* hy, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Eigenmodes of patterned layers for a batch of problems.  Replaces
+ * alternative.solve_structured_layer (khepri/alternative.py:158-178):
+ * (lam^2, W) = eig(P Q), lam = principal sqrt(lam^2), V = Q W / lam.
+ *   map_index: int32 [batch] structure of each problem (into conv/hx/hy, [nmaps][nh][nh]);
+ *   kp: complex [batch][2] in-plane wavevector (absolute); k0: real [batch] = 2 pi / wavelength;
+ *   W, V: complex [batch][n][n];  lam: complex [batch][n];  status: int32 [batch].
+ */
+size_t khp_layer_modes_workspace(int64_t batch, int32_t nh);
+int khp_layer_modes(int64_t batch, int32_t nh, const int32_t* map_index, const double* conv, const double* hx,
+                    const double* hy, const double* gx, const double* gy, const double* kp, const double* k0,
+                    double* W, double* V, double* lam, int32_t* status, void* workspace, size_t ws_bytes,
+                    void* stream);
+
+/*
+ * S-matrix of a layer of thickness depth[b] between free-space gaps.  Replaces
+ * alternative.build_scatmat (khepri/alternative.py:181-195) with W0 = I and V0 the free-space
+ * modes of alternative.free_space_eigenmodes (alternative.py:84-99).
+ *   W, V: complex [batch][n][n];  lam: complex [batch][n];  depth, k0: real [batch];
+ *   S: complex [batch][2][2][n][n].
+ */
+size_t khp_layer_smatrix_workspace(int64_t batch, int32_t nh);
+int khp_layer_smatrix(int64_t batch, int32_t nh, const double* W, const double* V, const double* lam,
+                      const double* depth, const double* gx, const double* gy, const double* kp, const double* k0,
+                      double* S, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Closed-form S-matrices of homogeneous media (per-harmonic 2x2 algebra, no dense solve).
+ * kind 0: uniform layer (alternative.solve_uniform_layer + build_scatmat, alternative.py:130-156,
+ *         181-195); kind 1: incidence half-space (alternative.scattering_reflection, :32-56);
+ *         kind 2: emergence half-space (alternative.scattering_transmission, :59-82).
+ *   eps: complex [batch];  depth: real [batch] (ignored for kinds 1, 2);
+ *   S: complex [batch][2][2][n][n];  W, V: complex [batch][n][n] or NULL;  lam: complex [batch][n] or NULL.
+ */
+int khp_closed_form_smatrix(int64_t batch, int32_t nh, int32_t kind, const double* eps, const double* depth,
+                            const double* gx, const double* gy, const double* kp, const double* k0, double* S,
+                            double* W, double* V, double* lam, int32_t* status, void* stream);
+
+/*
+ * Redheffer star product S = SA * SB.  Replaces alternative.redheffer_product
+ * (khepri/alternative.py:19-30).  One LU of D = I - SB11 SA22 serves all four blocks
+ * (F^-1 = I + SA22 D^-1 SB11).  sa_stride / sb_stride: batch strides in complex elements
+ * (0 broadcasts one matrix to the whole batch).  S must not alias SA or SB.
+ */
+size_t khp_star_product_workspace(int64_t batch, int32_t n);
+int khp_star_product(int64_t batch, int32_t n, const double* SA, int64_t sa_stride, const double* SB,
+                     int64_t sb_stride, double* S, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Reflected and transmitted power.  Replaces Crystal.poynting_flux_end
+ * (khepri/crystal.py:363-396) with the source vector of alternative.incident
+ * (alternative.py:101-128) and alternative.poynting_fluxes (alternative.py:235-245).
+ *   S: complex [batch][2][2][n][n] global S-matrix (s_stride: batch stride in complex elements);
+ *   te, tm: complex [batch] polarisation weights;  epsi, epse: complex scalars (host values);
+ *   R, T: real [batch];  r_orders, t_orders: real [batch][nh] or NULL.
+ * Evanescent incidence (Re kz_inc = 0) yields NaN, as in the reference.
+ */
+int khp_flux(int64_t batch, int32_t px, int32_t py, const double* S, int64_t s_stride, const double* gx,
+             const double* gy, const double* kp, const double* k0, const double* te, const double* tm, double epsi_re,
+             double epsi_im, double epse_re, double epse_im, double* R, double* T, double* r_orders, double* t_orders,
+             void* stream);
+
+/*
+ * Field reconstruction (Crystal.fields_coords_xy / fields_volume, khepri/crystal.py:234-343).
+ *
+ * khp_fields_amplitudes — one solved problem; for each of nlayers layers l (arrays of device
+ * pointers, one entry per layer): forward-chain S at l (sl_ptrs, [2][2][n][n]), reverse-chain
+ * S at l (sr_ptrs), the layer's W and V ([n][n]).  vref: V of the incidence half-space [n][n];
+ * inc: complex [2n] incident (E; H) Fourier vector; kp: complex [2]; k0: real [1].
+ * Output amps: complex [nlayers][2n] = RI^-1 R0 [c+; c-], with c+- from
+ * fields.translate_mode_amplitudes (khepri/fields.py:18-27) and c1p from Crystal._fourier_fields
+ * (crystal.py:259-264).  status: int32 [1], OR-ed flags.
+ */
+size_t khp_fields_amplitudes_workspace(int64_t nlayers, int32_t nh);
+int khp_fields_amplitudes(int64_t nlayers, int32_t nh, const int64_t* sl_ptrs, const int64_t* sr_ptrs,
+                          const int64_t* w_ptrs, const int64_t* v_ptrs, const double* vref, const double* inc,
+                          const double* gx, const double* gy, const double* kp, const double* k0, double* amps,
+                          int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Fourier-space fields at nz depths (khepri/fields.py:53-76): for depth z in slot s = slot_of_z[z],
+ * f = RI (L o amps[s]) with L = [exp(lam zbar), exp(-lam zbar)] clamped to modulus <= 1e14,
+ * then sz = -i IC (kx uy - ky ux), uz = -i (kx sy - ky sx).  ic_ptrs[s] points to the layer's
+ * C^-1 ([nh][nh]) or is 0, in which case the complex scalar ic_scalar[s] (= 1/eps) is used.
+ * zbar: real [nz] = k0 (depth - z_rel).  ff: complex [nz][6][nh] = (sx, sy, sz, ux, uy, uz).
+ */
+int khp_fields_fourier(int64_t nz, int32_t nh, const int32_t* slot_of_z, const double* zbar, const int64_t* w_ptrs,
+                       const int64_t* v_ptrs, const int64_t* lam_ptrs, const int64_t* ic_ptrs, const double* ic_scalar,
+                       const double* amps, const double* gx, const double* gy, const double* kp, const double* k0,
+                       double* ff, void* stream);
+
+/*
+ * Inverse Fourier sum to real space, khepri/fourier.py:136-142 (idft):
+ * out[r][p] = sum_g ff[r][g] exp(i ((kp_x + gx_g) x_p + (kp_y + gy_g) y_p)).
+ * ff: complex [rows][nh]; x, y: real [npts]; kp: complex [2]; out: complex [rows][npts].
+ */
+int khp_fields_idft(int64_t rows, int32_t nh, const double* ff, const double* gx, const double* gy, const double* kp,
+                    int64_t npts, const double* x, const double* y, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KHEPRI_GB300_H */

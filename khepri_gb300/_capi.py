@@ -1,0 +1,107 @@
+"""ctypes binding of libkhp (include/khepri_gb300.h).
+
+The library is the only compute path: if it is missing or no CUDA device is present the
+calls fail loudly (ImportError / KhpError); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import torch
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libkhp.so")
+
+_c_i64 = ctypes.c_int64
+_c_i32 = ctypes.c_int32
+_c_p = ctypes.c_void_p
+_c_sz = ctypes.c_size_t
+_c_d = ctypes.c_double
+
+_SIGNATURES = {
+    "khp_version": (ctypes.c_int, []),
+    "khp_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "khp_convmat_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32]),
+    "khp_convmat": (ctypes.c_int, [_c_i64, _c_i64, _c_i64, _c_p, _c_i32, _c_i32, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_structure_prep_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_structure_prep": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz,
+                                          _c_p]),
+    "khp_layer_modes_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_layer_modes": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                       _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_layer_smatrix_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_layer_smatrix": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                         _c_p, _c_sz, _c_p]),
+    "khp_closed_form_smatrix": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                               _c_p, _c_p, _c_p, _c_p]),
+    "khp_star_product_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_star_product": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_flux": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_d, _c_d,
+                                _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p]),
+    "khp_fields_amplitudes_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_fields_amplitudes": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                             _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_fields_fourier": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                          _c_p, _c_p, _c_p, _c_p]),
+    "khp_fields_idft": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p]),
+}
+
+_lib = None
+
+
+class KhpError(RuntimeError):
+    """A libkhp call or a per-problem status reported a failure."""
+
+
+def load():
+    """Load libkhp.so (built by khepri_gb300.build) and declare its C signatures."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libkhp is not built ({LIB_PATH} missing): run khepri_gb300.build.build()")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def exported_symbols():
+    """Names of the C entry points this binding declares."""
+    return sorted(_SIGNATURES)
+
+
+def status_string(code: int) -> str:
+    return load().khp_status_string(int(code)).decode()
+
+
+def check(code: int, what: str):
+    if code != 0:
+        raise KhpError(f"{what} failed: {status_string(code)} (code {code})")
+
+
+def ptr(t):
+    """Device pointer of a tensor (None -> NULL)."""
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise KhpError("libkhp needs a CUDA device; none is available (there is no CPU fallback)")
+    load()
+
+
+STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-finite value"}
+
+
+def decode_status(word: int) -> str:
+    return ", ".join(v for k, v in STATUS_BITS.items() if word & k) or "ok"

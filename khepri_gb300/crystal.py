@@ -1,0 +1,212 @@
+"""Drop-in ``Crystal`` for the reference's Crystal RCWA solve path, computed by libkhp on the GPU.
+
+Method names, arguments, return values and error behaviour follow khepri/crystal.py:34-406:
+``add_layer_uniform``, ``add_layer_pixmap``, ``add_pixmap_or_uniform``, ``add_layer``,
+``set_device``, ``set_source``, ``solve``, ``poynting_flux_end``, ``fields_coords_xy``,
+``fields_volume`` and the ``depth`` / ``zmax`` / ``solved`` / ``source_defined`` properties.
+
+Differences a user may notice:
+* ``S``/``Stot`` and the stacking matrices are torch complex128 CUDA tensors of the
+  reference's shapes ([2, 2, n, n]); ``poynting_flux_end`` returns Python floats / numpy arrays.
+* A layer solve that hits a singular pivot, a non-converged eigensolve or a non-finite value
+  raises ``KhpError`` naming the condition instead of returning NaN silently.
+* The convolution matrix, C^-1 and the Hx/Hy products of a pixmap are computed once per pixmap
+  content, not on every ``solve`` (the reference rebuilds them, layer.py:156-158); the pixmap
+  is still read at ``solve`` time, so in-place edits between solves are honoured.
+"""
+from __future__ import annotations
+
+import cmath
+import math
+from copy import copy
+from types import SimpleNamespace
+
+import numpy as np
+import torch
+
+from . import _capi, engine
+from .engine import LayerSpec
+
+
+class Layer:
+    """Layer descriptors of the Layer API subset used by Crystal.add_layer (khepri/layer.py:63-143)."""
+
+    def __init__(self, kind, eps, depth):
+        self.kind, self.epsilon, self.depth = kind, eps, depth
+        self.fields = False
+
+    @classmethod
+    def uniform(cls, expansion, epsilon, depth):
+        return cls("uniform", epsilon, depth)
+
+    @classmethod
+    def pixmap(cls, expansion, pixmap, depth):
+        return cls("pixmap", pixmap, depth)
+
+    @classmethod
+    def pixmap_or_uniform(cls, expansion, pixmap, depth):
+        eps0 = np.asarray(pixmap).flatten()[0]
+        if np.all(np.asarray(pixmap) == eps0):
+            return cls.uniform(expansion, eps0, depth)
+        return cls.pixmap(expansion, pixmap, depth)
+
+    @classmethod
+    def half_infinite(cls, expansion, type, epsilon):
+        if type == "reflexion":
+            return cls("inc", epsilon, 0)
+        if type == "transmission":
+            return cls("trn", epsilon, 0)
+        raise ValueError(f"unknown half-space type {type!r}")
+
+    def spec(self):
+        return LayerSpec(self.kind, self.epsilon, self.depth)
+
+
+class Crystal:
+    """GPU drop-in for khepri.crystal.Crystal (square, hexagonal or explicit lattices)."""
+
+    def __init__(self, pw, lattice="square", lattice_pitch=1, void=False, epsi=1, epse=1, device="cuda"):
+        self.pw = tuple(pw)
+        self.a = lattice_pitch
+        self.void = void
+        self.epsi = epsi
+        self.epse = epse
+        self.source = None
+        self.lattice = engine.lattice_vectors(lattice, lattice_pitch)
+        self._struct = engine.StructureGPU(self.pw, self.lattice, device)
+        self.device = self._struct.device
+        self.layers = dict()
+        self.stacking_matrices = list()
+        self.stack_positions = []
+        self.S = None
+
+    # -- layers ----------------------------------------------------------------------------
+    def add_layer_uniform(self, name, epsilon, depth):
+        self.layers[name] = Layer("uniform", epsilon, depth)
+
+    def add_pixmap_or_uniform(self, name, epsilon, depth):
+        sample = np.asarray(epsilon).flatten()[0]
+        if np.all(np.asarray(epsilon) == sample):
+            self.add_layer_uniform(name, sample, depth)
+        else:
+            self.add_layer_pixmap(name, epsilon, depth)
+
+    def add_layer_pixmap(self, name, epsilon, depth):
+        self.layers[name] = Layer("pixmap", epsilon, depth)
+
+    def add_layer(self, name, layer, extended=False):
+        if extended:
+            raise NotImplementedError("extended (twisted) layers are not part of this GPU path")
+        self.layers[name] = layer
+
+    def set_device(self, layers_stack, fields_mask=False):
+        """crystal.py:131-164."""
+        self.device_stack = copy(layers_stack)
+        self.global_stacking = []
+        if not self.void:
+            self.global_stacking.append("Sref")
+        self.global_stacking.extend(layers_stack)
+        if not self.void:
+            self.global_stacking.append("Strans")
+        required = set(self.global_stacking)
+        if "Sref" in required and "Sref" not in self.layers:
+            self.layers["Sref"] = Layer.half_infinite(None, "reflexion", self.epsi)
+            self.layers["Sref"].fields = True
+        if "Strans" in required and "Strans" not in self.layers:
+            self.layers["Strans"] = Layer.half_infinite(None, "transmission", self.epse)
+            self.layers["Strans"].fields = True
+        fields_mask = [fields_mask] * len(layers_stack) if isinstance(fields_mask, bool) else fields_mask
+        self.stack_retain_mask = [True] + list(fields_mask) + [True]
+        for name, enabled in zip(self.global_stacking, self.stack_retain_mask):
+            self.layers[name].fields |= enabled
+
+    @property
+    def depth(self):
+        return sum(self.layers[name].depth for name in self.device_stack)
+
+    @property
+    def source_defined(self):
+        return self.source is not None
+
+    @property
+    def solved(self):
+        return self.S is not None
+
+    @property
+    def zmax(self):
+        return self.stack_positions[-2]
+
+    # -- source / solve --------------------------------------------------------------------
+    def set_source(self, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, kp=None):
+        """crystal.py:345-360."""
+        self.source = SimpleNamespace(te=te, tm=tm, theta=theta, phi=phi, wavelength=wavelength)
+        if kp is not None:
+            self.kp = (kp[0], kp[1])
+        else:
+            self.kp = engine.compute_kplanar(self.epsi, wavelength, theta, phi)
+        self.k0 = 2 * np.pi / wavelength
+        self.kzi = np.conj(cmath.sqrt(self.k0 ** 2 * self.epsi - self.kp[0] ** 2 - self.kp[1] ** 2))
+
+    def _problems(self):
+        return engine.Problems.make([self.source.wavelength], [self.kp], self.source.te, self.source.tm, self.device)
+
+    def solve(self):
+        """crystal.py:180-206: every distinct layer once, then the forward (and, when fields are
+        retained, reverse) star-product chains."""
+        assert self.source_defined, "Call set_source before solving."
+        prob = self._problems()
+        status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        specs = {name: self.layers[name].spec() for name in set(self.global_stacking)}
+        keep = {name for name in specs if self.layers[name].fields}
+        states = engine.solve_layers(self._struct, specs, self.global_stacking, prob, status, keep_modes=keep)
+        layer_sizes = [self.layers[name].depth for name in self.global_stacking]
+        self.stack_positions = list(np.cumsum(layer_sizes))
+        self.stack_positions[-1] = np.inf
+        if not self.void:
+            self.stack_positions.insert(0, -np.inf)
+        want_fields = any(self.stack_retain_mask[1:-1])
+        fwd, rev, Stot = engine.chain(states, self.global_stacking, self.stack_retain_mask, status,
+                                      reverse=want_fields)
+        word = int(status.item())
+        if word:
+            raise _capi.KhpError(f"solve: {_capi.decode_status(word)}")
+        self._states = states
+        self._prob = prob
+        self._fwd, self._rev = fwd, rev
+        self.stacking_matrices = [None if s is None else s[0] for s in fwd]
+        self.stacking_reverse_matrices = None if rev is None else [None if s is None else s[0] for s in rev]
+        self.Stot = Stot[0]
+        self.S = self.Stot
+        self._Stot_b = Stot
+
+    def poynting_flux_end(self, only_total=True):
+        """crystal.py:363-396."""
+        assert self.solved, "Call solve first"
+        R, T, ro, to = engine.flux(self._struct, self._Stot_b, self._prob, self.epsi, self.epse, orders=not only_total)
+        if only_total:
+            return float(R.item()), float(T.item())
+        return (float(R.item()), ro[0].cpu().numpy()), (float(T.item()), to[0].cpu().numpy())
+
+    # -- fields ------------------------------------------------------------------------------
+    def get_source_as_field_vectors(self):
+        """crystal.py:281-295: (E, H) source vectors, H = 0."""
+        from .fields import incident_vector
+        e = incident_vector(self.pw, self.source.te, self.source.tm, (self.kp[0], self.kp[1], self.kzi))
+        return e, np.zeros_like(e)
+
+    def fields_coords_xy(self, x, y, z, incident_fields=None, kp=None, return_fourier=False):
+        """crystal.py:297-333: E, H at the (x, y) meshgrid for one depth z."""
+        from . import fields
+        return fields.fields_coords_xy(self, x, y, z, incident_fields, kp, return_fourier)
+
+    def fields_volume(self, x, y, z, incident_fields=None):
+        """crystal.py:335-343: E, H of shape [Nz, 3, X, Y]."""
+        from . import fields
+        return fields.fields_volume(self, x, y, z, incident_fields)
+
+
+class Multilayer(Crystal):
+    """1x1-harmonic Crystal (khepri/crystal.py:404-406)."""
+
+    def __init__(self, epsi=1, epse=1, device="cuda"):
+        super().__init__((1, 1), lattice="square", lattice_pitch=1, void=False, epsi=epsi, epse=epse, device=device)

@@ -1,0 +1,409 @@
+// Dense complex linear algebra written against the Team abstraction (khp_core.cuh):
+// LU with partial pivoting, triangular solves / inverse, Householder Hessenberg reduction,
+// single-shift complex QR (Schur form) and eigenvectors of the triangular factor.
+//
+// One team (one CTA) works on one matrix; matrices are row-major with leading dimension ld.
+// These are the numerical building blocks of the per-layer mode solve (eig of P*Q,
+// khepri/alternative.py:158-178), of build_scatmat (alternative.py:181-195) and of the
+// Redheffer star product (alternative.py:19-30), whose reference implementations call LAPACK
+// zgeev / zgesv through numpy.
+#pragma once
+
+#include "khp_core.cuh"
+
+namespace khp {
+
+template <typename T> KHP_HD T tmax(T a, T b) { return a > b ? a : b; }
+template <typename T> KHP_HD T tmin(T a, T b) { return a < b ? a : b; }
+
+// ------------------------------------------------------------------------------------------
+// LU factorisation with partial pivoting (row interchanges applied to whole rows).
+// A = P L U in place; piv[k] = row swapped with k at step k.  Returns status bits.
+// ------------------------------------------------------------------------------------------
+template <class Team, typename T>
+KHP_HD int team_getrf(const Team& t, cplx<T>* A, int64_t ld, int n, int* piv, TeamShared* sh) {
+  int info = 0;
+  for (int k = 0; k < n; ++k) {
+    T best = T(-1);
+    int bi = k;
+    for (int i = k + t.tid(); i < n; i += t.size()) {
+      const T v = abs1(A[i * ld + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    team_argmax(t, best, bi, sh);
+    if (t.tid() == 0) piv[k] = bi;
+    if (!(best > T(0))) {  // zero (or NaN) column: nothing to eliminate
+      if (best == T(0)) info |= KHP_BIT_SINGULAR;
+      else info |= KHP_BIT_NONFINITE;
+      t.sync();
+      continue;
+    }
+    if (bi != k) {
+      for (int j = t.tid(); j < n; j += t.size()) {
+        const cplx<T> a = A[k * ld + j];
+        A[k * ld + j] = A[bi * ld + j];
+        A[bi * ld + j] = a;
+      }
+    }
+    t.sync();
+    const cplx<T> pv = A[k * ld + k];
+    for (int i = k + 1 + t.tid(); i < n; i += t.size()) A[i * ld + k] = cdiv(A[i * ld + k], pv);
+    t.sync();
+    const int m = n - k - 1;
+    for (int e = t.tid(); e < m * m; e += t.size()) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      fms_acc(A[i * ld + j], A[i * ld + k], A[k * ld + j]);
+    }
+    t.sync();
+  }
+  return info;
+}
+
+// Solve A X = B in place in B (n x m, leading dimension ldb) given team_getrf's factors.
+template <class Team, typename T>
+KHP_HD void team_getrs(const Team& t, const cplx<T>* A, int64_t lda, int n, const int* piv, cplx<T>* B,
+                       int64_t ldb, int m) {
+  if (2 * m >= t.size()) {
+    // Enough right-hand sides for every thread: each owns whole columns, no barriers needed.
+    for (int j = t.tid(); j < m; j += t.size()) {
+      for (int k = 0; k < n; ++k) {
+        const int p = piv[k];
+        if (p != k) {
+          const cplx<T> a = B[k * ldb + j];
+          B[k * ldb + j] = B[p * ldb + j];
+          B[p * ldb + j] = a;
+        }
+      }
+      for (int k = 0; k < n; ++k) {
+        const cplx<T> bk = B[k * ldb + j];
+        for (int i = k + 1; i < n; ++i) fms_acc(B[i * ldb + j], A[i * lda + k], bk);
+      }
+      for (int k = n - 1; k >= 0; --k) {
+        const cplx<T> bk = cdiv(B[k * ldb + j], A[k * lda + k]);
+        B[k * ldb + j] = bk;
+        for (int i = 0; i < k; ++i) fms_acc(B[i * ldb + j], A[i * lda + k], bk);
+      }
+    }
+    t.sync();
+    return;
+  }
+  for (int j = t.tid(); j < m; j += t.size()) {
+    for (int k = 0; k < n; ++k) {
+      const int p = piv[k];
+      if (p != k) {
+        const cplx<T> a = B[k * ldb + j];
+        B[k * ldb + j] = B[p * ldb + j];
+        B[p * ldb + j] = a;
+      }
+    }
+  }
+  t.sync();
+  for (int k = 0; k + 1 < n; ++k) {
+    const int rows = n - k - 1;
+    for (int e = t.tid(); e < rows * m; e += t.size()) {
+      const int i = k + 1 + e / m, j = e % m;
+      fms_acc(B[i * ldb + j], A[i * lda + k], B[k * ldb + j]);
+    }
+    t.sync();
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    for (int j = t.tid(); j < m; j += t.size()) B[k * ldb + j] = cdiv(B[k * ldb + j], A[k * lda + k]);
+    t.sync();
+    for (int e = t.tid(); e < k * m; e += t.size()) {
+      const int i = e / m, j = e % m;
+      fms_acc(B[i * ldb + j], A[i * lda + k], B[k * ldb + j]);
+    }
+    t.sync();
+  }
+}
+
+template <class Team, typename T>
+KHP_HD void team_set_identity(const Team& t, cplx<T>* B, int64_t ld, int n, int m) {
+  for (int e = t.tid(); e < n * m; e += t.size()) {
+    const int i = e / m, j = e % m;
+    B[i * ld + j] = mk(T(i == j ? 1 : 0));
+  }
+  t.sync();
+}
+
+// C = alpha * A B + beta * C  (A: n x k, B: k x m).  Plain reference form; the tiled batched
+// kernel in khp_gemm.cu is the fast path.
+template <class Team, typename T>
+KHP_HD void team_gemm(const Team& t, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda,
+                      const cplx<T>* B, int64_t ldb, cplx<T> beta, cplx<T>* C, int64_t ldc) {
+  const bool use_beta = !(beta.re == T(0) && beta.im == T(0));
+  for (int e = t.tid(); e < n * m; e += t.size()) {
+    const int i = e / m, j = e % m;
+    cplx<T> acc = mk(T(0));
+    for (int l = 0; l < k; ++l) fma_acc(acc, A[i * lda + l], B[l * ldb + j]);
+    cplx<T> r = alpha * acc;
+    if (use_beta) r += beta * C[i * ldc + j];
+    C[i * ldc + j] = r;
+  }
+  t.sync();
+}
+
+// ------------------------------------------------------------------------------------------
+// Hessenberg reduction by Householder reflectors, H = Q^H A Q, Q accumulated into Z.
+// Reflector convention: P = I - tau u u^H with u = [1, v], beta real, P^H [alpha; x] = [beta; 0].
+// vbuf: n complex of scratch.
+// ------------------------------------------------------------------------------------------
+template <class Team, typename T>
+KHP_HD void team_gehrd(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* vbuf,
+                       TeamShared* sh) {
+  team_set_identity(t, Z, ldz, n, n);
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1;
+    T s = T(0);
+    for (int i = k + 2 + t.tid(); i < n; i += t.size()) s += norm2(H[i * ld + k]);
+    s = team_sum(t, s, sh);
+    const cplx<T> alpha = H[(k + 1) * ld + k];
+    if (s == T(0) && alpha.im == T(0)) continue;  // already reduced (tau = 0)
+    const T beta = -copysign(sqrt(norm2(alpha) + s), alpha.re);
+    const cplx<T> tau = mk((beta - alpha.re) / beta, -alpha.im / beta);
+    const cplx<T> scal = cdiv(mk(T(1)), alpha - mk(beta));
+    for (int l = t.tid(); l < m; l += t.size()) vbuf[l] = (l == 0) ? mk(T(1)) : H[(k + 1 + l) * ld + k] * scal;
+    t.sync();
+    for (int l = t.tid(); l < m; l += t.size()) H[(k + 1 + l) * ld + k] = (l == 0) ? mk(beta) : mk(T(0));
+    // H <- P^H H on rows k+1.., columns k+1..
+    const cplx<T> ctau = conj(tau);
+    for (int j = k + 1 + t.tid(); j < n; j += t.size()) {
+      cplx<T> w = mk(T(0));
+      for (int l = 0; l < m; ++l) w += conj_mul(vbuf[l], H[(k + 1 + l) * ld + j]);
+      w = ctau * w;
+      for (int l = 0; l < m; ++l) fms_acc(H[(k + 1 + l) * ld + j], vbuf[l], w);
+    }
+    t.sync();
+    // H <- H P on all rows, columns k+1..; Z <- Z P
+    for (int i = t.tid(); i < n; i += t.size()) {
+      cplx<T> y = mk(T(0));
+      for (int l = 0; l < m; ++l) fma_acc(y, H[i * ld + k + 1 + l], vbuf[l]);
+      y = tau * y;
+      for (int l = 0; l < m; ++l) H[i * ld + k + 1 + l] -= mul_conj(y, vbuf[l]);
+      cplx<T> yz = mk(T(0));
+      for (int l = 0; l < m; ++l) fma_acc(yz, Z[i * ldz + k + 1 + l], vbuf[l]);
+      yz = tau * yz;
+      for (int l = 0; l < m; ++l) Z[i * ldz + k + 1 + l] -= mul_conj(yz, vbuf[l]);
+    }
+    t.sync();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Complex Schur form of an upper Hessenberg H by single-shift implicit QR (Wilkinson shift,
+// exceptional shifts after 10 and 20 stalled iterations, Ahues-Tisseur deflation test).
+// Updates H to upper triangular T and Z <- Z Q.  Returns status bits (NOT_CONVERGED when
+// the iteration cap 30*n + 60 is reached: every loop in here is bounded).
+// ------------------------------------------------------------------------------------------
+template <typename T>
+KHP_HD bool hqr_negligible(const cplx<T>* H, int64_t ld, int k, int hi, T smlnum) {
+  const cplx<T> h = H[k * ld + k - 1];
+  const T ah = abs1(h);
+  if (ah <= smlnum) return true;
+  const T ulp = Eps<T>::ulp;
+  T tst = abs1(H[(k - 1) * ld + k - 1]) + abs1(H[k * ld + k]);
+  if (tst == T(0)) {
+    if (k - 2 >= 0) tst += fabs(H[(k - 1) * ld + k - 2].re);
+    if (k + 1 <= hi) tst += fabs(H[(k + 1) * ld + k].re);
+  }
+  if (ah > ulp * tst) return false;
+  const T hu = abs1(H[(k - 1) * ld + k]);
+  const T ab = tmax(ah, hu), ba = tmin(ah, hu);
+  const T d1 = abs1(H[k * ld + k]), d2 = abs1(H[(k - 1) * ld + k - 1] - H[k * ld + k]);
+  const T aa = tmax(d1, d2), bb = tmin(d1, d2);
+  const T s = aa + ab;
+  return ba * (ab / s) <= tmax(smlnum, ulp * (bb * (aa / s)));
+}
+
+template <typename T>
+KHP_HD cplx<T> hqr_shift(const cplx<T>* H, int64_t ld, int lo, int hi, int its) {
+  if (its == 10) return H[lo * ld + lo] + mk(T(0.75) * abs1(H[(lo + 1) * ld + lo]));
+  if (its == 20) return H[hi * ld + hi] + mk(T(0.75) * abs1(H[hi * ld + hi - 1]));
+  const cplx<T> a = H[(hi - 1) * ld + hi - 1], b = H[(hi - 1) * ld + hi];
+  const cplx<T> c = H[hi * ld + hi - 1], d = H[hi * ld + hi];
+  const cplx<T> p = T(0.5) * (a - d);
+  const cplx<T> bc = b * c;
+  cplx<T> disc = csqrt(p * p + bc);
+  if (p.re * disc.re + p.im * disc.im < T(0)) disc = -disc;
+  const cplx<T> den = p + disc;
+  if (den.re == T(0) && den.im == T(0)) return d;
+  return d - cdiv(bc, den);
+}
+
+// Givens rotation G = [[c, s], [-conj(s), c]] (c real) with G [x; y] = [r; 0].
+template <typename T>
+KHP_HD void givens(cplx<T> x, cplx<T> y, T& c, cplx<T>& s, cplx<T>& r) {
+  const T ax = cabs(x), ay = cabs(y);
+  if (ay == T(0)) { c = T(1); s = mk(T(0)); r = x; return; }
+  if (ax == T(0)) { c = T(0); s = conj(y) * (T(1) / ay); r = mk(ay); return; }
+  const T rho = hypot(ax, ay);
+  const cplx<T> ph = x * (T(1) / ax);
+  c = ax / rho;
+  s = ph * conj(y) * (T(1) / rho);
+  r = ph * rho;
+}
+
+template <class Team, typename T>
+KHP_HD int team_hqr(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, TeamShared* sh) {
+  const T smlnum = Eps<T>::safemin * (T(n) / Eps<T>::ulp);
+  const int cap = 30 * n + 60;
+  int hi = n - 1, its = 0, total = 0, status = 0;  // used by thread 0 only
+  while (true) {
+    t.sync();
+    if (t.tid() == 0) {
+      int action = 2, lo = 0;
+      cplx<T> mu = mk(T(0));
+      if (hi >= 0) {
+        int l = 0;
+        for (int k = hi; k >= 1; --k) {
+          if (hqr_negligible(H, ld, k, hi, smlnum)) {
+            H[k * ld + k - 1] = mk(T(0));
+            l = k;
+            break;
+          }
+        }
+        if (l == hi) {
+          hi -= 1;
+          its = 0;
+          action = 1;
+        } else {
+          ++its;
+          ++total;
+          if (total > cap) {
+            status |= KHP_BIT_NOT_CONVERGED;
+          } else {
+            action = 0;
+            lo = l;
+            mu = hqr_shift(H, ld, l, hi, its);
+          }
+        }
+      }
+      sh->bi[0] = action;
+      sh->bi[1] = lo;
+      sh->bi[2] = hi;
+      sh->bi[3] = status;
+      sh->bd[0] = (double)mu.re;
+      sh->bd[1] = (double)mu.im;
+    }
+    t.sync();
+    const int action = sh->bi[0];
+    if (action == 2) break;
+    if (action == 1) continue;
+    const int lo = sh->bi[1], ahi = sh->bi[2];
+    const cplx<T> mu = mk((T)sh->bd[0], (T)sh->bd[1]);
+    for (int k = lo; k < ahi; ++k) {
+      if (t.tid() == 0) {
+        cplx<T> x, y;
+        if (k == lo) {
+          x = H[lo * ld + lo] - mu;
+          y = H[(lo + 1) * ld + lo];
+        } else {
+          x = H[k * ld + k - 1];
+          y = H[(k + 1) * ld + k - 1];
+        }
+        T c;
+        cplx<T> s, r;
+        givens(x, y, c, s, r);
+        if (k > lo) {
+          H[k * ld + k - 1] = r;
+          H[(k + 1) * ld + k - 1] = mk(T(0));
+        }
+        sh->bd[2] = (double)c;
+        sh->bd[3] = (double)s.re;
+        sh->bd[4] = (double)s.im;
+      }
+      t.sync();
+      const T c = (T)sh->bd[2];
+      const cplx<T> s = mk((T)sh->bd[3], (T)sh->bd[4]);
+      const int j0 = (k == lo) ? lo : k;
+      for (int j = j0 + t.tid(); j < n; j += t.size()) {
+        const cplx<T> h1 = H[k * ld + j], h2 = H[(k + 1) * ld + j];
+        H[k * ld + j] = c * h1 + s * h2;
+        H[(k + 1) * ld + j] = c * h2 - conj_mul(s, h1);
+      }
+      t.sync();
+      const int i1 = (k + 2 < ahi) ? k + 2 : ahi;
+      for (int i = t.tid(); i <= i1; i += t.size()) {
+        const cplx<T> g1 = H[i * ld + k], g2 = H[i * ld + k + 1];
+        H[i * ld + k] = c * g1 + mul_conj(g2, s);
+        H[i * ld + k + 1] = c * g2 - s * g1;
+      }
+      for (int i = t.tid(); i < n; i += t.size()) {
+        const cplx<T> g1 = Z[i * ldz + k], g2 = Z[i * ldz + k + 1];
+        Z[i * ldz + k] = c * g1 + mul_conj(g2, s);
+        Z[i * ldz + k + 1] = c * g2 - s * g1;
+      }
+      t.sync();
+    }
+  }
+  return sh->bi[3];
+}
+
+// ------------------------------------------------------------------------------------------
+// Eigenvectors of an upper triangular T (in place): lam[k] = T[k][k]; the strictly upper part
+// becomes X with T X = X diag(lam), X unit upper triangular.  All eigenvectors are built at
+// once, row by row from the bottom; near-equal eigenvalues are separated by a floor
+// max(ulp |lam_k|, smlnum) on the divisor.
+// ------------------------------------------------------------------------------------------
+template <class Team, typename T>
+KHP_HD void team_trevc(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* lam) {
+  const T smlnum = Eps<T>::safemin * (T(n) / Eps<T>::ulp);
+  for (int k = t.tid(); k < n; k += t.size()) lam[k] = H[k * ld + k];
+  t.sync();
+  for (int e = t.tid(); e < n * n; e += t.size()) {
+    const int i = e / n, j = e % n;
+    if (i < j) H[i * ld + j] = -H[i * ld + j];
+    else H[i * ld + j] = mk(T(i == j ? 1 : 0));
+  }
+  t.sync();
+  for (int j = n - 2; j >= 0; --j) {
+    const cplx<T> tjj = lam[j];
+    for (int k = j + 1 + t.tid(); k < n; k += t.size()) {
+      cplx<T> den = tjj - lam[k];
+      const T smin = tmax(Eps<T>::ulp * abs1(lam[k]), smlnum);
+      if (abs1(den) < smin) den = mk(smin);
+      H[j * ld + k] = cdiv(H[j * ld + k], den);
+    }
+    t.sync();
+    const int cols = n - 1 - j;
+    for (int e = t.tid(); e < j * cols; e += t.size()) {
+      const int i = e / cols, k = j + 1 + e % cols;
+      fma_acc(H[i * ld + k], H[i * ld + j], H[j * ld + k]);
+    }
+    t.sync();
+  }
+}
+
+// W = Z X (X unit upper triangular), then every column scaled to unit 2-norm.
+template <class Team, typename T>
+KHP_HD void team_backtransform(const Team& t, const cplx<T>* Z, int64_t ldz, const cplx<T>* X, int64_t ldx, int n,
+                               cplx<T>* W, int64_t ldw) {
+  for (int e = t.tid(); e < n * n; e += t.size()) {
+    const int i = e / n, k = e % n;
+    cplx<T> acc = mk(T(0));
+    for (int l = 0; l <= k; ++l) fma_acc(acc, Z[i * ldz + l], X[l * ldx + k]);
+    W[i * ldw + k] = acc;
+  }
+  t.sync();
+  for (int k = t.tid(); k < n; k += t.size()) {
+    T s = T(0);
+    for (int i = 0; i < n; ++i) s += norm2(W[i * ldw + k]);
+    const T inv = s > T(0) ? T(1) / sqrt(s) : T(1);
+    for (int i = 0; i < n; ++i) W[i * ldw + k] = W[i * ldw + k] * inv;
+  }
+  t.sync();
+}
+
+// Full eigendecomposition A W = W diag(lam).  A is overwritten (Schur factor, then X);
+// Z: n x n scratch; vbuf: n scratch.  Returns status bits.
+template <class Team, typename T>
+KHP_HD int team_geev(const Team& t, cplx<T>* A, int64_t lda, int n, cplx<T>* Z, int64_t ldz, cplx<T>* W,
+                     int64_t ldw, cplx<T>* lam, cplx<T>* vbuf, TeamShared* sh) {
+  team_gehrd(t, A, lda, n, Z, ldz, vbuf, sh);
+  const int st = team_hqr(t, A, lda, n, Z, ldz, sh);
+  team_trevc(t, A, lda, n, lam);
+  team_backtransform(t, Z, ldz, A, lda, n, W, ldw);
+  return st;
+}
+
+}  // namespace khp

@@ -1,0 +1,51 @@
+// Internal C++ launch interface of libkhp (not part of the C-ABI): batched dense kernels over
+// strided batches of row-major complex matrices, all asynchronous on the given stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "khp_core.cuh"
+
+namespace khp {
+
+// LU factorisation with partial pivoting of batch matrices A[b] (n x n); piv: batch x n ints.
+// info[b] |= status bits (SINGULAR / NONFINITE).
+template <typename T>
+int launch_getrf(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv, int* info, cudaStream_t s);
+
+// Solve A[b] X = B[b] with getrf factors; B (n x m) overwritten.
+template <typename T>
+int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv, cplx<T>* B,
+                 int64_t ldb, int64_t bsB, int m, cudaStream_t s);
+
+// C = alpha A B + beta C (A n x k, B k x m).  A batch stride of 0 broadcasts one matrix;
+// aidx (optional, device int[batch]) picks A[aidx[b]] for problem b.
+template <typename T>
+int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda, int64_t bsA,
+                const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
+                cudaStream_t s, const int* aidx = nullptr);
+
+// Eigen-decomposition A W = W diag(lam); A destroyed; Z: batch x n x n scratch (ld n).
+template <typename T>
+int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
+                int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s);
+
+// Element-wise helpers on batches of n x m matrices.
+template <typename T>
+int launch_copy(int64_t batch, int n, int m, const cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb,
+                int64_t bsB, cudaStream_t s);
+template <typename T>
+int launch_identity(int64_t batch, int n, int m, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T> diag, cudaStream_t s);
+// C = a A + b B (C may alias A or B)
+template <typename T>
+int launch_axpby(int64_t batch, int n, int m, cplx<T> a, const cplx<T>* A, int64_t lda, int64_t bsA, cplx<T> b,
+                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T>* C, int64_t ldc, int64_t bsC, cudaStream_t s);
+
+// Inverse: Ainv[b] = A[b]^-1 (A destroyed: holds the LU factors on return).
+template <typename T>
+int launch_inverse(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
+                   int64_t bsI, int* piv, int* info, cudaStream_t s);
+
+inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
+
+}  // namespace khp

@@ -1,0 +1,74 @@
+"""CPU-side checks of the boundary: libkhp loads and exports every symbol the header declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(khp_\w+)\s*\(", text, re.M))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from khepri_gb300 import build as kb
+    kb.build()
+    from khepri_gb300 import _capi
+    return _capi.load()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert {"khp_version", "khp_status_string", "khp_convmat", "khp_layer_modes", "khp_layer_smatrix",
+            "khp_closed_form_smatrix", "khp_star_product", "khp_flux"} <= names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in sorted(_declared()):
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header(lib):
+    from khepri_gb300 import _capi
+    assert set(_capi.exported_symbols()) == _declared()
+
+
+def test_version_and_status_strings(lib):
+    from khepri_gb300 import _capi
+    assert lib.khp_version() >= 100
+    assert _capi.status_string(0) == "ok"
+    assert "workspace" in _capi.status_string(2)
+    assert _capi.decode_status(5) == "singular pivot, non-finite value"
+
+
+def test_workspace_sizes_are_monotone(lib):
+    for f, args in [(lib.khp_layer_modes_workspace, (8, 25)), (lib.khp_layer_smatrix_workspace, (8, 25)),
+                    (lib.khp_star_product_workspace, (8, 50)), (lib.khp_convmat_workspace, (8, 5, 5))]:
+        small = f(*args)
+        big = f(args[0] * 2, *args[1:])
+        assert 0 < small < big and small % 256 == 0
+
+
+def test_invalid_arguments_rejected_without_gpu(lib):
+    # Validation happens before any CUDA call: even-sized harmonic sets and null pointers.
+    assert lib.khp_convmat(1, 16, 16, None, 4, 3, None, None, 0, None) == 1
+    assert lib.khp_star_product(1, 10, None, 0, None, 0, None, None, None, 0, None) == 1
+    assert lib.khp_flux(1, 3, 3, None, 0, None, None, None, None, None, None, 1.0, 0.0, 1.0, 0.0, None, None, None,
+                        None, None) == 1
+
+
+def test_no_gpu_means_loud_failure():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from khepri_gb300 import Crystal, KhpError
+    with pytest.raises(KhpError):
+        Crystal((3, 3))
