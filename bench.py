@@ -1,0 +1,331 @@
+"""Benchmark: batched RCWA solves/s at 11x11 harmonics on GB300 (one JSON line on stdout).
+
+Workload (the batched sweep): one seed of the 11x11 structure — a 256x256 binary pixmap (union
+of 1-4 periodic discs, eps 12 in eps 1) shared by 3 patterned layers, 2 uniform layers, depths
+U(0.2, 1.0) — over 64 frequencies 0.3-0.7 c/a x a 32x32 Bloch grid (65,536 problems), both
+polarisations from one S-matrix per problem.  A step solves one chunk of ``--batch`` problems
+(successive chunks of the sweep).  Synthetic seeded inputs: no dataset is involved.
+
+* value: problems (S-matrix solves) per second with the problem arrays resident in HBM,
+  timed with CUDA events over exactly K steps (barrier + synchronize on both sides).
+* e2e: the same metric through the public batched API (khepri_gb300.batch.solve_rt) from host
+  numpy inputs to host R/T, host<->device copies inside the timed region.
+* roofline: the libkhp entry point with the largest share of the timed region, algorithmic
+  FP64 flops per launch / its mean launch duration (events on the launching stream), against
+  the FP64 FMA throughput measured in this run by khp_probe_fp64_tflops.
+* cpu_baseline: the CPU oracle (numpy/LAPACK restatement of the reference) on a bounded sample.
+
+``--impl reference`` times that CPU restatement alone (all host threads), same metric/config.
+Multi-GPU (torchrun): independent replicas, each rank solving its own chunks; no collective on
+the data path; value = problems of all ranks / max over ranks of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RCWA solves/s + solve+grad/s, 11×11 harmonics, batched vs plain GPU, |ΔT|≤1e-6"
+UNIT = "solves/s"
+PW = (11, 11)
+N_MAT = 2 * PW[0] * PW[1]
+# Algorithmic flops per problem of each entry point (real flops, complex MAC = 8; conventions:
+# GEMM 8n^3, LU 8/3 n^3, eig 100 n^3; P build 1, P.Q 8, eig 100, V 8 -> modes 117 n^3;
+# build_scatmat 85.3 n^3; star product 106.7 n^3).
+FLOPS_PER_CALL = {
+    "khp_layer_modes": 117.0 * N_MAT ** 3,
+    "khp_layer_smatrix": 85.3 * N_MAT ** 3,
+    "khp_star_product": 106.7 * N_MAT ** 3,
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=192)
+    ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=6)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ------------------------------------------------------------------------------------------
+# CPU oracle timing (reported baseline / reference arm)
+# ------------------------------------------------------------------------------------------
+def time_oracle(problems, st, wl, kp):
+    from oracle import khepri_oracle as ko
+    cl = ko.OracleCrystal(st.pw)
+    for name, (kind, eps, depth) in st.layers.items():
+        (cl.add_layer_uniform if kind == "uniform" else cl.add_layer_pixmap)(name, eps, depth)
+    cl.set_device(st.stack, False)
+    t0 = time.perf_counter()
+    for p in problems:
+        cl.set_source(wl[p], 1.0, 0.0, kp=tuple(kp[p]))
+        cl.solve()
+        cl.poynting_flux_end()
+        cl.source.te, cl.source.tm = 0.0, 1.0
+        cl.poynting_flux_end()
+    return time.perf_counter() - t0
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# Reference arm
+# ------------------------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from khepri_gb300 import workloads
+    st = workloads.batched_structure(0)
+    wl, kp = workloads.batched_problems()
+    inside = np.flatnonzero(np.hypot(kp[:, 0], kp[:, 1]) < 2 * np.pi / wl)
+    per_step = 2
+    rng = np.random.default_rng(0)
+    for _ in range(args.warmup):
+        time_oracle(rng.choice(inside, per_step, replace=False), st, wl, kp)
+    total = 0.0
+    for _ in range(args.steps):
+        total += time_oracle(rng.choice(inside, per_step, replace=False), st, wl, kp)
+    value = per_step * args.steps / total
+    cores = cpu_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "batched sweep 11x11, 256x256 multi-disc map, [P,U,P,U,P], both polarisations",
+                   "batch": per_step, "harmonics": "11x11", "parallelism": "host cores (numpy/LAPACK)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{per_step} in-cone (f, k) problems per step of the 11x11 sweep, CPU oracle"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from khepri_gb300 import _capi, batch, engine, workloads
+
+    lib = _capi.load()
+    st = workloads.batched_structure(0)
+    wl_all, kp_all = workloads.batched_problems()
+    P = wl_all.shape[0]
+    B = args.batch
+    struct = engine.StructureGPU(st.pw, engine.lattice_vectors("square"), dev)
+    specs = batch._specs(st.layers, 1.0, 1.0)
+    for name, sp in specs.items():
+        if sp.kind == "pixmap":
+            struct.prepare_map(sp.eps)  # per-structure preparation, outside the timed region
+
+    def chunk(step):
+        s = ((step * world + rank) * B) % P
+        idx = np.arange(s, s + B) % P
+        return idx
+
+    nsteps = args.warmup + args.steps
+    probs = [engine.Problems.make(wl_all[chunk(k)], kp_all[chunk(k)], 1.0, 0.0, dev) for k in range(nsteps)]
+    statuses = [torch.zeros(B, dtype=torch.int32, device=dev) for _ in range(nsteps)]
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+
+    def step(k):
+        return batch.solve_chunk_both_pols(struct, specs, st.stack, probs[k], statuses[k])
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    timer = engine.StageTimer()
+    results = []
+    launches0 = lib.khp_launch_count()
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        with timer:
+            for k in range(args.warmup, nsteps):
+                flush.zero_()
+                results.append(step(k))
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+    launches = lib.khp_launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * B * args.steps / (ms * 1e-3)
+    bad = int(sum(int((s != 0).sum().item()) for s in statuses))
+
+    # roofline of the entry point with the largest share of the timed region
+    totals = timer.totals_ms()
+    dom = max(totals, key=lambda k: totals[k][0])
+    dom_ms, dom_calls = totals[dom]
+    share = {k: round(v[0] / ms, 4) for k, v in totals.items()}
+    scratch = torch.empty(1024 * 1024, dtype=torch.float64, device=dev)
+    fp64_peak = lib.khp_probe_fp64_tflops(_capi.ptr(scratch), scratch.numel(), _capi.stream_ptr())
+    roof = None
+    if dom in FLOPS_PER_CALL:
+        achieved = FLOPS_PER_CALL[dom] * B / (dom_ms / dom_calls * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+                "peak_source": "FP64 FMA pipe measured in this run (khp_probe_fp64_tflops); MEASURED_PEAKS.json "
+                               "lists only HBM and bf16",
+                "flops_per_launch": FLOPS_PER_CALL[dom] * B, "launch_ms": dom_ms / dom_calls,
+                "share_of_step": share}
+
+    # end to end through the public API: host numpy inputs -> host R, T
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        idx = chunk(args.warmup + k)
+        batch.solve_rt(st.pw, st.layers, st.stack, wl_all[idx], kp_all[idx], chunk=B, struct=struct,
+                       strict=False, both_pols=True)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    h2d = B * (8 + 32 + 16 + 16)  # k0, kp, te, tm per problem
+    d2h = B * (2 * 2 * 8 + 4)      # R, T for two polarisations, status
+
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        inside = np.flatnonzero(np.hypot(kp_all[:, 0], kp_all[:, 1]) < 2 * np.pi / wl_all)
+        sample = np.random.default_rng(1).choice(inside, args.cpu_sample, replace=False)
+        t_cpu = time_oracle(sample, st, wl_all, kp_all)
+        cpu = {"value": args.cpu_sample / t_cpu, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+               "sample": f"{args.cpu_sample} in-cone problems of the 11x11 sweep, both polarisations, CPU oracle "
+                         f"(numpy/LAPACK), {t_cpu:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+            "config": {"workload": "batched sweep 11x11 (n=242), 256x256 multi-disc map, [P,U,P,U,P], 64 f x "
+                                   "32x32 k, both polarisations per S-matrix",
+                       "batch": B, "harmonics": "11x11", "precision": "fp64 (complex128) throughout",
+                       "l2": "256 MB buffer written between steps (> 129 MB L2)",
+                       "parallelism": f"replicas x{world}", "problems_with_status": bad,
+                       "grad": "solve+grad/s not measured by this bench"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": world * B * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,16 @@ int khp_fields_fourier(int64_t nz, int32_t nh, const int32_t* slot_of_z, const d
 int khp_fields_idft(int64_t rows, int32_t nh, const double* ff, const double* gx, const double* gy, const double* kp,
                     int64_t npts, const double* x, const double* y, double* out, void* stream);
 
+/*
+ * Diagnostics (no counterpart in the reference).
+ * khp_launch_count: number of kernels libkhp has launched in this process (all entry points).
+ * khp_probe_fp64_tflops: measured FP64 FMA throughput of the current device in TFLOP/s, the
+ * denominator of FP64 roofline fractions; synchronises `stream`; scratch: device doubles,
+ * at least 1024 * (number of SMs); returns a negative value on failure.
+ */
+long long khp_launch_count(void);
+double khp_probe_fp64_tflops(double* scratch, int64_t scratch_doubles, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

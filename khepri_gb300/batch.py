@@ -22,8 +22,8 @@ def _specs(layers, epsi, epse):
     return specs
 
 
-def solve_chunk(struct, specs, stack, prob, status, orders=False, epsi=1.0, epse=1.0):
-    """R, T (and per-order powers) of one chunk of problems on the device."""
+def global_smatrix(struct, specs, stack, prob, status):
+    """Global S-matrix of every problem of the chunk, streamed left to right."""
     modes = {}
     Stot, _, _, _ = engine.closed_form(struct, "inc", specs["__inc__"].eps, 0.0, prob, status)
     for name in list(stack) + ["__trn__"]:
@@ -38,17 +38,37 @@ def solve_chunk(struct, specs, stack, prob, status, orders=False, epsi=1.0, epse
             S, _, _, _ = engine.closed_form(struct, sp.kind, sp.eps, sp.depth, prob, status)
         Stot = engine.star(Stot, S, status)
         del S
+    return Stot
+
+
+def solve_chunk(struct, specs, stack, prob, status, orders=False, epsi=1.0, epse=1.0):
+    """R, T (and per-order powers) of one chunk of problems on the device."""
+    Stot = global_smatrix(struct, specs, stack, prob, status)
     return engine.flux(struct, Stot, prob, epsi, epse, orders=orders)
 
 
+def solve_chunk_both_pols(struct, specs, stack, prob, status, epsi=1.0, epse=1.0):
+    """R, T for (te, tm) = (1, 0) and (0, 1) from one S-matrix per problem: each [B, 2]."""
+    Stot = global_smatrix(struct, specs, stack, prob, status)
+    one, zero = torch.ones_like(prob.te), torch.zeros_like(prob.te)
+    out = []
+    for te, tm in ((one, zero), (zero, one)):
+        p = engine.Problems(prob.k0, prob.kp, te, tm)
+        r, t, _, _ = engine.flux(struct, Stot, p, epsi, epse)
+        out.append((r, t))
+    return torch.stack([out[0][0], out[1][0]], 1), torch.stack([out[0][1], out[1][1]], 1)
+
+
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
-             chunk=256, orders=False, device="cuda", struct=None, strict=True):
+             chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False):
     """R and T of every problem (host numpy arrays); problems share ``layers``/``stack``.
 
     layers: name -> ("pixmap", eps_map, depth) | ("uniform", eps, depth); stack: layer names
     from the incidence side.  wavelengths [P], kp [P, 2] (absolute, complex allowed), te/tm
     scalars or [P].  Returns (R, T, status) or (R, T, r_orders, t_orders, status) with
-    ``orders=True``.  With ``strict`` a non-zero per-problem status raises KhpError.
+    ``orders=True``.  ``both_pols=True`` solves each S-matrix once and returns R, T of shape
+    [P, 2] for (te, tm) = (1, 0) and (0, 1).  With ``strict`` a non-zero per-problem status
+    raises KhpError.
     """
     _capi.require_cuda()
     wl = np.atleast_1d(np.asarray(wavelengths, dtype=float))
@@ -59,8 +79,8 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     if struct is None:
         struct = engine.StructureGPU(pw, engine.lattice_vectors(lattice), device)
     specs = _specs(layers, epsi, epse)
-    R = np.empty(P)
-    T = np.empty(P)
+    R = np.empty((P, 2) if both_pols else P)
+    T = np.empty((P, 2) if both_pols else P)
     ro = np.empty((P, struct.nh)) if orders else None
     to = np.empty((P, struct.nh)) if orders else None
     st = np.zeros(P, dtype=np.int32)
@@ -68,7 +88,11 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
         e = min(P, s + chunk)
         prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
         status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
-        r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
+        if both_pols:
+            r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
+            r_o = t_o = None
+        else:
+            r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
         R[s:e] = r.cpu().numpy()
         T[s:e] = t.cpu().numpy()
         if orders:

@@ -152,6 +152,7 @@ template <typename T>
 int launch_getrf(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv, int* info, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
   k_getrf<T><<<(unsigned)batch, kTeamThreads, 0, s>>>(n, A, lda, bsA, piv, info);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -160,6 +161,7 @@ int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bs
                  int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
   k_getrs<T><<<(unsigned)batch, kTeamThreads, 0, s>>>(n, A, lda, bsA, piv, B, ldb, bsB, m);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -174,6 +176,7 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
     dim3 grid((m + BN - 1) / BN, (n + BM - 1) / BM, nb);
     k_gemm<T, BM, BN, BK><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
                                                 aidx);
+    count_launches(1);
   }
   return cuda_status();
 }
@@ -184,6 +187,7 @@ int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx
   if (batch <= 0) return KHP_OK;
   const size_t smem = sizeof(cplx<T>) * (size_t)n;
   k_geev<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, W, ldw, bsW, lam, bsLam, info);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -193,6 +197,7 @@ int launch_copy(int64_t batch, int n, int m, const cplx<T>* A, int64_t lda, int6
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     k_copy<T><<<dim3(ew_blocks(n, m), nb), 256, 0, s>>>(n, m, A, lda, bsA, B, ldb, bsB, off);
+    count_launches(1);
   }
   return cuda_status();
 }
@@ -202,6 +207,7 @@ int launch_identity(int64_t batch, int n, int m, cplx<T>* A, int64_t lda, int64_
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     k_identity<T><<<dim3(ew_blocks(n, m), nb), 256, 0, s>>>(n, m, A, lda, bsA, diag, off);
+    count_launches(1);
   }
   return cuda_status();
 }
@@ -212,6 +218,7 @@ int launch_axpby(int64_t batch, int n, int m, cplx<T> a, const cplx<T>* A, int64
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     k_axpby<T><<<dim3(ew_blocks(n, m), nb), 256, 0, s>>>(n, m, a, A, lda, bsA, b, B, ldb, bsB, C, ldc, bsC, off);
+    count_launches(1);
   }
   return cuda_status();
 }

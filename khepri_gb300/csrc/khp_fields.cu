@@ -269,6 +269,7 @@ int khp_fields_amplitudes(int64_t nlayers, int32_t nh, const int64_t* sl_ptrs, c
   k_fields_amplitudes<<<(unsigned)nlayers, kThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
       nh, (const long long*)sl_ptrs, (const long long*)sr_ptrs, (const long long*)w_ptrs, (const long long*)v_ptrs,
       (const cd*)vref, (const cd*)inc, gx, gy, kp, k0, F, Wc, Vc, vec, piv, (cd*)amps, status);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -290,6 +291,7 @@ int khp_fields_fourier(int64_t nz, int32_t nh, const int32_t* slot_of_z, const d
                                                         (const long long*)v_ptrs, (const long long*)lam_ptrs,
                                                         (const long long*)ic_ptrs, (const cd*)ic_scalar,
                                                         (const cd*)amps, gx, gy, kp, k0, (cd*)ff);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -303,6 +305,7 @@ int khp_fields_idft(int64_t rows, int32_t nh, const double* ff, const double* gx
   dim3 grid((unsigned)((npts + 127) / 128), (unsigned)gy_blocks);
   k_fields_idft<RT><<<grid, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(rows, nh, (const cd*)ff, gx, gy, kp,
                                                                                npts, x, y, (cd*)out);
+  count_launches(1);
   return cuda_status();
 }
 

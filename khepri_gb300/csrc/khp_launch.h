@@ -48,4 +48,7 @@ int launch_inverse(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, c
 
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 
+// Adds k to the process-wide launch counter reported by khp_launch_count().
+void count_launches(int k);
+
 }  // namespace khp

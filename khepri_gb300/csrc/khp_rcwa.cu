@@ -579,8 +579,10 @@ int khp_convmat(int64_t nmaps, int64_t nx, int64_t ny, const double* eps, int32_
       cudaFuncSetAttribute(k_convmat_dft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
   k_convmat_dft<<<dim3(2 * px - 1, (unsigned)nmaps), 256, smem, s>>>(nx, ny, (const cd*)eps, px, py, w.F);
+  count_launches(1);
   const int64_t total = nmaps * (int64_t)px * py * px * py;
   k_convmat_gather<<<ew_grid(total), 256, 0, s>>>(nmaps, px, py, w.F, (cd*)conv);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -603,9 +605,11 @@ int khp_structure_prep(int64_t nmaps, int32_t nh, const double* conv, const doub
   KHP_TRY(launch_copy<double>(nmaps, nh, nh, C, nh, hh, w.lu, nh, hh, s));
   KHP_TRY(launch_inverse<double>(nmaps, nh, w.lu, nh, hh, (cd*)ic, nh, hh, w.piv, status, s));
   k_row_scale_real<<<ew_grid(nmaps * hh), 256, 0, s>>>(nmaps, nh, gx, C, w.tmp);
+  count_launches(1);
   KHP_TRY(launch_gemm<double>(nmaps, nh, nh, nh, mk(1.0), (const cd*)ic, nh, hh, w.tmp, nh, hh, mk(0.0), (cd*)hx, nh,
                               hh, s));
   k_row_scale_real<<<ew_grid(nmaps * hh), 256, 0, s>>>(nmaps, nh, gy, C, w.tmp);
+  count_launches(1);
   KHP_TRY(launch_gemm<double>(nmaps, nh, nh, nh, mk(1.0), (const cd*)ic, nh, hh, w.tmp, nh, hh, mk(0.0), (cd*)hy, nh,
                               hh, s));
   return cuda_status();
@@ -633,15 +637,18 @@ int khp_layer_modes(int64_t batch, int32_t nh, const int32_t* map_index, const d
   const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh, hn = (int64_t)nh * n;
   k_assemble_pq<<<ew_grid(batch * nn), 256, 0, s>>>(batch, nh, map_index, (const cd*)conv, (const cd*)hx,
                                                      (const cd*)hy, gx, gy, kp, k0, w.M);
+  count_launches(1);
   KHP_TRY(cuda_status());
   KHP_TRY(launch_geev<double>(batch, n, w.M, n, nn, w.Z, (cd*)W, n, nn, (cd*)lam, n, status, s));
   k_sqrt_lam<<<ew_grid(batch * n), 256, 0, s>>>(batch * n, (cd*)lam);
+  count_launches(1);
   KHP_TRY(launch_gemm<double>(batch, nh, n, nh, mk(1.0), (const cd*)conv, nh, hh, (const cd*)W, n, nn, mk(0.0), w.CWt,
                               n, hn, s, map_index));
   KHP_TRY(launch_gemm<double>(batch, nh, n, nh, mk(1.0), (const cd*)conv, nh, hh, (const cd*)W + hn, n, nn, mk(0.0),
                               w.CWb, n, hn, s, map_index));
   k_modes_v<<<ew_grid(batch * nn), 256, 0, s>>>(batch, nh, gx, gy, kp, k0, (const cd*)W, w.CWt, w.CWb,
                                                  (const cd*)lam, (cd*)V, status);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -672,12 +679,14 @@ int khp_layer_smatrix(int64_t batch, int32_t nh, const double* W, const double* 
   KHP_TRY(launch_inverse<double>(batch, n, w.b1, n, nn, w.b3, n, nn, w.piv, status, s));  // b3 = Vi
   k_build_ab<<<ew_grid(batch * nn), 256, 0, s>>>(batch, nh, gx, gy, kp, k0, w.b2, w.b3, w.b0, w.b1);  // b0 = A, b1 = B
   KHP_TRY(cuda_status());
+  count_launches(1);
   // Ai = A^-1 (b3 <- copy of A for the LU, b2 <- Ai)
   KHP_TRY(launch_copy<double>(batch, n, n, w.b0, n, nn, w.b3, n, nn, s));
   KHP_TRY(launch_inverse<double>(batch, n, w.b3, n, nn, w.b2, n, nn, w.piv, status, s));
   // p1 = X B Ai X
   KHP_TRY(launch_gemm<double>(batch, n, n, n, one, w.b1, n, nn, w.b2, n, nn, zero, w.p1, n, nn, s));
   k_xmx<<<ew_grid(batch * nn), 256, 0, s>>>(batch, n, L, depth, k0, w.p1);
+  count_launches(1);
   // p2 = T = A - p1 B
   KHP_TRY(launch_copy<double>(batch, n, n, w.b0, n, nn, w.p2, n, nn, s));
   KHP_TRY(launch_gemm<double>(batch, n, n, n, mone, w.p1, n, nn, w.b1, n, nn, one, w.p2, n, nn, s));
@@ -689,10 +698,12 @@ int khp_layer_smatrix(int64_t batch, int32_t nh, const double* W, const double* 
   KHP_TRY(launch_copy<double>(batch, n, n, w.b0, n, nn, w.tmp, n, nn, s));
   KHP_TRY(launch_gemm<double>(batch, n, n, n, mone, w.b1, n, nn, w.b3, n, nn, one, w.tmp, n, nn, s));
   k_xrows<<<ew_grid(batch * nn), 256, 0, s>>>(batch, n, L, depth, k0, w.tmp, w.rhs + n, 2 * n, 2 * nn);
+  count_launches(1);
   // [S11 | S12] = T^-1 rhs
   KHP_TRY(launch_getrf<double>(batch, n, w.p2, n, nn, w.piv, status, s));
   KHP_TRY(launch_getrs<double>(batch, n, w.p2, n, nn, w.piv, w.rhs, 2 * n, 2 * nn, 2 * n, s));
   k_scatter_sym<<<ew_grid(batch * 2 * nn), 256, 0, s>>>(batch, n, w.rhs, (cd*)S, status);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -710,6 +721,7 @@ int khp_closed_form_smatrix(int64_t batch, int32_t nh, int32_t kind, const doubl
   if (V && cudaMemsetAsync(V, 0, sizeof(cd) * batch * nn, s) != cudaSuccess) return KHP_ERR_CUDA;
   k_closed_form<<<ew_grid(batch * nh), 256, 0, s>>>(batch, nh, kind, (const cd*)eps, depth, gx, gy, kp, k0, (cd*)S,
                                                      (cd*)W, (cd*)V, (cd*)lam, status);
+  count_launches(1);
   return cuda_status();
 }
 
@@ -769,6 +781,7 @@ int khp_flux(int64_t batch, int32_t px, int32_t py, const double* S, int64_t s_s
   k_flux<<<(unsigned)batch, 128, 0, as_stream(stream)>>>(px, py, (const cd*)S, s_stride, gx, gy, kp, k0,
                                                          (const cd*)te, (const cd*)tm, mk(epsi_re, epsi_im),
                                                          mk(epse_re, epse_im), R, T, r_orders, t_orders);
+  count_launches(1);
   return cuda_status();
 }
 

@@ -74,6 +74,53 @@ def compute_kplanar(eps_inc, wavelength, theta_deg=0.0, phi_deg=0.0):
 
 
 # ------------------------------------------------------------------------------------------
+# Optional per-entry-point timing with CUDA events on the launching stream (used by bench.py)
+# ------------------------------------------------------------------------------------------
+class StageTimer:
+    """Collects (start, end) CUDA events around each libkhp entry point while active."""
+
+    def __init__(self):
+        self.events = {}
+
+    def __enter__(self):
+        global _TIMER
+        _TIMER = self
+        return self
+
+    def __exit__(self, *exc):
+        global _TIMER
+        _TIMER = None
+
+    def record(self, name):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    def add(self, name, e0, e1):
+        self.events.setdefault(name, []).append((e0, e1))
+
+    def totals_ms(self):
+        torch.cuda.synchronize()
+        return {k: (sum(a.elapsed_time(b) for a, b in v), len(v)) for k, v in self.events.items()}
+
+
+_TIMER = None
+
+
+class _stage:
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        self.e0 = _TIMER.record(self.name) if _TIMER is not None else None
+        return self
+
+    def __exit__(self, *exc):
+        if self.e0 is not None and _TIMER is not None:
+            _TIMER.add(self.name, self.e0, _TIMER.record(self.name))
+
+
+# ------------------------------------------------------------------------------------------
 # Workspace: one growing device byte buffer per device (caller-owned scratch for libkhp)
 # ------------------------------------------------------------------------------------------
 _WS = {}
@@ -198,11 +245,12 @@ def layer_modes(struct: StructureGPU, entry, prob: Problems, status):
     mi = torch.zeros(B, dtype=torch.int32, device=dev)
     lib = _capi.load()
     ws = workspace(lib.khp_layer_modes_workspace(B, nh), dev)
-    _capi.check(lib.khp_layer_modes(B, nh, _capi.ptr(mi), _capi.ptr(entry["conv"]), _capi.ptr(entry["hx"]),
+    with _stage("khp_layer_modes"):
+        code = lib.khp_layer_modes(B, nh, _capi.ptr(mi), _capi.ptr(entry["conv"]), _capi.ptr(entry["hx"]),
                                     _capi.ptr(entry["hy"]), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
                                     _capi.ptr(prob.kp), _capi.ptr(prob.k0), _capi.ptr(W), _capi.ptr(V),
-                                    _capi.ptr(lam), _capi.ptr(status), _capi.ptr(ws), ws.numel(), _capi.stream_ptr()),
-                "khp_layer_modes")
+                                    _capi.ptr(lam), _capi.ptr(status), _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+    _capi.check(code, "khp_layer_modes")
     return W, V, lam
 
 
@@ -213,10 +261,12 @@ def layer_smatrix(struct: StructureGPU, W, V, lam, depth, prob: Problems, status
     d = torch.full((B,), float(depth), dtype=F64, device=dev)
     lib = _capi.load()
     ws = workspace(lib.khp_layer_smatrix_workspace(B, nh), dev)
-    _capi.check(lib.khp_layer_smatrix(B, nh, _capi.ptr(W), _capi.ptr(V), _capi.ptr(lam), _capi.ptr(d),
+    with _stage("khp_layer_smatrix"):
+        code = lib.khp_layer_smatrix(B, nh, _capi.ptr(W), _capi.ptr(V), _capi.ptr(lam), _capi.ptr(d),
                                       _capi.ptr(struct.gx), _capi.ptr(struct.gy), _capi.ptr(prob.kp),
                                       _capi.ptr(prob.k0), _capi.ptr(S), _capi.ptr(status), _capi.ptr(ws), ws.numel(),
-                                      _capi.stream_ptr()), "khp_layer_smatrix")
+                                      _capi.stream_ptr())
+    _capi.check(code, "khp_layer_smatrix")
     return S
 
 
@@ -235,10 +285,12 @@ def closed_form(struct: StructureGPU, kind, eps, depth, prob: Problems, status, 
         V = torch.empty_like(W)
         lam = torch.empty((B, n), dtype=C128, device=dev)
     lib = _capi.load()
-    _capi.check(lib.khp_closed_form_smatrix(B, nh, _KIND[kind], _capi.ptr(e), _capi.ptr(d), _capi.ptr(struct.gx),
+    with _stage("khp_closed_form_smatrix"):
+        code = lib.khp_closed_form_smatrix(B, nh, _KIND[kind], _capi.ptr(e), _capi.ptr(d), _capi.ptr(struct.gx),
                                             _capi.ptr(struct.gy), _capi.ptr(prob.kp), _capi.ptr(prob.k0), _capi.ptr(S),
                                             _capi.ptr(W), _capi.ptr(V), _capi.ptr(lam), _capi.ptr(status),
-                                            _capi.stream_ptr()), "khp_closed_form_smatrix")
+                                            _capi.stream_ptr())
+    _capi.check(code, "khp_closed_form_smatrix")
     return S, W, V, lam
 
 
@@ -250,8 +302,10 @@ def star(SA, SB, status, out=None):
     lib = _capi.load()
     ws = workspace(lib.khp_star_product_workspace(B, n), SA.device)
     nn4 = 4 * n * n
-    _capi.check(lib.khp_star_product(B, n, _capi.ptr(SA), nn4, _capi.ptr(SB), nn4, _capi.ptr(out), _capi.ptr(status),
-                                     _capi.ptr(ws), ws.numel(), _capi.stream_ptr()), "khp_star_product")
+    with _stage("khp_star_product"):
+        code = lib.khp_star_product(B, n, _capi.ptr(SA), nn4, _capi.ptr(SB), nn4, _capi.ptr(out), _capi.ptr(status),
+                                     _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+    _capi.check(code, "khp_star_product")
     return out
 
 
@@ -275,10 +329,12 @@ def flux(struct: StructureGPU, Stot, prob: Problems, epsi, epse, orders=False):
         to = torch.empty((B, nh), dtype=F64, device=dev)
     epsi, epse = complex(epsi), complex(epse)
     lib = _capi.load()
-    _capi.check(lib.khp_flux(B, struct.pw[0], struct.pw[1], _capi.ptr(Stot), 4 * n * n, _capi.ptr(struct.gx),
+    with _stage("khp_flux"):
+        code = lib.khp_flux(B, struct.pw[0], struct.pw[1], _capi.ptr(Stot), 4 * n * n, _capi.ptr(struct.gx),
                              _capi.ptr(struct.gy), _capi.ptr(prob.kp), _capi.ptr(prob.k0), _capi.ptr(prob.te),
                              _capi.ptr(prob.tm), epsi.real, epsi.imag, epse.real, epse.imag, _capi.ptr(R), _capi.ptr(T),
-                             _capi.ptr(ro), _capi.ptr(to), _capi.stream_ptr()), "khp_flux")
+                             _capi.ptr(ro), _capi.ptr(to), _capi.stream_ptr())
+    _capi.check(code, "khp_flux")
     return R, T, ro, to
 
 

@@ -73,7 +73,6 @@ def fourier_fields(cl, zs, incident_fields):
     st = [cl._states[nm] for nm in names]
     sl = [cl._fwd[i][0] for i in order]
     sr = [cl._rev[i][0] for i in order]
-    keep = (sl, sr)  # noqa: F841  (tensors stay alive while their pointers are in use)
     lib = _capi.load()
     sp = _capi.stream_ptr()
     kp = torch.view_as_real(prob.kp[0]).contiguous()
@@ -84,22 +83,27 @@ def fourier_fields(cl, zs, incident_fields):
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     ws = engine.workspace(lib.khp_fields_amplitudes_workspace(L, nh), dev)
     vref = cl._states["Sref"].V[0]
-    _capi.check(lib.khp_fields_amplitudes(
-        L, nh, _capi.ptr(_i64([s.data_ptr() for s in sl], dev)), _capi.ptr(_i64([s.data_ptr() for s in sr], dev)),
-        _capi.ptr(_i64([s.W[0].data_ptr() for s in st], dev)), _capi.ptr(_i64([s.V[0].data_ptr() for s in st], dev)),
-        _capi.ptr(vref), _capi.ptr(inc), _capi.ptr(struct.gx), _capi.ptr(struct.gy), _capi.ptr(kp), _capi.ptr(k0t),
-        _capi.ptr(amps), _capi.ptr(status), _capi.ptr(ws), ws.numel(), sp), "khp_fields_amplitudes")
-    ic_ptr = [s.IC.data_ptr() if torch.is_tensor(s.IC) else 0 for s in st]
+    # Every argument tensor is held in a local until the launches are enqueued: a temporary
+    # would return its storage to the caching allocator while its address is still in use.
+    sl_p = _i64([s.data_ptr() for s in sl], dev)
+    sr_p = _i64([s.data_ptr() for s in sr], dev)
+    w_p = _i64([s.W[0].data_ptr() for s in st], dev)
+    v_p = _i64([s.V[0].data_ptr() for s in st], dev)
+    lam_p = _i64([s.lam[0].data_ptr() for s in st], dev)
+    ic_p = _i64([s.IC.data_ptr() if torch.is_tensor(s.IC) else 0 for s in st], dev)
     ic_sc = torch.tensor([0j if torch.is_tensor(s.IC) else complex(s.IC) for s in st], dtype=torch.complex128,
                          device=dev)
+    slot_t = torch.tensor(slot_of_z, dtype=torch.int32, device=dev)
+    zbar_t = torch.tensor(zbar, dtype=torch.float64, device=dev)
+    _capi.check(lib.khp_fields_amplitudes(
+        L, nh, _capi.ptr(sl_p), _capi.ptr(sr_p), _capi.ptr(w_p), _capi.ptr(v_p), _capi.ptr(vref), _capi.ptr(inc),
+        _capi.ptr(struct.gx), _capi.ptr(struct.gy), _capi.ptr(kp), _capi.ptr(k0t), _capi.ptr(amps),
+        _capi.ptr(status), _capi.ptr(ws), ws.numel(), sp), "khp_fields_amplitudes")
     ff = torch.empty((len(zs), 6, nh), dtype=torch.complex128, device=dev)
     _capi.check(lib.khp_fields_fourier(
-        len(zs), nh, _capi.ptr(torch.tensor(slot_of_z, dtype=torch.int32, device=dev)),
-        _capi.ptr(torch.tensor(zbar, dtype=torch.float64, device=dev)),
-        _capi.ptr(_i64([s.W[0].data_ptr() for s in st], dev)), _capi.ptr(_i64([s.V[0].data_ptr() for s in st], dev)),
-        _capi.ptr(_i64([s.lam[0].data_ptr() for s in st], dev)), _capi.ptr(_i64(ic_ptr, dev)), _capi.ptr(ic_sc),
-        _capi.ptr(amps), _capi.ptr(struct.gx), _capi.ptr(struct.gy), _capi.ptr(kp), _capi.ptr(k0t), _capi.ptr(ff), sp),
-        "khp_fields_fourier")
+        len(zs), nh, _capi.ptr(slot_t), _capi.ptr(zbar_t), _capi.ptr(w_p), _capi.ptr(v_p), _capi.ptr(lam_p),
+        _capi.ptr(ic_p), _capi.ptr(ic_sc), _capi.ptr(amps), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
+        _capi.ptr(kp), _capi.ptr(k0t), _capi.ptr(ff), sp), "khp_fields_fourier")
     word = int(status.item())
     if word:
         raise _capi.KhpError(f"fields: {_capi.decode_status(word)}")
@@ -117,11 +121,11 @@ def idft(cl, ff, x, y, kp=None):
     kpt = torch.tensor([complex(kpv[0]), complex(kpv[1])], dtype=torch.complex128, device=dev)
     rows = ff.reshape(-1, struct.nh).contiguous()
     out = torch.empty((rows.shape[0], xs.numel()), dtype=torch.complex128, device=dev)
+    kpr = torch.view_as_real(kpt).contiguous()
     lib = _capi.load()
     _capi.check(lib.khp_fields_idft(rows.shape[0], struct.nh, _capi.ptr(rows), _capi.ptr(struct.gx),
-                                    _capi.ptr(struct.gy), _capi.ptr(torch.view_as_real(kpt).contiguous()),
-                                    xs.numel(), _capi.ptr(xs), _capi.ptr(ys), _capi.ptr(out), _capi.stream_ptr()),
-                "khp_fields_idft")
+                                    _capi.ptr(struct.gy), _capi.ptr(kpr), xs.numel(), _capi.ptr(xs), _capi.ptr(ys),
+                                    _capi.ptr(out), _capi.stream_ptr()), "khp_fields_idft")
     return out.reshape(rows.shape[0], *shape)
 
 

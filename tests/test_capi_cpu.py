@@ -13,7 +13,7 @@ def _declared():
     for fn in os.listdir(os.path.join(ROOT, "include")):
         if fn.endswith(".h"):
             text = open(os.path.join(ROOT, "include", fn)).read()
-            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(khp_\w+)\s*\(", text, re.M))
+            names |= set(re.findall(r"^[A-Za-z_][\w \*]*?\b(khp_\w+)\s*\(", text, re.M))
     return names
 
 
