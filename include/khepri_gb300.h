@@ -114,6 +114,22 @@ int khp_star_product(int64_t batch, int32_t n, const double* SA, int64_t sa_stri
                      int64_t sb_stride, double* S, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 /*
+ * Star product without a caller-supplied workspace.  No counterpart in the reference: it
+ * serves callers that cannot allocate or lend device memory (a host whose device memory is
+ * fully partitioned up front, or a latency-critical loop where cudaMalloc, which may
+ * synchronise the device, is not allowed).  Same arguments and result as khp_star_product
+ * minus the workspace.  Its scratch is a fixed device array of KHP_NOALLOC_SCRATCH_BYTES
+ * inside libkhp, held by every GPU that loads the library until the process exits; batches
+ * whose khp_star_product_workspace(batch, n) exceeds it return KHP_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address (with that device current),
+ * so make it before any stream capture.  All calls share the one array and it keeps the last
+ * call's contents: calls that overlap on the GPU (other streams, other host threads) race.
+ */
+#define KHP_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int khp_star_product_noalloc(int64_t batch, int32_t n, const double* SA, int64_t sa_stride, const double* SB,
+                             int64_t sb_stride, double* S, int32_t* status, void* stream);
+
+/*
  * Reflected and transmitted power.  Replaces Crystal.poynting_flux_end
  * (khepri/crystal.py:363-396) with the source vector of alternative.incident
  * (alternative.py:101-128) and alternative.poynting_fluxes (alternative.py:235-245).

@@ -36,6 +36,7 @@ _SIGNATURES = {
                                                _c_p, _c_p, _c_p, _c_p]),
     "khp_star_product_workspace": (_c_sz, [_c_i64, _c_i32]),
     "khp_star_product": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_star_product_noalloc": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_p]),
     "khp_flux": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_d, _c_d,
                                 _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p]),
     "khp_fields_amplitudes_workspace": (_c_sz, [_c_i64, _c_i32]),
