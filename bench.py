@@ -48,12 +48,19 @@ FLOPS_PER_CALL = {
 }
 
 
+def solve_batched_flops(n, nmaps, npattern, nhomog):
+    """Algorithmic flops per problem of khp_solve_batched: per distinct map the modes (117 n^3)
+    and W^-1, V^-1 (2 x 10.67 n^3); per patterned layer 4 GEMMs + 2 LU + 2 right-solves
+    (53.3 n^3); per homogeneous layer an LU and a right-solve (10.67 n^3); the incidence LU."""
+    return n ** 3 * (nmaps * (117.0 + 21.33) + 53.33 * npattern + 10.67 * nhomog + 2.67)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=192)
+    ap.add_argument("--batch", type=int, default=304)
     ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=6)
     return ap.parse_args()
@@ -218,8 +225,12 @@ def run_gpu(args):
     statuses = [torch.zeros(B, dtype=torch.int32, device=dev) for _ in range(nsteps)]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 
+    plan = batch.StackPlan(struct, specs, st.stack)
+    npat = int((plan.kinds == 1).sum())
+    FLOPS_PER_CALL["khp_solve_batched"] = solve_batched_flops(N_MAT, plan.nmaps, npat, len(plan.kinds) - npat)
+
     def step(k):
-        return batch.solve_chunk_both_pols(struct, specs, st.stack, probs[k], statuses[k])
+        return batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k])
 
     for k in range(args.warmup):
         step(k)
@@ -281,7 +292,7 @@ def run_gpu(args):
     for k in range(e2e_steps):
         idx = chunk(args.warmup + k)
         batch.solve_rt(st.pw, st.layers, st.stack, wl_all[idx], kp_all[idx], chunk=B, struct=struct,
-                       strict=False, both_pols=True)
+                       strict=False, both_pols=True, method="gamma")
     torch.cuda.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -305,6 +316,7 @@ def run_gpu(args):
             "config": {"workload": "batched sweep 11x11 (n=242), 256x256 multi-disc map, [P,U,P,U,P], 64 f x "
                                    "32x32 k, both polarisations per S-matrix",
                        "batch": B, "harmonics": "11x11", "precision": "fp64 (complex128) throughout",
+                       "method": "reflection-matrix recursion (khp_solve_batched), one eigensolve per problem",
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
                        "grad": "solve+grad/s not measured by this bench"},

@@ -114,6 +114,28 @@ int khp_star_product(int64_t batch, int32_t n, const double* SA, int64_t sa_stri
                      int64_t sb_stride, double* S, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 /*
+ * Batched reflection and transmission of one layer stack for many problems, in one call.
+ * Replaces the per-point loop Crystal.set_source -> solve -> poynting_flux_end
+ * (khepri/crystal.py:180-206, 363-396; README.md:52-58) when only R and T are wanted: instead
+ * of every layer's S-matrix and the four-block chain (alternative.py:19-30, 181-195;
+ * layer.py:35-60) it runs a backward reflection-matrix recursion and a forward pass of the two
+ * source columns (same continuity conditions; patterned layers handled in their mode basis).
+ *   layer_kind, layer_map, layer_eps, layer_depth: HOST arrays [nlayers] from the incidence side;
+ *     kind 0 = uniform (eps: complex pair), 1 = patterned (map index into conv/hx/hy);
+ *   conv, hx, hy: device complex [nmaps][nh][nh] from khp_convmat / khp_structure_prep;
+ *   kp: complex [batch][2]; k0: [batch]; te, tm: complex [batch][npol] (npol polarisations
+ *   share one recursion);  R, T: real [batch][npol].
+ */
+size_t khp_solve_batched_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
+                                   const int32_t* layer_map);
+int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                      const int32_t* layer_map, const double* layer_eps, const double* layer_depth, int64_t nmaps,
+                      const double* conv, const double* hx, const double* hy, const double* gx, const double* gy,
+                      double epsi_re, double epsi_im, double epse_re, double epse_im, const double* kp,
+                      const double* k0, int32_t npol, const double* te, const double* tm, double* R, double* T,
+                      int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
  * Star product without a caller-supplied workspace.  No counterpart in the reference: it
  * serves callers that cannot allocate or lend device memory (a host whose device memory is
  * fully partitioned up front, or a latency-critical loop where cudaMalloc, which may

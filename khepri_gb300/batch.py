@@ -8,6 +8,8 @@ that share a pixmap share one eigensolve per problem.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -59,17 +61,108 @@ def solve_chunk_both_pols(struct, specs, stack, prob, status, epsi=1.0, epse=1.0
     return torch.stack([out[0][0], out[1][0]], 1), torch.stack([out[0][1], out[1][1]], 1)
 
 
+class StackPlan:
+    """Host description of a layer stack for khp_solve_batched, with the stacked per-pixmap
+    device matrices (C, Hx, Hy) it reads."""
+
+    def __init__(self, struct, specs, stack):
+        kinds, maps, eps, depth = [], [], [], []
+        keys, entries = [], []
+        for name in stack:
+            sp = specs[name]
+            if sp.kind == "pixmap":
+                e = struct.prepare_map(sp.eps)
+                if e["key"] not in keys:
+                    keys.append(e["key"])
+                    entries.append(e)
+                kinds.append(1)
+                maps.append(keys.index(e["key"]))
+                eps.append(0j)
+            else:
+                kinds.append(0)
+                maps.append(0)
+                eps.append(complex(sp.eps))
+            depth.append(float(sp.depth))
+        self.kinds = np.asarray(kinds, dtype=np.int32)
+        self.maps = np.asarray(maps, dtype=np.int32)
+        self.eps = np.asarray(eps, dtype=np.complex128)
+        self.depth = np.asarray(depth, dtype=np.float64)
+        self.nmaps = len(entries)
+        if entries:
+            self.conv = torch.cat([e["conv"] for e in entries]).contiguous()
+            self.hx = torch.cat([e["hx"] for e in entries]).contiguous()
+            self.hy = torch.cat([e["hy"] for e in entries]).contiguous()
+        else:
+            self.conv = self.hx = self.hy = None
+
+
+def _host(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None):
+    """R, T of one chunk by the reflection-matrix recursion (khp_solve_batched).
+
+    te, tm: optional [B, npol] complex device tensors (default: prob.te, prob.tm as one
+    polarisation); the recursion runs once and every polarisation is read from it.
+    Returns R, T of shape [B] (one polarisation) or [B, npol].
+    """
+    B = prob.batch
+    dev = struct.device
+    one_pol = te is None
+    if one_pol:
+        te, tm = prob.te.reshape(B, 1), prob.tm.reshape(B, 1)
+    te, tm = te.contiguous(), tm.contiguous()
+    npol = te.shape[1]
+    R = torch.empty((B, npol), dtype=torch.float64, device=dev)
+    T = torch.empty((B, npol), dtype=torch.float64, device=dev)
+    lib = _capi.load()
+    L = len(plan.kinds)
+    ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)), dev)
+    epsi, epse = complex(epsi), complex(epse)
+    with engine._stage("khp_solve_batched"):
+        code = lib.khp_solve_batched(B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps),
+                                     _host(plan.eps), _host(plan.depth), plan.nmaps, _capi.ptr(plan.conv),
+                                     _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx),
+                                     _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
+                                     _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm),
+                                     _capi.ptr(R), _capi.ptr(T), _capi.ptr(status), _capi.ptr(ws), ws.numel(),
+                                     _capi.stream_ptr())
+    _capi.check(code, "khp_solve_batched")
+    if one_pol:
+        return R[:, 0], T[:, 0]
+    return R, T
+
+
+def both_pol_weights(B, device):
+    """te, tm [B, 2] for the polarisations (te, tm) = (1, 0) and (0, 1)."""
+    te = torch.zeros((B, 2), dtype=torch.complex128, device=device)
+    tm = torch.zeros((B, 2), dtype=torch.complex128, device=device)
+    te[:, 0] = 1.0
+    tm[:, 1] = 1.0
+    return te, tm
+
+
+def solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi=1.0, epse=1.0):
+    """R, T [B, 2] for (te, tm) = (1, 0) and (0, 1) from one recursion per problem."""
+    te, tm = both_pol_weights(prob.batch, struct.device)
+    return solve_chunk_gamma(struct, plan, prob, status, epsi, epse, te, tm)
+
+
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
-             chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False):
+             chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False, method="gamma"):
     """R and T of every problem (host numpy arrays); problems share ``layers``/``stack``.
 
     layers: name -> ("pixmap", eps_map, depth) | ("uniform", eps, depth); stack: layer names
     from the incidence side.  wavelengths [P], kp [P, 2] (absolute, complex allowed), te/tm
     scalars or [P].  Returns (R, T, status) or (R, T, r_orders, t_orders, status) with
-    ``orders=True``.  ``both_pols=True`` solves each S-matrix once and returns R, T of shape
-    [P, 2] for (te, tm) = (1, 0) and (0, 1).  With ``strict`` a non-zero per-problem status
-    raises KhpError.
+    ``orders=True``.  ``both_pols=True`` returns R, T of shape [P, 2] for (te, tm) = (1, 0)
+    and (0, 1).  ``method``: "gamma" (reflection-matrix recursion, khp_solve_batched; R and T
+    only) or "chain" (layer S-matrices and the star-product chain, as the reference; needed for
+    per-order powers).  With ``strict`` a non-zero per-problem status raises KhpError.
     """
+    if orders:
+        method = "chain"
     _capi.require_cuda()
     wl = np.atleast_1d(np.asarray(wavelengths, dtype=float))
     P = wl.shape[0]
@@ -79,6 +172,7 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     if struct is None:
         struct = engine.StructureGPU(pw, engine.lattice_vectors(lattice), device)
     specs = _specs(layers, epsi, epse)
+    plan = StackPlan(struct, specs, stack) if method == "gamma" else None
     R = np.empty((P, 2) if both_pols else P)
     T = np.empty((P, 2) if both_pols else P)
     ro = np.empty((P, struct.nh)) if orders else None
@@ -88,7 +182,13 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
         e = min(P, s + chunk)
         prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
         status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
-        if both_pols:
+        if method == "gamma":
+            r_o = t_o = None
+            if both_pols:
+                r, t = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse)
+            else:
+                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse)
+        elif both_pols:
             r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
             r_o = t_o = None
         else:

@@ -117,6 +117,36 @@ KHP_HD void team_getrs(const Team& t, const cplx<T>* A, int64_t lda, int n, cons
   }
 }
 
+// Solve X A = B in place in B (m x n rows, leading dimension ldb) given team_getrf's factors
+// of A: L U = Pi A with Pi the recorded row interchanges, so X = ((B U^-1) L^-1) Pi.
+// Each thread owns whole rows of B (no barriers).
+template <class Team, typename T>
+KHP_HD void team_getrs_right(const Team& t, const cplx<T>* A, int64_t lda, int n, const int* piv, cplx<T>* B,
+                             int64_t ldb, int m) {
+  for (int i = t.tid(); i < m; i += t.size()) {
+    cplx<T>* x = B + (int64_t)i * ldb;
+    for (int j = 0; j < n; ++j) {  // z U = b
+      cplx<T> acc = x[j];
+      for (int k = 0; k < j; ++k) fms_acc(acc, x[k], A[(int64_t)k * lda + j]);
+      x[j] = cdiv(acc, A[(int64_t)j * lda + j]);
+    }
+    for (int j = n - 2; j >= 0; --j) {  // y L = z (L unit lower)
+      cplx<T> acc = x[j];
+      for (int k = j + 1; k < n; ++k) fms_acc(acc, x[k], A[(int64_t)k * lda + j]);
+      x[j] = acc;
+    }
+    for (int k = n - 1; k >= 0; --k) {  // x = y Pi: undo the interchanges, last first
+      const int p = piv[k];
+      if (p != k) {
+        const cplx<T> a = x[k];
+        x[k] = x[p];
+        x[p] = a;
+      }
+    }
+  }
+  t.sync();
+}
+
 template <class Team, typename T>
 KHP_HD void team_set_identity(const Team& t, cplx<T>* B, int64_t ld, int n, int m) {
   for (int e = t.tid(); e < n * m; e += t.size()) {

@@ -219,3 +219,58 @@ def test_fields_without_retained_layers(khp):
     E0, H0 = ref.fields_volume(x, y, x[0])
     np.testing.assert_allclose(E, E0, atol=1e-12)
     np.testing.assert_allclose(H, H0, atol=1e-12)
+
+
+def test_gamma_recursion_oblique_media(khp, golden):
+    """khp_solve_batched (reflection-matrix recursion) on the oblique/complex-media golden cases."""
+    from khepri_gb300 import batch, engine
+    g = golden("oblique_5x5")
+    emap, d, eu = g["eps_map"], g["depths"], g["eps_u"]
+    layers = {"P1": ("pixmap", emap, d[0]), "U1": ("uniform", eu[0], d[1]), "P2": ("pixmap", emap, d[2]),
+              "U2": ("uniform", eu[1], d[3]), "P3": ("pixmap", emap, d[4])}
+    for i in range(len(g["R"])):
+        kp = engine.compute_kplanar(g["epsi"][i], g["wavelength"][i], g["theta"][i], g["phi"][i])
+        R, T, s = batch.solve_rt((5, 5), layers, ["P1", "U1", "P2", "U2", "P3"], [g["wavelength"][i]], [kp],
+                                 g["te"][i], g["tm"][i], epsi=g["epsi"][i], epse=g["epse"][i], method="gamma")
+        assert abs(R[0] - g["R"][i]) < TIGHT and abs(T[0] - g["T"][i]) < TIGHT
+
+
+def test_gamma_recursion_both_polarisations_11x11(khp, golden):
+    from khepri_gb300 import batch, workloads
+    g = golden("batched_11x11")
+    st = workloads.batched_structure(int(g["seed"]))
+    wl, kp = workloads.batched_problems()
+    p = g["problems"]
+    R, T, s = batch.solve_rt(st.pw, st.layers, st.stack, wl[p], kp[p], both_pols=True, method="gamma")
+    np.testing.assert_allclose(R[:, 0], g["R_te"], atol=RT_TOL)
+    np.testing.assert_allclose(T[:, 0], g["T_te"], atol=RT_TOL)
+    np.testing.assert_allclose(R[:, 1], g["R_tm"], atol=RT_TOL)
+    np.testing.assert_allclose(T[:, 1], g["T_tm"], atol=RT_TOL)
+    assert np.abs(R + T - 1).max() < 1e-8
+
+
+def test_gamma_matches_chain_hexagonal_and_uneven(khp, golden):
+    from khepri_gb300 import batch, workloads
+    g = golden("hex_3x3")
+    R, T, s = batch.solve_rt((3, 3), {"H": ("pixmap", g["eps_map"], 0.4)}, ["H"], g["wavelength"], g["kp"], 1.0, 1.0,
+                             lattice="hexagonal", method="gamma")
+    assert np.abs(R - g["R"]).max() < TIGHT and np.abs(T - g["T"]).max() < TIGHT
+    u = golden("uneven_small")
+    structs = workloads.uneven_structures(int(u["count"]), seed=int(u["seed"]), n_pix=int(u["n_pix"]),
+                                          max_pw=int(u["max_pw"]), max_layers=int(u["max_layers"]))
+    for i, (st, wl, kp) in enumerate(structs):
+        R, T, s = batch.solve_rt(st.pw, st.layers, st.stack, [wl], [kp], 1.0, 1.0, method="gamma")
+        assert abs(R[0] - u["R"][i]) < 1e-8 and abs(T[0] - u["T"][i]) < 1e-8
+
+
+def test_gamma_vs_chain_sweep_chunk(khp):
+    """The two batched formulations on 64 problems of the 11x11 sweep (lossless: R + T = 1)."""
+    from khepri_gb300 import batch, workloads
+    st = workloads.batched_structure(3)
+    wl, kp = workloads.batched_problems()
+    idx = np.arange(40000, 40064)
+    Rg, Tg, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="gamma")
+    Rc, Tc, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="chain")
+    ok = np.isfinite(Rc)
+    assert np.abs(Rg[ok] - Rc[ok]).max() < RT_TOL and np.abs(Tg[ok] - Tc[ok]).max() < RT_TOL
+    assert np.abs(Rg[ok] + Tg[ok] - 1).max() < 1e-8
