@@ -36,12 +36,15 @@ __global__ void __launch_bounds__(kTeamThreads) k_geev(int n, cplx<T>* A, int64_
                                                         cplx<T>* W, int64_t ldw, int64_t bsW, cplx<T>* lam,
                                                         int64_t bsLam, int* info) {
   __shared__ TeamShared sh;
+  __shared__ cplx<T> win[(KHP_HQR_WIN + 2) * (KHP_HQR_WIN + 2)];
+  __shared__ cplx<T> rs[KHP_HQR_WIN];
+  __shared__ T rc[KHP_HQR_WIN];
   extern __shared__ unsigned char dyn[];
   cplx<T>* vbuf = reinterpret_cast<cplx<T>*>(dyn);
   TeamCta t;
   const int64_t b = blockIdx.x;
   const int st = team_geev(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, W + b * bsW, ldw, lam + b * bsLam,
-                           vbuf, &sh);
+                           vbuf, win, rc, rs, &sh);
   if (threadIdx.x == 0 && st) info[b] |= st;
 }
 

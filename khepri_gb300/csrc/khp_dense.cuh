@@ -369,6 +369,159 @@ KHP_HD int team_hqr(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, in
   return sh->bi[3];
 }
 
+// Windowed form of the same single-shift QR sweep.  The bulge is chased through a window of
+// at most KHP_HQR_WIN rotations held in shared memory (win: (KHP_HQR_WIN + 2)^2 complex), the
+// rotations are recorded (rc, rs), and only then applied to the parts of H and Z outside the
+// window in one rolling pass per row or column (two live values per thread).  Same rotations,
+// same order of application per element as team_hqr; per-step work touches shared memory only.
+#ifndef KHP_HQR_WIN
+#define KHP_HQR_WIN 32
+#endif
+
+template <class Team, typename T>
+KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, int lo, int hi,
+                             cplx<T> mu, cplx<T>* win, T* rc, cplx<T>* rs, TeamShared* sh) {
+  constexpr int WS = KHP_HQR_WIN + 2;
+  int k0 = lo;
+  while (k0 < hi) {
+    const int k1 = (k0 + KHP_HQR_WIN - 1 < hi) ? k0 + KHP_HQR_WIN - 1 : hi;
+    const int r0 = k0, r1 = (k1 + 1 < hi) ? k1 + 1 : hi;
+    const int c0 = (k0 > lo) ? k0 - 1 : k0;
+    const int nr = r1 - r0 + 1, nc = k1 - c0 + 1;
+    for (int e = t.tid(); e < nr * nc; e += t.size()) {
+      const int i = e / nc, j = e % nc;
+      win[i * WS + j] = H[(int64_t)(r0 + i) * ld + c0 + j];
+    }
+    t.sync();
+    for (int k = k0; k < k1; ++k) {
+      const int lk = k - r0;       // window row of k
+      const int ck = k - c0;       // window column of k
+      if (t.tid() == 0) {
+        cplx<T> x, y;
+        if (k == lo) {
+          x = win[lk * WS + ck] - mu;
+          y = win[(lk + 1) * WS + ck];
+        } else {
+          x = win[lk * WS + ck - 1];
+          y = win[(lk + 1) * WS + ck - 1];
+        }
+        T c;
+        cplx<T> s, r;
+        givens(x, y, c, s, r);
+        if (k > lo) {
+          win[lk * WS + ck - 1] = r;
+          win[(lk + 1) * WS + ck - 1] = mk(T(0));
+        }
+        rc[k - k0] = c;
+        rs[k - k0] = s;
+      }
+      t.sync();
+      const T c = rc[k - k0];
+      const cplx<T> s = rs[k - k0];
+      // row rotation from column k (column k-1 already holds r and 0 when k > lo)
+      for (int j = ck + t.tid(); j < nc; j += t.size()) {
+        const cplx<T> h1 = win[lk * WS + j], h2 = win[(lk + 1) * WS + j];
+        win[lk * WS + j] = c * h1 + s * h2;
+        win[(lk + 1) * WS + j] = c * h2 - conj_mul(s, h1);
+      }
+      t.sync();
+      const int ilast = ((k + 2 < hi) ? k + 2 : hi) - r0;
+      for (int i = t.tid(); i <= ilast; i += t.size()) {
+        const cplx<T> g1 = win[i * WS + ck], g2 = win[i * WS + ck + 1];
+        win[i * WS + ck] = c * g1 + mul_conj(g2, s);
+        win[i * WS + ck + 1] = c * g2 - s * g1;
+      }
+      t.sync();
+    }
+    for (int e = t.tid(); e < nr * nc; e += t.size()) {
+      const int i = e / nc, j = e % nc;
+      H[(int64_t)(r0 + i) * ld + c0 + j] = win[i * WS + j];
+    }
+    const int nrot = k1 - k0;
+    // rows k0..k1, columns right of the window: left rotations, rolling down the column
+    for (int j = k1 + 1 + t.tid(); j < n; j += t.size()) {
+      cplx<T> a = H[(int64_t)k0 * ld + j];
+      for (int q = 0; q < nrot; ++q) {
+        const T c = rc[q];
+        const cplx<T> s = rs[q];
+        const cplx<T> b = H[(int64_t)(k0 + q + 1) * ld + j];
+        H[(int64_t)(k0 + q) * ld + j] = c * a + s * b;
+        a = c * b - conj_mul(s, a);
+      }
+      H[(int64_t)k1 * ld + j] = a;
+    }
+    // rows above the window (columns k0..k1) and every row of Z: right rotations, rolling along the row
+    for (int i = t.tid(); i < r0 + n; i += t.size()) {
+      cplx<T>* row = (i < r0) ? H + (int64_t)i * ld : Z + (int64_t)(i - r0) * ldz;
+      cplx<T> a = row[k0];
+      for (int q = 0; q < nrot; ++q) {
+        const T c = rc[q];
+        const cplx<T> s = rs[q];
+        const cplx<T> b = row[k0 + q + 1];
+        row[k0 + q] = c * a + mul_conj(b, s);
+        a = c * b - s * a;
+      }
+      row[k1] = a;
+    }
+    t.sync();
+    k0 = k1;
+  }
+}
+
+template <class Team, typename T>
+KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* win, T* rc,
+                        cplx<T>* rs, TeamShared* sh) {
+  const T smlnum = Eps<T>::safemin * (T(n) / Eps<T>::ulp);
+  const int cap = 30 * n + 60;
+  int its = 0, total = 0;  // iteration counters, thread 0 only
+  if (t.tid() == 0) {
+    sh->bi[2] = n - 1;  // hi
+    sh->bi[3] = 0;      // status
+  }
+  t.sync();
+  while (true) {
+    const int hi = sh->bi[2];
+    if (hi < 0) break;
+    // Largest k in [1, hi] with a negligible subdiagonal H[k][k-1], searched by the whole team.
+    T best = T(-1);
+    int bk = 0;
+    for (int k = 1 + t.tid(); k <= hi; k += t.size()) {
+      if (T(k) > best && hqr_negligible(H, ld, k, hi, smlnum)) {
+        best = T(k);
+        bk = k;
+      }
+    }
+    team_argmax(t, best, bk, sh);
+    const int l = best > T(0) ? bk : 0;
+    if (t.tid() == 0) {
+      if (l > 0) H[(int64_t)l * ld + l - 1] = mk(T(0));
+      if (l == hi) {
+        sh->bi[2] = hi - 1;
+        its = 0;
+        sh->bi[0] = 1;
+      } else {
+        ++its;
+        ++total;
+        if (total > cap) {
+          sh->bi[3] |= KHP_BIT_NOT_CONVERGED;
+          sh->bi[2] = -1;
+          sh->bi[0] = 2;
+        } else {
+          const cplx<T> mu = hqr_shift(H, ld, l, hi, its);
+          sh->bi[0] = 0;
+          sh->bi[1] = l;
+          sh->bd[0] = (double)mu.re;
+          sh->bd[1] = (double)mu.im;
+        }
+      }
+    }
+    t.sync();
+    if (sh->bi[0] != 0) continue;
+    hqr_window_sweep(t, H, ld, n, Z, ldz, sh->bi[1], hi, mk((T)sh->bd[0], (T)sh->bd[1]), win, rc, rs, sh);
+  }
+  return sh->bi[3];
+}
+
 // ------------------------------------------------------------------------------------------
 // Eigenvectors of an upper triangular T (in place): lam[k] = T[k][k]; the strictly upper part
 // becomes X with T X = X diag(lam), X unit upper triangular.  All eigenvectors are built at
@@ -425,12 +578,13 @@ KHP_HD void team_backtransform(const Team& t, const cplx<T>* Z, int64_t ldz, con
 }
 
 // Full eigendecomposition A W = W diag(lam).  A is overwritten (Schur factor, then X);
-// Z: n x n scratch; vbuf: n scratch.  Returns status bits.
+// Z: n x n scratch; vbuf: n scratch; win, rc, rs: window scratch of team_hqr_win.
+// Returns status bits.
 template <class Team, typename T>
 KHP_HD int team_geev(const Team& t, cplx<T>* A, int64_t lda, int n, cplx<T>* Z, int64_t ldz, cplx<T>* W,
-                     int64_t ldw, cplx<T>* lam, cplx<T>* vbuf, TeamShared* sh) {
+                     int64_t ldw, cplx<T>* lam, cplx<T>* vbuf, cplx<T>* win, T* rc, cplx<T>* rs, TeamShared* sh) {
   team_gehrd(t, A, lda, n, Z, ldz, vbuf, sh);
-  const int st = team_hqr(t, A, lda, n, Z, ldz, sh);
+  const int st = team_hqr_win(t, A, lda, n, Z, ldz, win, rc, rs, sh);
   team_trevc(t, A, lda, n, lam);
   team_backtransform(t, Z, ldz, A, lda, n, W, ldw);
   return st;

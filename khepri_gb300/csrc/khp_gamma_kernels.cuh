@@ -1,0 +1,329 @@
+// Kernels of the batched reflection-matrix recursion (khp_solve_batched, khp_solve_batched_mixed):
+// mode assembly and post-processing, free-space V0 products, closed-form homogeneous blocks,
+// the per-harmonic structured products of the recursion, and the two-column flux.
+// Templated on the storage type T of the dense matrices; per-harmonic physics in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "khp_dense.cuh"
+#include "khp_launch.h"
+#include "khp_physics.cuh"
+
+namespace khp {
+namespace {
+
+using cd = cplx<double>;
+using phys::M2;
+
+inline int grid_for(int64_t total) { return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 32)); }
+
+template <typename T>
+__device__ __forceinline__ cplx<T> to_t(cd z) { return mk((T)z.re, (T)z.im); }
+template <typename T>
+__device__ __forceinline__ cd to_d(cplx<T> z) { return mk((double)z.re, (double)z.im); }
+
+// Element (r, c) of a 2x2 block: r, c in {0, 1}.
+__device__ __forceinline__ cd blk(const M2& m, int r, int c) { return r == 0 ? (c == 0 ? m.a : m.b) : (c == 0 ? m.c : m.d); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_getrs_right(int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv,
+                                                      cplx<T>* B, int64_t ldb, int64_t bsB, int m) {
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  team_getrs_right(t, A + b * bsA, lda, n, piv + b * n, B + b * bsB, ldb, m);
+}
+
+template <typename T>
+__global__ void k_convert(int64_t count, const cd* __restrict__ in, cplx<T>* out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = to_t<T>(in[e]);
+}
+
+// M = P Q of one pixmap for every problem (same identity as khp_layer_modes).
+template <typename T>
+__global__ void k_assemble_pq_t(int64_t batch, int nh, const cd* __restrict__ C, const cd* __restrict__ Hx,
+                                const cd* __restrict__ Hy, const double* gx, const double* gy, const double* kp,
+                                const double* k0, cplx<T>* M) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int i = r % nh, j = c % nh;
+    const int bi = r / nh, bj = c / nh;
+    const int64_t mo = (int64_t)i * nh + j;
+    const double k = k0[b];
+    const cd ax = mk(kp[4 * b + 0] / k, kp[4 * b + 1] / k), ay = mk(kp[4 * b + 2] / k, kp[4 * b + 3] / k);
+    cd kxi, kyi;
+    phys::kvec(kp, k0, gx, gy, b, i, kxi, kyi);
+    const bool dg = (i == j);
+    const cd gxv = Hx[mo] * (1.0 / k) + (dg ? ax : mk(0.0));
+    const cd gyv = Hy[mo] * (1.0 / k) + (dg ? ay : mk(0.0));
+    cd v;
+    if (bi == 0 && bj == 0) v = kxi * gxv - C[mo] + (dg ? kyi * kyi : mk(0.0));
+    else if (bi == 0) v = kxi * gyv - (dg ? kxi * kyi : mk(0.0));
+    else if (bj == 0) v = kyi * gxv - (dg ? kxi * kyi : mk(0.0));
+    else v = kyi * gyv - C[mo] + (dg ? kxi * kxi : mk(0.0));
+    M[e] = to_t<T>(v);
+  }
+}
+
+template <typename T>
+__global__ void k_sqrt_lam_t(int64_t count, cplx<T>* lam) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    lam[e] = to_t<T>(csqrt(to_d(lam[e])));
+}
+
+// V = Q W / lam (alternative.py:167-176), CWt = C W_top, CWb = C W_bottom.
+template <typename T>
+__global__ void k_modes_v_t(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
+                            const double* k0, const cplx<T>* __restrict__ W, const cplx<T>* __restrict__ CWt,
+                            const cplx<T>* __restrict__ CWb, const cplx<T>* __restrict__ lam, cplx<T>* V, int* status) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n, hn = (int64_t)nh * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int i = r % nh;
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, i, kx, ky);
+    const cd wt = to_d(W[b * nn + (int64_t)i * n + c]), wb = to_d(W[b * nn + (int64_t)(nh + i) * n + c]);
+    const cd kxy = kx * ky;
+    cd q;
+    if (r < nh) q = kxy * wt - kx * kx * wb + to_d(CWb[b * hn + (int64_t)i * n + c]);
+    else q = ky * ky * wt - to_d(CWt[b * hn + (int64_t)i * n + c]) - kxy * wb;
+    const cd v = cdiv(q, to_d(lam[b * n + c]));
+    V[e] = to_t<T>(v);
+    if (!cfinite(v)) atomicOr(status + b, KHP_BIT_NONFINITE);
+  }
+}
+
+// out = A V0 (V0: free-space modes, one 2x2 block per harmonic).
+template <typename T>
+__global__ void k_v0_right(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
+                           const double* k0, const cplx<T>* __restrict__ A, cplx<T>* out) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int g = c % nh, cb = c / nh;
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
+    const M2 v0 = phys::v0_block(kx, ky);
+    const cd a0 = to_d(A[b * nn + (int64_t)r * n + g]), a1 = to_d(A[b * nn + (int64_t)r * n + nh + g]);
+    out[e] = to_t<T>(a0 * blk(v0, 0, cb) + a1 * blk(v0, 1, cb));
+  }
+}
+
+// out = V0^-1 A.
+template <typename T>
+__global__ void k_v0inv_left(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
+                             const double* k0, const cplx<T>* __restrict__ A, cplx<T>* out) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int g = r % nh, rb = r / nh;
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
+    const M2 vi = phys::inv2(phys::v0_block(kx, ky));
+    const cd a0 = to_d(A[b * nn + (int64_t)g * n + c]), a1 = to_d(A[b * nn + (int64_t)(nh + g) * n + c]);
+    out[e] = to_t<T>(blk(vi, rb, 0) * a0 + blk(vi, rb, 1) * a1);
+  }
+}
+
+// Homogeneous media: per problem and harmonic the four 2x2 blocks of S (double), [batch][nh][4].
+__global__ void k_homog_blocks(int64_t batch, int nh, int kind, cd eps, double depth, const double* gx, const double* gy,
+                               const double* kp, const double* k0, M2* out, int* status) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nh;
+    const int g = (int)(e % nh);
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
+    M2 s[4], vm;
+    cd lm;
+    phys::homogeneous_blocks(kind, kx, ky, eps, depth * k0[b], s, vm, lm);
+    bool fin = true;
+    for (int q = 0; q < 4; ++q) {
+      out[e * 4 + q] = s[q];
+      fin = fin && cfinite(s[q].a) && cfinite(s[q].b) && cfinite(s[q].c) && cfinite(s[q].d);
+    }
+    if (!fin) atomicOr(status + b, KHP_BIT_NONFINITE);
+  }
+}
+
+// Gamma = S11 of a homogeneous medium, densely.
+template <typename T>
+__global__ void k_gamma_from_blocks(int64_t batch, int nh, const M2* __restrict__ S, int q, cplx<T>* G) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int gi = r % nh, gj = c % nh;
+    G[e] = gi == gj ? to_t<T>(blk(S[(b * nh + gi) * 4 + q], r / nh, c / nh)) : mk(T(0));
+  }
+}
+
+// out = I - S22 Gamma (S22 per-harmonic blocks).
+template <typename T>
+__global__ void k_i_minus_sg(int64_t batch, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ G,
+                             cplx<T>* out) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int g = r % nh, rb = r / nh;
+    const M2& s22 = S[(b * nh + g) * 4 + 3];
+    const cd v = blk(s22, rb, 0) * to_d(G[b * nn + (int64_t)g * n + c]) + blk(s22, rb, 1) * to_d(G[b * nn + (int64_t)(nh + g) * n + c]);
+    out[e] = to_t<T>((r == c ? mk(1.0) : mk(0.0)) - v);
+  }
+}
+
+// out = S11 + S12 Z S21 (all S blocks per-harmonic).
+template <typename T>
+__global__ void k_sandwich(int64_t batch, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ Z, cplx<T>* out) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int r = rc / n, c = rc % n;
+    const int gi = r % nh, ri = r / nh, gj = c % nh, cj = c / nh;
+    const M2* Si = S + (b * nh + gi) * 4;
+    const M2* Sj = S + (b * nh + gj) * 4;
+    const cplx<T>* Zb = Z + b * nn;
+    cd acc = gi == gj ? blk(Si[0], ri, cj) : mk(0.0);
+    for (int ra = 0; ra < 2; ++ra) {
+      const cd s12 = blk(Si[1], ri, ra);
+      const int a = ra * nh + gi;
+      const cd z0 = to_d(Zb[(int64_t)a * n + gj]), z1 = to_d(Zb[(int64_t)a * n + nh + gj]);
+      acc += s12 * (z0 * blk(Sj[2], 0, cj) + z1 * blk(Sj[2], 1, cj));
+    }
+    out[e] = to_t<T>(acc);
+  }
+}
+
+// A = F - G (into a), B = F + G (into f).
+template <typename T>
+__global__ void k_diff_sum(int64_t count, cplx<T>* f, const cplx<T>* __restrict__ g, cplx<T>* a) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const cplx<T> fv = f[e], gv = g[e];
+    a[e] = fv - gv;
+    f[e] = fv + gv;
+  }
+}
+
+// rho <- X rho X, X = exp(-lam k0 d) (one depth for the batch).
+template <typename T>
+__global__ void k_xmx_t(int64_t batch, int n, const cplx<T>* __restrict__ lam, double depth, const double* k0, cplx<T>* M) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const double dk = depth * k0[b];
+    const cd xi = cexp(-(to_d(lam[b * n + rc / n]) * dk)), xj = cexp(-(to_d(lam[b * n + rc % n]) * dk));
+    M[e] = to_t<T>(xi * to_d(M[e]) * xj);
+  }
+}
+
+// Two-column vectors [batch][n][2].
+// u = S21 columns c0 and nh + c0 of a homogeneous medium (its response to the unit sources).
+template <typename T>
+__global__ void k_src_cols(int64_t batch, int nh, const M2* __restrict__ S, int q, cplx<T>* u) {
+  const int n = 2 * nh;
+  const int c0 = (nh - 1) / 2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n * 2; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / (2 * n);
+    const int r = (int)((e / 2) % n), col = (int)(e % 2);
+    const int g = r % nh;
+    u[e] = g == c0 ? to_t<T>(blk(S[(b * nh + g) * 4 + q], r / nh, col)) : mk(T(0));
+  }
+}
+
+// out = S_q u (+ S_p columns of the unit sources when add_src >= 0).
+template <typename T>
+__global__ void k_block_apply(int64_t batch, int nh, const M2* __restrict__ S, int q, const cplx<T>* __restrict__ u,
+                              cplx<T>* out, int add_src) {
+  const int n = 2 * nh;
+  const int c0 = (nh - 1) / 2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n * 2; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / (2 * n);
+    const int r = (int)((e / 2) % n), col = (int)(e % 2);
+    const int g = r % nh, rb = r / nh;
+    const M2& s = S[(b * nh + g) * 4 + q];
+    const cplx<T>* ub = u + b * n * 2;
+    cd v = blk(s, rb, 0) * to_d(ub[g * 2 + col]) + blk(s, rb, 1) * to_d(ub[(nh + g) * 2 + col]);
+    if (add_src >= 0 && g == c0) v += blk(S[(b * nh + g) * 4 + add_src], rb, col);
+    out[e] = to_t<T>(v);
+  }
+}
+
+// u <- 4 X u (patterned layer, forward pass).
+template <typename T>
+__global__ void k_vec_x4(int64_t batch, int n, const cplx<T>* __restrict__ lam, double depth, const double* k0, cplx<T>* u) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n * 2; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / (2 * n);
+    const int r = (int)((e / 2) % n);
+    const cd x = cexp(-(to_d(lam[b * n + r]) * (depth * k0[b])));
+    u[e] = to_t<T>((4.0 * x) * to_d(u[e]));
+  }
+}
+
+// R, T from the two source columns of r and t ([batch][n][2]) for npol polarisations
+// (te, tm: [batch][npol]; R, T: [batch][npol]), one CTA per problem.
+template <typename T>
+__global__ void k_flux_cols(int nh, int npol, const cplx<T>* __restrict__ rv, const cplx<T>* __restrict__ tv,
+                            const double* gx, const double* gy, const double* kp, const double* k0v, const cd* te_v,
+                            const cd* tm_v, cd epsi, cd epse, double* R, double* Tt) {
+  __shared__ TeamShared sh;
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  const int n = 2 * nh;
+  const double k0 = k0v[b];
+  const cd kpx = mk(kp[4 * b + 0], kp[4 * b + 1]), kpy = mk(kp[4 * b + 2], kp[4 * b + 3]);
+  const cd kzi_abs = conj(csqrt(mk(k0 * k0) * epsi - kpx * kpx - kpy * kpy));
+  const cd kzi_n = kzi_abs * (1.0 / k0);
+  for (int pol = 0; pol < npol; ++pol) {
+    cd px, py;
+    phys::source_pol(kpx, kpy, kzi_abs, te_v[b * npol + pol], tm_v[b * npol + pol], px, py);
+    double rs = 0.0, ts = 0.0;
+    for (int g = t.tid(); g < nh; g += t.size()) {
+      const cd kxa = mk(kp[4 * b + 0] + gx[g], kp[4 * b + 1]);
+      const cd kya = mk(kp[4 * b + 2] + gy[g], kp[4 * b + 3]);
+      const cd kx = kxa * (1.0 / k0), ky = kya * (1.0 / k0);
+      for (int which = 0; which < 2; ++which) {
+        const cplx<T>* v = (which == 0 ? rv : tv) + b * n * 2;
+        const cd eps = which == 0 ? epsi : epse;
+        const cd kz = conj(csqrt(mk(k0 * k0) * conj(eps) - kxa * kxa - kya * kya)) * (1.0 / k0);
+        const cd sx = to_d(v[g * 2 + 0]) * px + to_d(v[g * 2 + 1]) * py;
+        const cd sy = to_d(v[(nh + g) * 2 + 0]) * px + to_d(v[(nh + g) * 2 + 1]) * py;
+        const cd sz = -cdiv(kx * sx + ky * sy, kz);
+        const double tg = kz.re / kzi_n.re * (norm2(sx) + norm2(sy) + norm2(sz));
+        if (which == 0) rs += tg;
+        else ts += tg;
+      }
+    }
+    rs = team_sum(t, rs, &sh);
+    ts = team_sum(t, ts, &sh);
+    if (threadIdx.x == 0) {
+      R[b * npol + pol] = rs;
+      Tt[b * npol + pol] = ts;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace khp

@@ -1,0 +1,826 @@
+// Mixed-precision batched R/T (khp_solve_batched_mixed): FP32 for every O(n^3) step, FP64 only
+// where accuracy is decided.
+//
+// GB300 runs FP32 at ~58x its FP64 rate, but an all-FP32 solve misses |dR|, |dT| <= 1e-6 (errors
+// of a few 1e-6 on the 11x11 sweep).  This pipeline:
+//   1. modes: FP32 eigensolve of M = P Q, then one FP64 refinement step of the eigenpairs:
+//      E = W^-1 (M W - W mu) with the residual formed in FP64 and the solve in FP32,
+//      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i) (pairs closer than a relative
+//      1e-5 are left coupled: their coupling error is second order);  V = Q W / lam in FP64;
+//   2. the reflection-matrix recursion of khp_solve_batched on the FP32-rounded refined modes,
+//      keeping every factor it makes (LU factors, rho, Gamma at every gap, Gamma M^-1);
+//   3. iterative refinement of the interface-continuity system of the whole stack (the
+//      equations the reference's S-matrix chain encodes, crystal.py:180-206 / layer.py:35-60),
+//      for the two source columns: residual in FP64 with the refined FP64 modes and the FP64
+//      closed-form homogeneous blocks (O(n^2) per layer), correction by an affine sweep through
+//      the kept FP32 factors (O(n^2) per layer).
+// The converged amplitudes solve the FP64 system; R and T follow as in crystal.py:363-396.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "khepri_gb300.h"
+#include "khp_dense.cuh"
+#include "khp_gamma_kernels.cuh"
+#include "khp_launch.h"
+#include "khp_physics.cuh"
+
+namespace khp {
+namespace {
+
+using cf = cplx<float>;
+
+constexpr int kMaxLayers = 16;
+
+// ------------------------------------------------------------------------------------------
+// Eigen-refinement kernels
+// ------------------------------------------------------------------------------------------
+// R32 = (M64 W64 - W64 diag(mu)) in FP32, where MW already holds M64 W64.
+__global__ void k_eig_residual(int64_t batch, int n, const cd* __restrict__ MW, const cd* __restrict__ W64,
+                               const cf* __restrict__ mu, cf* R32) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int j = (int)(e % nn) % n;
+    const cf m = mu[b * n + j];
+    const cd r = MW[e] - W64[e] * mk((double)m.re, (double)m.im);
+    R32[e] = mk((float)r.re, (float)r.im);
+  }
+}
+
+// mu64 = mu32 + diag(E); F_ij = E_ij / (mu_j - mu_i) for well-separated pairs (in place on E).
+__global__ void k_eig_update(int64_t batch, int n, const cf* __restrict__ mu32, cf* E, cd* mu64) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int rc = (int)(e % nn);
+    const int i = rc / n, j = rc % n;
+    const cd mi = mk((double)mu32[b * n + i].re, (double)mu32[b * n + i].im);
+    const cd mj = mk((double)mu32[b * n + j].re, (double)mu32[b * n + j].im);
+    const cf ev = E[e];
+    const cd ed = mk((double)ev.re, (double)ev.im);
+    if (i == j) {
+      mu64[b * n + i] = mi + ed;
+      E[e] = mk(0.f, 0.f);
+      continue;
+    }
+    const cd d = mj - mi;
+    const double scale = cabs(mi) + cabs(mj);
+    if (cabs(d) > 1e-5 * scale) {
+      const cd f = cdiv(ed, d);
+      E[e] = mk((float)f.re, (float)f.im);
+    } else {
+      E[e] = mk(0.f, 0.f);
+    }
+  }
+}
+
+// W64 += D32 ; W32 = round(W64)
+__global__ void k_add_correction(int64_t count, cd* W64, const cf* __restrict__ D, cf* W32) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const cd w = W64[e] + mk((double)D[e].re, (double)D[e].im);
+    W64[e] = w;
+    W32[e] = mk((float)w.re, (float)w.im);
+  }
+}
+
+__global__ void k_to_double(int64_t count, const cf* __restrict__ in, cd* out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = mk((double)in[e].re, (double)in[e].im);
+}
+
+// lam64 = sqrt(mu64) (principal), lam32 = round(lam64)
+__global__ void k_sqrt_mu(int64_t count, const cd* __restrict__ mu64, cd* lam64, cf* lam32) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const cd l = csqrt(mu64[e]);
+    lam64[e] = l;
+    lam32[e] = mk((float)l.re, (float)l.im);
+  }
+}
+
+__global__ void k_round(int64_t count, const cd* __restrict__ in, cf* out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = mk((float)in[e].re, (float)in[e].im);
+}
+
+// ------------------------------------------------------------------------------------------
+// Element table for the per-problem vector kernels
+// ------------------------------------------------------------------------------------------
+struct Elem {
+  int kind;  // 0 homogeneous layer, 1 patterned layer
+  int slot;  // map slot (patterned)
+  double depth;
+  const M2* blocks;  // homogeneous: [batch][nh][4] (FP64)
+  const cf* lu1;     // homogeneous: LU of M; patterned: LU of F - G
+  const int* piv1;
+  const cf* lu2;  // patterned: LU of P1 - P2
+  const int* piv2;
+  const cf* zr;  // homogeneous: Gamma M^-1;  patterned: rho
+};
+
+struct MapPtrs {
+  const cd* W64;
+  const cd* V64;
+  const cd* lam64;
+  const cf* W32;
+  const cf* V32;
+  const cf* lam32;
+  const cf* Wi;
+  const cf* Vi;
+};
+
+struct Table {
+  int L;
+  int nh;
+  int64_t batch;
+  const M2* inc;
+  const M2* trn;
+  const cf* lu0;   // LU of I - S22_inc Gamma_0
+  const int* piv0;
+  const cf* gam;   // Gamma at gaps 0..L: [L+1][batch][n][n]
+  Elem e[kMaxLayers];
+  MapPtrs m[kMaxLayers];
+};
+
+// Unknowns of one problem (FP64), two columns each, [..][n][2]:
+//   gap g = 0..L: c+ at x + (2g) * 2n, c- at x + (2g+1) * 2n;
+//   patterned layer l: a+ at xa + (2l) * 2n, a- at xa + (2l+1) * 2n;   r, t.
+// Residual slots per element (FP64): 4 x [n][2]; element 0 = incidence, 1..L layers, L+1 emergence.
+
+template <typename V>
+__device__ __forceinline__ cd ld2(const V* v, int i, int c) {
+  return mk((double)v[2 * i + c].re, (double)v[2 * i + c].im);
+}
+
+// y = A x for two columns; A row-major n x n, x, y [n][2]; accumulation in A's precision.
+template <typename TA, typename TX, typename TY>
+__device__ void team_mv2(const TeamCta& t, const cplx<TA>* A, int n, const cplx<TX>* x, cplx<TY>* y) {
+  for (int i = t.tid(); i < n; i += t.size()) {
+    cplx<TA> a0 = mk(TA(0)), a1 = mk(TA(0));
+    const cplx<TA>* row = A + (int64_t)i * n;
+    for (int j = 0; j < n; ++j) {
+      const cplx<TA> aij = row[j];
+      fma_acc(a0, aij, mk((TA)x[2 * j].re, (TA)x[2 * j].im));
+      fma_acc(a1, aij, mk((TA)x[2 * j + 1].re, (TA)x[2 * j + 1].im));
+    }
+    y[2 * i] = mk((TY)a0.re, (TY)a0.im);
+    y[2 * i + 1] = mk((TY)a1.re, (TY)a1.im);
+  }
+}
+
+// y = S_q x for a per-harmonic block matrix (q = 0..3: S11, S12, S21, S22).
+template <typename TX>
+__device__ __forceinline__ cd blk_mv(const M2* S, int q, int nh, int i, int c, const TX* x) {
+  const int g = i % nh, rb = i / nh;
+  const M2& s = S[g * 4 + q];
+  return blk(s, rb, 0) * ld2(x, g, c) + blk(s, rb, 1) * ld2(x, nh + g, c);
+}
+
+__device__ __forceinline__ cd src_col(const M2* S, int q, int nh, int i, int c) {
+  const int g = i % nh;
+  return g == (nh - 1) / 2 ? blk(S[g * 4 + q], i / nh, c) : mk(0.0);
+}
+
+__device__ __forceinline__ cd xprop(const cd* lam64, int i, double dk) { return cexp(-(lam64[i] * dk)); }
+
+// FP64 residual of the stack equations at the current unknowns x (see the Elem comments).
+__global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* gx, const double* gy,
+                                                        const double* kp, const double* k0v, const cd* __restrict__ X,
+                                                        const cd* __restrict__ XA, const cd* __restrict__ RT,
+                                                        cd* RES, cd* scratch) {
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  const int nh = tb.nh, n = 2 * nh, L = tb.L;
+  const int64_t nn = (int64_t)n * n;
+  const int64_t xs = (int64_t)(2 * (L + 1)) * 2 * n, xas = (int64_t)2 * L * 2 * n;
+  const cd* x = X + b * xs;
+  const cd* xa = XA + b * xas;
+  const cd* r = RT + b * 2 * n;
+  const cd* tt = RT + (tb.batch + b) * 2 * n;
+  cd* res = RES + b * (int64_t)(L + 2) * 4 * 2 * n;
+  cd* w1 = scratch + b * 4 * 2 * n;
+  cd* w2 = w1 + 2 * n;
+  cd* w3 = w2 + 2 * n;
+  cd* w4 = w3 + 2 * n;
+  const double k0 = k0v[b];
+  auto cp = [&](int g) { return x + (2 * g) * 2 * n; };
+  auto cm = [&](int g) { return x + (2 * g + 1) * 2 * n; };
+  // incidence: rA = S11 c + S12 c-_0 - r ; rB = S21 c + S22 c-_0 - c+_0
+  {
+    const M2* S = tb.inc + b * nh * 4;
+    cd* rA = res;
+    cd* rB = res + 2 * n;
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      rA[e] = src_col(S, 0, nh, i, c) + blk_mv(S, 1, nh, i, c, cm(0)) - r[e];
+      rB[e] = src_col(S, 2, nh, i, c) + blk_mv(S, 3, nh, i, c, cm(0)) - cp(0)[e];
+    }
+  }
+  int pl = 0;
+  for (int l = 0; l < L; ++l) {
+    const Elem& E = tb.e[l];
+    cd* rs = res + (int64_t)(l + 1) * 4 * 2 * n;
+    const cd *cpl = cp(l), *cml = cm(l), *cpr = cp(l + 1), *cmr = cm(l + 1);
+    if (E.kind == 0) {
+      const M2* S = E.blocks + b * nh * 4;
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const int i = e / 2, c = e % 2;
+        rs[e] = blk_mv(S, 0, nh, i, c, cpl) + blk_mv(S, 1, nh, i, c, cmr) - cml[e];
+        rs[2 * n + e] = blk_mv(S, 2, nh, i, c, cpl) + blk_mv(S, 3, nh, i, c, cmr) - cpr[e];
+      }
+      t.sync();
+      continue;
+    }
+    const MapPtrs& M = tb.m[E.slot];
+    const cd* W = M.W64 + b * nn;
+    const cd* V = M.V64 + b * nn;
+    const cd* lam = M.lam64 + b * n;
+    const double dk = E.depth * k0;
+    const cd* ap = xa + (2 * pl) * 2 * n;
+    const cd* am = xa + (2 * pl + 1) * 2 * n;
+    // w1 = a+ + X a-, w2 = X a- - a+, w3 = X a+ + a-, w4 = a- - X a+
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const cd xi = xprop(lam, e / 2, dk);
+      w1[e] = ap[e] + xi * am[e];
+      w2[e] = xi * am[e] - ap[e];
+      w3[e] = xi * ap[e] + am[e];
+      w4[e] = am[e] - xi * ap[e];
+    }
+    t.sync();
+    cd* r1 = rs;
+    cd* r2 = rs + 2 * n;
+    cd* r3 = rs + 4 * n;
+    cd* r4 = rs + 6 * n;
+    team_mv2(t, W, n, w1, r1);
+    team_mv2(t, V, n, w2, r2);
+    team_mv2(t, W, n, w3, r3);
+    team_mv2(t, V, n, w4, r4);
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      const int g = i % nh, rb = i / nh;
+      cd kx, ky;
+      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
+      const M2 v0 = phys::v0_block(kx, ky);
+      const cd dl0 = cml[2 * g + c] - cpl[2 * g + c], dl1 = cml[2 * (nh + g) + c] - cpl[2 * (nh + g) + c];
+      const cd dr0 = cmr[2 * g + c] - cpr[2 * g + c], dr1 = cmr[2 * (nh + g) + c] - cpr[2 * (nh + g) + c];
+      r1[e] = r1[e] - cpl[e] - cml[e];
+      r2[e] = r2[e] - (blk(v0, rb, 0) * dl0 + blk(v0, rb, 1) * dl1);
+      r3[e] = r3[e] - cpr[e] - cmr[e];
+      r4[e] = r4[e] - (blk(v0, rb, 0) * dr0 + blk(v0, rb, 1) * dr1);
+    }
+    t.sync();
+    ++pl;
+  }
+  // emergence: rA = S11 c+_L - c-_L ; rB = S21 c+_L - t
+  {
+    const M2* S = tb.trn + b * nh * 4;
+    cd* rA = res + (int64_t)(L + 1) * 4 * 2 * n;
+    cd* rB = rA + 2 * n;
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      rA[e] = blk_mv(S, 0, nh, i, c, cp(L)) - cm(L)[e];
+      rB[e] = blk_mv(S, 2, nh, i, c, cp(L)) - tt[e];
+    }
+  }
+}
+
+// FP32 affine sweep: solves the stack equations for the residual RES (correction system) with
+// the kept factors, and adds the correction to the FP64 unknowns.
+// Per problem workspace (FP32, [..][n][2]): s at every gap (L+1), per layer 5 vectors, 6 temps.
+__global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx, const double* gy, const double* kp,
+                                                     const double* k0v, const cd* __restrict__ RES, cd* X, cd* XA,
+                                                     cd* RT, cf* WS) {
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  const int nh = tb.nh, n = 2 * nh, L = tb.L;
+  const int64_t nn = (int64_t)n * n;
+  const int64_t xs = (int64_t)(2 * (L + 1)) * 2 * n, xas = (int64_t)2 * L * 2 * n;
+  cd* x = X + b * xs;
+  cd* xa = XA + b * xas;
+  cd* r = RT + b * 2 * n;
+  cd* tt = RT + (tb.batch + b) * 2 * n;
+  const cd* res = RES + b * (int64_t)(L + 2) * 4 * 2 * n;
+  const int64_t wsz = (int64_t)(L + 1 + 5 * L + 6) * 2 * n;
+  cf* ws = WS + b * wsz;
+  auto S_at = [&](int g) { return ws + (int64_t)g * 2 * n; };           // s at gap g
+  auto LV = [&](int l, int k) { return ws + (int64_t)(L + 1 + 5 * l + k) * 2 * n; };  // per-layer vectors
+  cf* T0 = ws + (int64_t)(L + 1 + 5 * L) * 2 * n;
+  cf* T1 = T0 + 2 * n;
+  cf* T2 = T1 + 2 * n;
+  cf* T3 = T2 + 2 * n;
+  cf* dcp = T3 + 2 * n;  // running correction of c+ (FP32)
+  cf* dcm = dcp + 2 * n;
+  const double k0 = k0v[b];
+  auto rsl = [&](int elem, int k) { return res + (int64_t)elem * 4 * 2 * n + (int64_t)k * 2 * n; };
+  auto gam = [&](int g) { return tb.gam + ((int64_t)g * tb.batch + b) * nn; };
+  // ---- backward ----
+  {
+    const cd* rA = rsl(L + 1, 0);
+    cf* s = S_at(L);
+    for (int e = t.tid(); e < 2 * n; e += t.size()) s[e] = mk((float)rA[e].re, (float)rA[e].im);
+  }
+  t.sync();
+  for (int l = L - 1; l >= 0; --l) {
+    const Elem& E = tb.e[l];
+    const cf* sj = S_at(l + 1);
+    cf* sl = S_at(l);
+    const cd* f1 = rsl(l + 1, 0);
+    const cd* f2 = rsl(l + 1, 1);
+    if (E.kind == 0) {
+      const M2* S = E.blocks + b * nh * 4;
+      cf* w = LV(l, 0);
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const int i = e / 2, c = e % 2;
+        const cd v = blk_mv(S, 3, nh, i, c, sj) + f2[e];
+        w[e] = mk((float)v.re, (float)v.im);
+      }
+      t.sync();
+      team_mv2(t, E.zr + b * nn, n, w, T0);  // Z w
+      t.sync();
+      for (int e = t.tid(); e < 2 * n; e += t.size()) T1[e] = T0[e] + sj[e];
+      t.sync();
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const int i = e / 2, c = e % 2;
+        const cd v = blk_mv(S, 1, nh, i, c, T1) + f1[e];
+        sl[e] = mk((float)v.re, (float)v.im);
+      }
+      t.sync();
+      continue;
+    }
+    const MapPtrs& M = tb.m[E.slot];
+    const cd* f3 = rsl(l + 1, 2);
+    const cd* f4 = rsl(l + 1, 3);
+    const double dk = E.depth * k0;
+    // T0 = f3 - s ; T1 = f4 - V0 s
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      const int g = i % nh, rb = i / nh;
+      cd kx, ky;
+      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
+      const M2 v0 = phys::v0_block(kx, ky);
+      const cd v0s = blk(v0, rb, 0) * ld2(sj, g, c) + blk(v0, rb, 1) * ld2(sj, nh + g, c);
+      const cd a = f3[e] - ld2(sj, i, c);
+      const cd bb = f4[e] - v0s;
+      T0[e] = mk((float)a.re, (float)a.im);
+      T1[e] = mk((float)bb.re, (float)bb.im);
+    }
+    t.sync();
+    cf* g3 = T2;
+    cf* g4 = T3;
+    team_mv2(t, M.Wi + b * nn, n, T0, g3);
+    team_mv2(t, M.Vi + b * nn, n, T1, g4);
+    t.sync();
+    cf* q = LV(l, 0);  // g3 - g4
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      q[e] = g3[e] - g4[e];
+      T1[e] = g3[e] + g4[e];
+    }
+    t.sync();
+    cf* h = LV(l, 1);
+    team_mv2(t, E.zr + b * nn, n, q, T0);  // rho q
+    t.sync();
+    const cf* lam = M.lam32 + b * n;
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      h[e] = mk(0.5f, 0.f) * (T0[e] - T1[e]);
+      const cd xi = cexp(-(mk((double)lam[e / 2].re, (double)lam[e / 2].im) * dk));
+      const cd xh = xi * ld2(h, e / 2, e % 2);
+      T2[e] = mk((float)xh.re, (float)xh.im);  // X h
+    }
+    t.sync();
+    team_mv2(t, M.W32 + b * nn, n, T2, T0);  // W X h
+    team_mv2(t, M.V32 + b * nn, n, T2, T1);  // V X h
+    t.sync();
+    cf* k1 = LV(l, 2);
+    cf* k2 = LV(l, 3);
+    const cd* f1p = rsl(l + 1, 0);
+    const cd* f2p = rsl(l + 1, 1);
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      const int g = i % nh, rb = i / nh;
+      cd kx, ky;
+      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
+      const M2 vi = phys::inv2(phys::v0_block(kx, ky));
+      const cd a1 = ld2(T0, i, c) + f1p[e];
+      const cd u0 = ld2(T1, g, c) + f2p[2 * g + c], u1 = ld2(T1, nh + g, c) + f2p[2 * (nh + g) + c];
+      const cd a2 = blk(vi, rb, 0) * u0 + blk(vi, rb, 1) * u1;
+      k1[e] = mk((float)a1.re, (float)a1.im);
+      k2[e] = mk((float)a2.re, (float)a2.im);
+    }
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) T3[e] = k2[e] - k1[e];
+    t.sync();
+    team_mv2(t, gam(l), n, T3, T0);  // Gamma_{left} (k2 - k1)
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) sl[e] = mk(0.5f, 0.f) * (T0[e] + k1[e] + k2[e]);
+    t.sync();
+  }
+  // ---- incidence: c+_0 = M0^-1 (S22 s_0 + rB), c-_0 = Gamma_0 c+_0 + s_0, r += S12 c-_0 + rA ----
+  {
+    const M2* S = tb.inc + b * nh * 4;
+    const cd* rA = rsl(0, 0);
+    const cd* rB = rsl(0, 1);
+    const cf* s0 = S_at(0);
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      const cd v = blk_mv(S, 3, nh, i, c, s0) + rB[e];
+      dcp[e] = mk((float)v.re, (float)v.im);
+    }
+    t.sync();
+    team_getrs(t, tb.lu0 + b * nn, n, n, tb.piv0 + b * n, dcp, 2, 2);
+    team_mv2(t, gam(0), n, dcp, T0);
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) dcm[e] = T0[e] + s0[e];
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      r[e] += blk_mv(S, 1, nh, i, c, dcm) + rA[e];
+      x[e] += ld2(dcp, i, c);
+      x[2 * n + e] += ld2(dcm, i, c);
+    }
+    t.sync();
+  }
+  // ---- forward ----
+  int pl = 0;
+  for (int l = 0; l < L; ++l) {
+    const Elem& E = tb.e[l];
+    const cf* sr = S_at(l + 1);
+    if (E.kind == 0) {
+      const M2* S = E.blocks + b * nh * 4;
+      const cf* w = LV(l, 0);
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const int i = e / 2, c = e % 2;
+        const cd v = blk_mv(S, 2, nh, i, c, dcp) + ld2(w, i, c);
+        T0[e] = mk((float)v.re, (float)v.im);
+      }
+      t.sync();
+      team_getrs(t, E.lu1 + b * nn, n, n, E.piv1 + b * n, T0, 2, 2);
+      for (int e = t.tid(); e < 2 * n; e += t.size()) dcp[e] = T0[e];
+      t.sync();
+    } else {
+      const MapPtrs& M = tb.m[E.slot];
+      const cf* q = LV(l, 0);
+      const cf* h = LV(l, 1);
+      const cf* k1 = LV(l, 2);
+      const cf* k2 = LV(l, 3);
+      const double dk = E.depth * k0;
+      const cf* lam = M.lam32 + b * n;
+      cd* ap = xa + (2 * pl) * 2 * n;
+      cd* am = xa + (2 * pl + 1) * 2 * n;
+      for (int e = t.tid(); e < 2 * n; e += t.size()) T0[e] = mk(2.f, 0.f) * dcp[e] - k1[e] + k2[e];
+      t.sync();
+      team_getrs(t, E.lu2 + b * nn, n, n, E.piv2 + b * n, T0, 2, 2);  // a+
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const cd xi = cexp(-(mk((double)lam[e / 2].re, (double)lam[e / 2].im) * dk));
+        const cd xa_ = xi * ld2(T0, e / 2, e % 2);
+        T1[e] = mk((float)xa_.re, (float)xa_.im);  // X a+
+        const cd v = 2.0 * xa_ + ld2(q, e / 2, e % 2);
+        T2[e] = mk((float)v.re, (float)v.im);
+      }
+      t.sync();
+      team_getrs(t, E.lu1 + b * nn, n, n, E.piv1 + b * n, T2, 2, 2);  // c+ right
+      team_mv2(t, E.zr + b * nn, n, T1, T3);                           // rho X a+
+      t.sync();
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        ap[e] += ld2(T0, e / 2, e % 2);
+        am[e] += ld2(T3, e / 2, e % 2) + ld2(h, e / 2, e % 2);
+        dcp[e] = T2[e];
+      }
+      t.sync();
+      ++pl;
+    }
+    // c-_{l+1} = Gamma c+ + s
+    team_mv2(t, gam(l + 1), n, dcp, T0);
+    t.sync();
+    cd* cpg = x + (2 * (l + 1)) * 2 * n;
+    cd* cmg = x + (2 * (l + 1) + 1) * 2 * n;
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      dcm[e] = T0[e] + sr[e];
+      cpg[e] += ld2(dcp, e / 2, e % 2);
+      cmg[e] += ld2(dcm, e / 2, e % 2);
+    }
+    t.sync();
+  }
+  // ---- emergence: t += S21 c+_L + rB ----
+  {
+    const M2* S = tb.trn + b * nh * 4;
+    const cd* rB = rsl(L + 1, 1);
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      tt[e] += blk_mv(S, 2, nh, i, c, dcp) + rB[e];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+struct Arena {
+  char* base;
+  size_t cap;
+  size_t off = 0;
+  bool ok = true;
+  template <typename U>
+  U* take(size_t count) {
+    const size_t bytes = (count * sizeof(U) + 255) & ~size_t(255);
+    U* p = base ? reinterpret_cast<U*>(base + off) : nullptr;
+    off += bytes;
+    if (base && off > cap) ok = false;
+    return p;
+  }
+};
+
+struct MixedPlan {
+  // per map slot
+  std::vector<cf*> W32, V32, lam32, Wi, Vi, Q0, Vt;
+  std::vector<cd*> W64, V64, lam64;
+  // modes scratch
+  cf *M32, *Z32, *E32, *lu32;
+  cd *M64, *MW64, *CW64, *Ct64, *mu64;
+  int* piv;
+  // per layer
+  std::vector<cf*> lu1, lu2, zr;
+  std::vector<int*> piv1, piv2;
+  std::vector<M2*> blocks;
+  M2 *inc, *trn;
+  cf *gam, *F, *Gb, *P, *lu0;
+  int* piv0;
+  // vectors
+  cd *X, *XA, *RT, *RES, *scr;
+  cf* SW;
+};
+
+MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, int nmaps_used) {
+  const size_t n = 2 * (size_t)nh, nn = n * n;
+  MixedPlan p;
+  for (int m = 0; m < nmaps_used; ++m) {
+    p.W32.push_back(a.take<cf>(batch * nn));
+    p.V32.push_back(a.take<cf>(batch * nn));
+    p.lam32.push_back(a.take<cf>(batch * n));
+    p.Wi.push_back(a.take<cf>(batch * nn));
+    p.Vi.push_back(a.take<cf>(batch * nn));
+    p.Q0.push_back(a.take<cf>(batch * nn));
+    p.Vt.push_back(a.take<cf>(batch * nn));
+    p.W64.push_back(a.take<cd>(batch * nn));
+    p.V64.push_back(a.take<cd>(batch * nn));
+    p.lam64.push_back(a.take<cd>(batch * n));
+  }
+  p.M32 = a.take<cf>(batch * nn);
+  p.Z32 = a.take<cf>(batch * nn);
+  p.E32 = a.take<cf>(batch * nn);
+  p.lu32 = a.take<cf>(batch * nn);
+  p.M64 = a.take<cd>(batch * nn);
+  p.MW64 = a.take<cd>(batch * nn);
+  p.CW64 = a.take<cd>(batch * nn);
+  p.Ct64 = nullptr;
+  p.mu64 = a.take<cd>(batch * n);
+  p.piv = a.take<int>(batch * n);
+  for (int l = 0; l < L; ++l) {
+    p.lu1.push_back(a.take<cf>(batch * nn));
+    p.piv1.push_back(a.take<int>(batch * n));
+    p.zr.push_back(a.take<cf>(batch * nn));
+    if (kinds[l] == 1) {
+      p.lu2.push_back(a.take<cf>(batch * nn));
+      p.piv2.push_back(a.take<int>(batch * n));
+      p.blocks.push_back(nullptr);
+    } else {
+      p.lu2.push_back(nullptr);
+      p.piv2.push_back(nullptr);
+      p.blocks.push_back(a.take<M2>(batch * nh * 4));
+    }
+  }
+  p.inc = a.take<M2>(batch * nh * 4);
+  p.trn = a.take<M2>(batch * nh * 4);
+  p.gam = a.take<cf>((size_t)(L + 1) * batch * nn);
+  p.F = a.take<cf>(batch * nn);
+  p.Gb = a.take<cf>(batch * nn);
+  p.P = a.take<cf>(batch * nn);
+  p.lu0 = a.take<cf>(batch * nn);
+  p.piv0 = a.take<int>(batch * n);
+  p.X = a.take<cd>(batch * (size_t)(2 * (L + 1)) * 2 * n);
+  p.XA = a.take<cd>(batch * (size_t)(2 * std::max(L, 1)) * 2 * n);
+  p.RT = a.take<cd>(batch * 4 * n);
+  p.RES = a.take<cd>(batch * (size_t)(L + 2) * 4 * 2 * n);
+  p.scr = a.take<cd>(batch * 4 * 2 * n);
+  p.SW = a.take<cf>(batch * (size_t)(L + 1 + 5 * L + 6) * 2 * n);
+  return p;
+}
+
+#define MX_TRY(x)        \
+  do {                   \
+    const int _s = (x);  \
+    if (_s) return _s;   \
+  } while (0)
+#define MX_EW(kernel, total, ...)                                        \
+  do {                                                                   \
+    kernel<<<grid_for(total), 256, 0, s>>>(__VA_ARGS__);                 \
+    count_launches(1);                                                   \
+    MX_TRY(cuda_status());                                               \
+  } while (0)
+
+int launch_getrs_right_f(int64_t batch, int n, const cf* A, int64_t lda, int64_t bsA, const int* piv, cf* B,
+                         int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
+  k_getrs_right<float><<<(unsigned)batch, 256, 0, s>>>(n, A, lda, bsA, piv, B, ldb, bsB, m);
+  count_launches(1);
+  return cuda_status();
+}
+
+int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const int* maps, const double* eps,
+                const double* depths, const double* conv, const double* hx, const double* hy, const double* gx,
+                const double* gy, cd epsi, cd epse, const double* kp, const double* k0, int npol, const double* te,
+                const double* tm, int refine, double* R, double* Tt, int* status, void* workspace, size_t ws_bytes,
+                cudaStream_t s) {
+  const int nh = px * py, n = 2 * nh;
+  const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh, hn = (int64_t)nh * n;
+  std::vector<int> used, slot(L, -1);
+  for (int l = 0; l < L; ++l) {
+    if (kinds[l] != 1) continue;
+    int sidx = -1;
+    for (size_t u = 0; u < used.size(); ++u)
+      if (used[u] == maps[l]) sidx = (int)u;
+    if (sidx < 0) {
+      sidx = (int)used.size();
+      used.push_back(maps[l]);
+    }
+    slot[l] = sidx;
+  }
+  Arena a{static_cast<char*>(workspace), ws_bytes};
+  MixedPlan p = plan_mixed(a, batch, nh, L, kinds, (int)used.size());
+  if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
+  const cf one = mk(1.f), zero = mk(0.f), mone = mk(-1.f);
+  const cd done = mk(1.0), dzero = mk(0.0);
+
+  // ---- 1. modes: FP32 eigensolve + FP64 refinement ----
+  for (size_t m = 0; m < used.size(); ++m) {
+    const cd* C = reinterpret_cast<const cd*>(conv) + used[m] * hh;
+    const cd* HX = reinterpret_cast<const cd*>(hx) + used[m] * hh;
+    const cd* HY = reinterpret_cast<const cd*>(hy) + used[m] * hh;
+    MX_EW(k_assemble_pq_t<float>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M32);
+    MX_TRY(launch_geev<float>(batch, n, p.M32, n, nn, p.Z32, p.W32[m], n, nn, p.lam32[m], n, status, s));
+    // residual R = M W - W mu in FP64
+    MX_EW(k_assemble_pq_t<double>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M64);
+    MX_EW(k_to_double, batch * nn, batch * nn, p.W32[m], p.W64[m]);
+    MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
+    MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], p.lam32[m], p.E32);
+    // E = W^-1 R (FP32), F, W += W F
+    MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_getrf<float>(batch, n, p.lu32, n, nn, p.piv, status, s));
+    MX_TRY(launch_getrs<float>(batch, n, p.lu32, n, nn, p.piv, p.E32, n, nn, n, s));
+    MX_EW(k_eig_update, batch * nn, batch, n, p.lam32[m], p.E32, p.mu64);
+    MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.E32, n, nn, zero, p.M32, n, nn, s));
+    MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.M32, p.W32[m]);
+    MX_EW(k_sqrt_mu, batch * n, batch * n, p.mu64, p.lam64[m], p.lam32[m]);
+    // V = Q W / lam in FP64
+    cd* CWt = p.CW64;
+    cd* CWb = p.CW64 + batch * hn;
+    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, C, nh, 0, p.W64[m], n, nn, dzero, CWt, n, hn, s));
+    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, C, nh, 0, p.W64[m] + hn, n, nn, dzero, CWb, n, hn, s));
+    MX_EW(k_modes_v_t<double>, batch * nn, batch, nh, gx, gy, kp, k0, p.W64[m], CWt, CWb, p.lam64[m], p.V64[m],
+          status);
+    MX_EW(k_round, batch * nn, batch * nn, p.V64[m], p.V32[m]);
+    // FP32 inverses and V0 products
+    MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_inverse<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
+    MX_TRY(launch_copy<float>(batch, n, n, p.V32[m], n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_inverse<float>(batch, n, p.lu32, n, nn, p.Vi[m], n, nn, p.piv, status, s));
+    MX_EW(k_v0_right<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.Vi[m], p.Q0[m]);
+    MX_EW(k_v0inv_left<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.V32[m], p.Vt[m]);
+  }
+  // ---- homogeneous blocks (FP64) ----
+  MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, 0.0, gx, gy, kp, k0, p.inc, status);
+  MX_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, 0.0, gx, gy, kp, k0, p.trn, status);
+  for (int l = 0; l < L; ++l)
+    if (kinds[l] != 1)
+      MX_EW(k_homog_blocks, batch * nh, batch, nh, 0, mk(eps[2 * l], eps[2 * l + 1]), depths[l], gx, gy, kp, k0,
+            p.blocks[l], status);
+  // ---- 2. FP32 backward recursion, keeping every factor ----
+  auto gam = [&](int g) { return p.gam + (int64_t)g * batch * nn; };
+  MX_EW(k_gamma_from_blocks<float>, batch * nn, batch, nh, p.trn, 0, gam(L));
+  for (int l = L - 1; l >= 0; --l) {
+    cf* G = gam(l + 1);
+    if (kinds[l] != 1) {
+      MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.blocks[l], G, p.lu1[l]);
+      MX_TRY(launch_getrf<float>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
+      MX_TRY(launch_copy<float>(batch, n, n, G, n, nn, p.zr[l], n, nn, s));
+      MX_TRY(launch_getrs_right_f(batch, n, p.lu1[l], n, nn, p.piv1[l], p.zr[l], n, nn, n, s));
+      MX_EW(k_sandwich<float>, batch * nn, batch, nh, p.blocks[l], p.zr[l], gam(l));
+    } else {
+      const int m = slot[l];
+      MX_TRY(launch_copy<float>(batch, n, n, p.Wi[m], n, nn, p.F, n, nn, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, G, n, nn, one, p.F, n, nn, s));
+      MX_TRY(launch_copy<float>(batch, n, n, p.Q0[m], n, nn, p.Gb, n, nn, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Q0[m], n, nn, G, n, nn, mone, p.Gb, n, nn, s));
+      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.F, p.Gb, p.lu1[l]);
+      MX_TRY(launch_getrf<float>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
+      MX_TRY(launch_getrs_right_f(batch, n, p.lu1[l], n, nn, p.piv1[l], p.F, n, nn, n, s));  // rho
+      MX_TRY(launch_copy<float>(batch, n, n, p.F, n, nn, p.zr[l], n, nn, s));
+      MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.lam32[m], depths[l], k0, p.F);
+      MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.Gb, n, nn, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));
+      MX_TRY(launch_copy<float>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Vt[m], n, nn, p.F, n, nn, mone, p.P, n, nn, s));
+      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.Gb, p.P, p.lu2[l]);
+      MX_TRY(launch_getrf<float>(batch, n, p.lu2[l], n, nn, p.piv2[l], status, s));
+      MX_TRY(launch_getrs_right_f(batch, n, p.lu2[l], n, nn, p.piv2[l], p.Gb, n, nn, n, s));
+      MX_TRY(launch_copy<float>(batch, n, n, p.Gb, n, nn, gam(l), n, nn, s));
+    }
+  }
+  MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.inc, gam(0), p.lu0);
+  MX_TRY(launch_getrf<float>(batch, n, p.lu0, n, nn, p.piv0, status, s));
+  // ---- 3. iterative refinement of the stack equations ----
+  Table tb;
+  tb.L = L;
+  tb.nh = nh;
+  tb.batch = batch;
+  tb.inc = p.inc;
+  tb.trn = p.trn;
+  tb.lu0 = p.lu0;
+  tb.piv0 = p.piv0;
+  tb.gam = p.gam;
+  for (int l = 0; l < L; ++l) {
+    Elem& E = tb.e[l];
+    E.kind = kinds[l] == 1 ? 1 : 0;
+    E.slot = slot[l];
+    E.depth = depths[l];
+    E.blocks = p.blocks[l];
+    E.lu1 = p.lu1[l];
+    E.piv1 = p.piv1[l];
+    E.lu2 = p.lu2[l];
+    E.piv2 = p.piv2[l];
+    E.zr = p.zr[l];
+  }
+  for (size_t m = 0; m < used.size(); ++m) {
+    MapPtrs& M = tb.m[m];
+    M.W64 = p.W64[m];
+    M.V64 = p.V64[m];
+    M.lam64 = p.lam64[m];
+    M.W32 = p.W32[m];
+    M.V32 = p.V32[m];
+    M.lam32 = p.lam32[m];
+    M.Wi = p.Wi[m];
+    M.Vi = p.Vi[m];
+  }
+  const size_t xbytes = sizeof(cd) * batch * (size_t)(2 * (L + 1)) * 2 * n;
+  if (cudaMemsetAsync(p.X, 0, xbytes, s) != cudaSuccess) return KHP_ERR_CUDA;
+  if (cudaMemsetAsync(p.XA, 0, sizeof(cd) * batch * (size_t)(2 * std::max(L, 1)) * 2 * n, s) != cudaSuccess)
+    return KHP_ERR_CUDA;
+  if (cudaMemsetAsync(p.RT, 0, sizeof(cd) * batch * 4 * n, s) != cudaSuccess) return KHP_ERR_CUDA;
+  for (int it = 0; it <= refine; ++it) {
+    k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr);
+    count_launches(1);
+    MX_TRY(cuda_status());
+    k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW);
+    count_launches(1);
+    MX_TRY(cuda_status());
+  }
+  k_flux_cols<double><<<(unsigned)batch, 128, 0, s>>>(nh, npol, p.RT, p.RT + batch * 2 * n, gx, gy, kp, k0,
+                                                       reinterpret_cast<const cd*>(te), reinterpret_cast<const cd*>(tm),
+                                                       epsi, epse, R, Tt);
+  count_launches(1);
+  return cuda_status();
+}
+
+}  // namespace
+}  // namespace khp
+
+using namespace khp;
+
+extern "C" {
+
+size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
+                                         const int32_t* layer_map) {
+  if (batch < 0 || nh < 1 || nlayers < 0 || nlayers > kMaxLayers || (nlayers > 0 && (!layer_kind || !layer_map)))
+    return 0;
+  std::vector<int> seen;
+  for (int l = 0; l < nlayers; ++l) {
+    if (layer_kind[l] != 1) continue;
+    if (std::find(seen.begin(), seen.end(), layer_map[l]) == seen.end()) seen.push_back(layer_map[l]);
+  }
+  Arena a{nullptr, 0};
+  plan_mixed(a, batch, nh, nlayers, layer_kind, (int)seen.size());
+  return a.off;
+}
+
+int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                            const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                            int64_t nmaps, const double* conv, const double* hx, const double* hy, const double* gx,
+                            const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
+                            const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
+                            int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
+                            size_t ws_bytes, void* stream) {
+  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 0 || refine_iters > 8 || !gx || !gy ||
+      !kp || !k0 || !te || !tm || !R || !T || !status)
+    return KHP_ERR_INVALID_ARG;
+  if (nlayers > kMaxLayers) return KHP_ERR_TOO_LARGE;
+  if (nlayers > 0 && (!layer_kind || !layer_map || !layer_eps || !layer_depth)) return KHP_ERR_INVALID_ARG;
+  for (int l = 0; l < nlayers; ++l) {
+    if (layer_kind[l] != 0 && layer_kind[l] != 1) return KHP_ERR_INVALID_ARG;
+    if (layer_kind[l] == 1 && (layer_map[l] < 0 || layer_map[l] >= nmaps || !conv || !hx || !hy))
+      return KHP_ERR_INVALID_ARG;
+  }
+  if (batch == 0) return KHP_OK;
+  return solve_mixed(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, conv, hx, hy, gx, gy,
+                     mk(epsi_re, epsi_im), mk(epse_re, epse_im), kp, k0, npol, te, tm, refine_iters, R, T, status,
+                     workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
