@@ -48,6 +48,13 @@ FLOPS_PER_CALL = {
 }
 
 
+def solve_mixed_flops(n, nmaps, npattern, nhomog):
+    """Algorithmic flops per problem of khp_solve_batched_mixed (FP32 and FP64 together): the
+    recursion as in solve_batched_flops, plus per map the eigen-refinement (FP64 residual GEMM
+    8 n^3, FP32 solve 10.67 n^3, FP32 correction GEMM 8 n^3, FP64 V = QW 4 n^3)."""
+    return solve_batched_flops(n, nmaps, npattern, nhomog) + n ** 3 * nmaps * (8.0 + 10.67 + 8.0 + 4.0)
+
+
 def solve_batched_flops(n, nmaps, npattern, nhomog):
     """Algorithmic flops per problem of khp_solve_batched: per distinct map the modes (117 n^3)
     and W^-1, V^-1 (2 x 10.67 n^3); per patterned layer 4 GEMMs + 2 LU + 2 right-solves
@@ -63,6 +70,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=304)
     ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=6)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--refine", type=int, default=2)
+    ap.add_argument("--plain", type=int, default=2, help="single-problem drop-in solves timed for comparison")
     return ap.parse_args()
 
 
@@ -228,9 +238,12 @@ def run_gpu(args):
     plan = batch.StackPlan(struct, specs, st.stack)
     npat = int((plan.kinds == 1).sum())
     FLOPS_PER_CALL["khp_solve_batched"] = solve_batched_flops(N_MAT, plan.nmaps, npat, len(plan.kinds) - npat)
+    FLOPS_PER_CALL["khp_solve_batched_mixed"] = solve_mixed_flops(N_MAT, plan.nmaps, npat, len(plan.kinds) - npat)
+    prec = args.precision
 
     def step(k):
-        return batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k])
+        return batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k], precision=prec,
+                                                 refine=args.refine)
 
     for k in range(args.warmup):
         step(k)
@@ -281,8 +294,51 @@ def run_gpu(args):
                 "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
                 "peak_source": "FP64 FMA pipe measured in this run (khp_probe_fp64_tflops); MEASURED_PEAKS.json "
                                "lists only HBM and bf16",
+                "note": "the mixed path runs its O(n^3) work on the FP32 pipe (70 TFLOP/s measured), so its "
+                        "fraction of the FP64 pipe can exceed 1" if prec == "mixed" else None,
                 "flops_per_launch": FLOPS_PER_CALL[dom] * B, "launch_ms": dom_ms / dom_calls,
                 "share_of_step": share}
+
+    # error of the timed path against the FP64 recursion on the first timed chunk (untimed)
+    err = None
+    fp64_rate = None
+    if prec == "mixed":
+        inside = np.flatnonzero(np.hypot(kp_all[:, 0], kp_all[:, 1]) < 2 * np.pi / wl_all)
+        sel = np.sort(np.random.default_rng(2).choice(inside, B, replace=False))
+        pchk = engine.Problems.make(wl_all[sel], kp_all[sel], 1.0, 0.0, dev)
+        st_a = torch.zeros(B, dtype=torch.int32, device=dev)
+        st_b = torch.zeros(B, dtype=torch.int32, device=dev)
+        Rm, Tm = batch.solve_chunk_gamma_both_pols(struct, plan, pchk, st_a, precision="mixed", refine=args.refine)
+        torch.cuda.synchronize()
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        e2.record()
+        R64, T64 = batch.solve_chunk_gamma_both_pols(struct, plan, pchk, st_b, precision="fp64")
+        e3.record()
+        torch.cuda.synchronize()
+        fp64_rate = B / (e2.elapsed_time(e3) * 1e-3)
+        err = max((Rm - R64).abs().max().item(), (Tm - T64).abs().max().item())
+
+    # the plain drop-in path: one Crystal.solve + poynting_flux_end per call (FP64 chain)
+    plain_rate = None
+    if rank == 0 and args.plain > 0:
+        from khepri_gb300 import Crystal
+        cl = Crystal(st.pw, device=dev)
+        for name, (kind, eps, depth) in st.layers.items():
+            (cl.add_layer_uniform if kind == "uniform" else cl.add_layer_pixmap)(name, eps, depth)
+        cl.set_device(st.stack, False)
+        idx = chunk(args.warmup)[: args.plain + 1]
+        cl.set_source(wl_all[idx[0]], 1.0, 0.0, kp=tuple(kp_all[idx[0]]))
+        cl.solve()
+        cl.poynting_flux_end()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for p_ in idx[1:]:
+            cl.set_source(wl_all[p_], 1.0, 0.0, kp=tuple(kp_all[p_]))
+            cl.solve()
+            cl.poynting_flux_end()
+        torch.cuda.synchronize()
+        plain_rate = args.plain / (time.perf_counter() - t0)
 
     # end to end through the public API: host numpy inputs -> host R, T
     e2e_steps = max(1, min(args.steps, 3))
@@ -292,7 +348,8 @@ def run_gpu(args):
     for k in range(e2e_steps):
         idx = chunk(args.warmup + k)
         batch.solve_rt(st.pw, st.layers, st.stack, wl_all[idx], kp_all[idx], chunk=B, struct=struct,
-                       strict=False, both_pols=True, method="gamma")
+                       strict=False, both_pols=True, method="mixed" if prec == "mixed" else "gamma",
+                       refine=args.refine)
     torch.cuda.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -315,8 +372,17 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
             "config": {"workload": "batched sweep 11x11 (n=242), 256x256 multi-disc map, [P,U,P,U,P], 64 f x "
                                    "32x32 k, both polarisations per S-matrix",
-                       "batch": B, "harmonics": "11x11", "precision": "fp64 (complex128) throughout",
-                       "method": "reflection-matrix recursion (khp_solve_batched), one eigensolve per problem",
+                       "batch": B, "harmonics": "11x11",
+                       "precision": ("mixed: FP32 O(n^3) work, FP64 eigen-refinement and %d rounds of FP64 "
+                                     "iterative refinement" % args.refine) if prec == "mixed"
+                       else "fp64 (complex128) throughout",
+                       "max_abs_err_vs_fp64": err,
+                       "err_sample": "R and T, both polarisations, of %d random in-cone problems of the sweep, "
+                                     "mixed vs the FP64 recursion" % B,
+                       "fp64_recursion_solves_per_s": fp64_rate,
+                       "plain_dropin_gpu_solves_per_s": plain_rate,
+                       "method": "reflection-matrix recursion (khp_solve_batched%s), one eigensolve per problem"
+                                 % ("_mixed" if prec == "mixed" else ""),
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
                        "grad": "solve+grad/s not measured by this bench"},

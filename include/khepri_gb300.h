@@ -136,6 +136,23 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
                       int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 /*
+ * Mixed-precision form of khp_solve_batched (same arguments plus refine_iters; at most 16
+ * layers).  Every O(n^3) step runs in FP32; FP64 is used for one eigen-refinement step per
+ * patterned-layer eigensolve (residual M W - W mu) and for the residual of the whole stack's
+ * interface equations, which refine_iters rounds of iterative refinement drive to FP64
+ * accuracy through the FP32 factors (0 = FP32 answer only; 2 is the default of the Python API).
+ */
+size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
+                                         const int32_t* layer_map);
+int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                            const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                            int64_t nmaps, const double* conv, const double* hx, const double* hy, const double* gx,
+                            const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
+                            const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
+                            int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
+                            size_t ws_bytes, void* stream);
+
+/*
  * Star product without a caller-supplied workspace.  No counterpart in the reference: it
  * serves callers that cannot allocate or lend device memory (a host whose device memory is
  * fully partitioned up front, or a latency-critical loop where cudaMalloc, which may

@@ -49,6 +49,10 @@ _SIGNATURES = {
     "khp_solve_batched": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p, _c_p,
                                          _c_p, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_p, _c_p, _c_i32, _c_p, _c_p,
                                          _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_solve_batched_mixed_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_p, _c_p]),
+    "khp_solve_batched_mixed": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p,
+                                               _c_p, _c_p, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_p, _c_p, _c_i32,
+                                               _c_p, _c_p, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
 }

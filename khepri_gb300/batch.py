@@ -100,7 +100,8 @@ def _host(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None):
+def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None, precision="fp64",
+                      refine=2):
     """R, T of one chunk by the reflection-matrix recursion (khp_solve_batched).
 
     te, tm: optional [B, npol] complex device tensors (default: prob.te, prob.tm as one
@@ -118,17 +119,25 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
     T = torch.empty((B, npol), dtype=torch.float64, device=dev)
     lib = _capi.load()
     L = len(plan.kinds)
-    ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)), dev)
     epsi, epse = complex(epsi), complex(epse)
-    with engine._stage("khp_solve_batched"):
-        code = lib.khp_solve_batched(B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps),
-                                     _host(plan.eps), _host(plan.depth), plan.nmaps, _capi.ptr(plan.conv),
-                                     _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx),
-                                     _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
-                                     _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm),
-                                     _capi.ptr(R), _capi.ptr(T), _capi.ptr(status), _capi.ptr(ws), ws.numel(),
-                                     _capi.stream_ptr())
-    _capi.check(code, "khp_solve_batched")
+    common = (B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
+              _host(plan.depth), plan.nmaps, _capi.ptr(plan.conv), _capi.ptr(plan.hx), _capi.ptr(plan.hy),
+              _capi.ptr(struct.gx), _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
+              _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm))
+    if precision == "mixed":
+        ws = engine.workspace(lib.khp_solve_batched_mixed_workspace(B, struct.nh, L, _host(plan.kinds),
+                                                                     _host(plan.maps)), dev)
+        with engine._stage("khp_solve_batched_mixed"):
+            code = lib.khp_solve_batched_mixed(*common, int(refine), _capi.ptr(R), _capi.ptr(T), _capi.ptr(status),
+                                               _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+        _capi.check(code, "khp_solve_batched_mixed")
+    else:
+        ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)),
+                              dev)
+        with engine._stage("khp_solve_batched"):
+            code = lib.khp_solve_batched(*common, _capi.ptr(R), _capi.ptr(T), _capi.ptr(status), _capi.ptr(ws),
+                                         ws.numel(), _capi.stream_ptr())
+        _capi.check(code, "khp_solve_batched")
     if one_pol:
         return R[:, 0], T[:, 0]
     return R, T
@@ -143,23 +152,26 @@ def both_pol_weights(B, device):
     return te, tm
 
 
-def solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi=1.0, epse=1.0):
+def solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi=1.0, epse=1.0, precision="fp64", refine=2):
     """R, T [B, 2] for (te, tm) = (1, 0) and (0, 1) from one recursion per problem."""
     te, tm = both_pol_weights(prob.batch, struct.device)
-    return solve_chunk_gamma(struct, plan, prob, status, epsi, epse, te, tm)
+    return solve_chunk_gamma(struct, plan, prob, status, epsi, epse, te, tm, precision, refine)
 
 
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
-             chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False, method="gamma"):
+             chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False, method="gamma",
+             refine=2):
     """R and T of every problem (host numpy arrays); problems share ``layers``/``stack``.
 
     layers: name -> ("pixmap", eps_map, depth) | ("uniform", eps, depth); stack: layer names
     from the incidence side.  wavelengths [P], kp [P, 2] (absolute, complex allowed), te/tm
     scalars or [P].  Returns (R, T, status) or (R, T, r_orders, t_orders, status) with
     ``orders=True``.  ``both_pols=True`` returns R, T of shape [P, 2] for (te, tm) = (1, 0)
-    and (0, 1).  ``method``: "gamma" (reflection-matrix recursion, khp_solve_batched; R and T
-    only) or "chain" (layer S-matrices and the star-product chain, as the reference; needed for
-    per-order powers).  With ``strict`` a non-zero per-problem status raises KhpError.
+    and (0, 1).  ``method``: "gamma" (reflection-matrix recursion in FP64, khp_solve_batched),
+    "mixed" (the same recursion in FP32 with FP64 eigen-refinement and ``refine`` rounds of FP64
+    iterative refinement, khp_solve_batched_mixed) or "chain" (layer S-matrices and the
+    star-product chain, as the reference; needed for per-order powers).  With ``strict`` a
+    non-zero per-problem status raises KhpError.
     """
     if orders:
         method = "chain"
@@ -172,7 +184,8 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     if struct is None:
         struct = engine.StructureGPU(pw, engine.lattice_vectors(lattice), device)
     specs = _specs(layers, epsi, epse)
-    plan = StackPlan(struct, specs, stack) if method == "gamma" else None
+    plan = StackPlan(struct, specs, stack) if method in ("gamma", "mixed") else None
+    prec = "mixed" if method == "mixed" else "fp64"
     R = np.empty((P, 2) if both_pols else P)
     T = np.empty((P, 2) if both_pols else P)
     ro = np.empty((P, struct.nh)) if orders else None
@@ -182,12 +195,12 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
         e = min(P, s + chunk)
         prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
         status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
-        if method == "gamma":
+        if method in ("gamma", "mixed"):
             r_o = t_o = None
             if both_pols:
-                r, t = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse)
+                r, t = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine)
             else:
-                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse)
+                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine)
         elif both_pols:
             r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
             r_o = t_o = None

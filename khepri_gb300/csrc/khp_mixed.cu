@@ -3,7 +3,7 @@
 //
 // GB300 runs FP32 at ~58x its FP64 rate, but an all-FP32 solve misses |dR|, |dT| <= 1e-6 (errors
 // of a few 1e-6 on the 11x11 sweep).  This pipeline:
-//   1. modes: FP32 eigensolve of M = P Q, then one FP64 refinement step of the eigenpairs:
+//   1. modes: FP32 eigensolve of M = P Q, then two FP64 refinement steps of the eigenpairs:
 //      E = W^-1 (M W - W mu) with the residual formed in FP64 and the solve in FP32,
 //      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i) (pairs closer than a relative
 //      1e-5 are left coupled: their coupling error is second order);  V = Q W / lam in FP64;
@@ -38,30 +38,29 @@ constexpr int kMaxLayers = 16;
 // ------------------------------------------------------------------------------------------
 // R32 = (M64 W64 - W64 diag(mu)) in FP32, where MW already holds M64 W64.
 __global__ void k_eig_residual(int64_t batch, int n, const cd* __restrict__ MW, const cd* __restrict__ W64,
-                               const cf* __restrict__ mu, cf* R32) {
+                               const cd* __restrict__ mu, cf* R32) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int j = (int)(e % nn) % n;
-    const cf m = mu[b * n + j];
-    const cd r = MW[e] - W64[e] * mk((double)m.re, (double)m.im);
+    const cd r = MW[e] - W64[e] * mu[b * n + j];
     R32[e] = mk((float)r.re, (float)r.im);
   }
 }
 
-// mu64 = mu32 + diag(E); F_ij = E_ij / (mu_j - mu_i) for well-separated pairs (in place on E).
-__global__ void k_eig_update(int64_t batch, int n, const cf* __restrict__ mu32, cf* E, cd* mu64) {
+// mu_out = mu_in + diag(E); F_ij = E_ij / (mu_j - mu_i) for well-separated pairs (in place on E).
+__global__ void k_eig_update(int64_t batch, int n, const cd* __restrict__ mu_in, cf* E, cd* mu_out) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int rc = (int)(e % nn);
     const int i = rc / n, j = rc % n;
-    const cd mi = mk((double)mu32[b * n + i].re, (double)mu32[b * n + i].im);
-    const cd mj = mk((double)mu32[b * n + j].re, (double)mu32[b * n + j].im);
+    const cd mi = mu_in[b * n + i];
+    const cd mj = mu_in[b * n + j];
     const cf ev = E[e];
     const cd ed = mk((double)ev.re, (double)ev.im);
     if (i == j) {
-      mu64[b * n + i] = mi + ed;
+      mu_out[b * n + i] = mi + ed;
       E[e] = mk(0.f, 0.f);
       continue;
     }
@@ -535,7 +534,7 @@ struct MixedPlan {
   std::vector<cd*> W64, V64, lam64;
   // modes scratch
   cf *M32, *Z32, *E32, *lu32;
-  cd *M64, *MW64, *CW64, *Ct64, *mu64;
+  cd *M64, *MW64, *CW64, *Ct64, *mu64, *mu64b;
   int* piv;
   // per layer
   std::vector<cf*> lu1, lu2, zr;
@@ -573,6 +572,7 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.CW64 = a.take<cd>(batch * nn);
   p.Ct64 = nullptr;
   p.mu64 = a.take<cd>(batch * n);
+  p.mu64b = a.take<cd>(batch * n);
   p.piv = a.take<int>(batch * n);
   for (int l = 0; l < L; ++l) {
     p.lu1.push_back(a.take<cf>(batch * nn));
@@ -656,19 +656,25 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     const cd* HY = reinterpret_cast<const cd*>(hy) + used[m] * hh;
     MX_EW(k_assemble_pq_t<float>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M32);
     MX_TRY(launch_geev<float>(batch, n, p.M32, n, nn, p.Z32, p.W32[m], n, nn, p.lam32[m], n, status, s));
-    // residual R = M W - W mu in FP64
+    // Two refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 factors of the FP32 W),
+    // mu += diag(E), W += W F.
     MX_EW(k_assemble_pq_t<double>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M64);
     MX_EW(k_to_double, batch * nn, batch * nn, p.W32[m], p.W64[m]);
-    MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
-    MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], p.lam32[m], p.E32);
-    // E = W^-1 R (FP32), F, W += W F
+    MX_EW(k_to_double, batch * n, batch * n, p.lam32[m], p.mu64);
     MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
     MX_TRY(launch_getrf<float>(batch, n, p.lu32, n, nn, p.piv, status, s));
-    MX_TRY(launch_getrs<float>(batch, n, p.lu32, n, nn, p.piv, p.E32, n, nn, n, s));
-    MX_EW(k_eig_update, batch * nn, batch, n, p.lam32[m], p.E32, p.mu64);
-    MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.E32, n, nn, zero, p.M32, n, nn, s));
-    MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.M32, p.W32[m]);
-    MX_EW(k_sqrt_mu, batch * n, batch * n, p.mu64, p.lam64[m], p.lam32[m]);
+    cd* mu_a = p.mu64;
+    cd* mu_b = p.mu64b;
+    for (int step = 0; step < 2; ++step) {
+      MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
+      MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], mu_a, p.E32);
+      MX_TRY(launch_getrs<float>(batch, n, p.lu32, n, nn, p.piv, p.E32, n, nn, n, s));
+      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.E32, mu_b);
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.E32, n, nn, zero, p.M32, n, nn, s));
+      MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.M32, p.W32[m]);
+      std::swap(mu_a, mu_b);
+    }
+    MX_EW(k_sqrt_mu, batch * n, batch * n, mu_a, p.lam64[m], p.lam32[m]);
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
     cd* CWb = p.CW64 + batch * hn;

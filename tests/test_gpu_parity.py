@@ -274,3 +274,39 @@ def test_gamma_vs_chain_sweep_chunk(khp):
     ok = np.isfinite(Rc)
     assert np.abs(Rg[ok] - Rc[ok]).max() < RT_TOL and np.abs(Tg[ok] - Tc[ok]).max() < RT_TOL
     assert np.abs(Rg[ok] + Tg[ok] - 1).max() < 1e-8
+
+
+def test_mixed_precision_11x11(khp, golden):
+    """khp_solve_batched_mixed (FP32 O(n^3) work, FP64 refinement) against the reference's
+    complex128 golden values and against the FP64 recursion on a sweep chunk: bar |dR|, |dT| <= 1e-6."""
+    from khepri_gb300 import batch, workloads
+    g = golden("batched_11x11")
+    st = workloads.batched_structure(int(g["seed"]))
+    wl, kp = workloads.batched_problems()
+    p = g["problems"]
+    R, T, s = batch.solve_rt(st.pw, st.layers, st.stack, wl[p], kp[p], both_pols=True, method="mixed")
+    assert not s.any()
+    np.testing.assert_allclose(R[:, 0], g["R_te"], atol=RT_TOL)
+    np.testing.assert_allclose(T[:, 0], g["T_te"], atol=RT_TOL)
+    np.testing.assert_allclose(R[:, 1], g["R_tm"], atol=RT_TOL)
+    np.testing.assert_allclose(T[:, 1], g["T_tm"], atol=RT_TOL)
+    idx = np.arange(20000, 20096)
+    Rm, Tm, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="mixed")
+    Rg, Tg, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="gamma")
+    ok = np.isfinite(Rg)
+    err = max(np.abs(Rm[ok] - Rg[ok]).max(), np.abs(Tm[ok] - Tg[ok]).max())
+    print("mixed vs fp64 max |dR|,|dT| =", err)
+    assert err < RT_TOL
+
+
+def test_mixed_precision_small_cases(khp, golden):
+    from khepri_gb300 import batch, engine
+    g = golden("oblique_5x5")
+    emap, d, eu = g["eps_map"], g["depths"], g["eps_u"]
+    layers = {"P1": ("pixmap", emap, d[0]), "U1": ("uniform", eu[0], d[1]), "P2": ("pixmap", emap, d[2]),
+              "U2": ("uniform", eu[1], d[3]), "P3": ("pixmap", emap, d[4])}
+    for i in range(len(g["R"])):
+        kp = engine.compute_kplanar(g["epsi"][i], g["wavelength"][i], g["theta"][i], g["phi"][i])
+        R, T, s = batch.solve_rt((5, 5), layers, ["P1", "U1", "P2", "U2", "P3"], [g["wavelength"][i]], [kp],
+                                 g["te"][i], g["tm"][i], epsi=g["epsi"][i], epse=g["epse"][i], method="mixed")
+        assert abs(R[0] - g["R"][i]) < RT_TOL and abs(T[0] - g["T"][i]) < RT_TOL
