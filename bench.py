@@ -212,7 +212,7 @@ def run_gpu(args):
 
     import __graft_entry__
     __graft_entry__.build()
-    from khepri_gb300 import _capi, batch, engine, workloads
+    from khepri_gb300 import _capi, batch, engine, replicas, workloads
 
     lib = _capi.load()
     st = workloads.batched_structure(0)
@@ -226,9 +226,7 @@ def run_gpu(args):
             struct.prepare_map(sp.eps)  # per-structure preparation, outside the timed region
 
     def chunk(step):
-        s = ((step * world + rank) * B) % P
-        idx = np.arange(s, s + B) % P
-        return idx
+        return replicas.chunk_indices(P, B, step, rank, world)
 
     nsteps = args.warmup + args.steps
     probs = [engine.Problems.make(wl_all[chunk(k)], kp_all[chunk(k)], 1.0, 0.0, dev) for k in range(nsteps)]
@@ -272,11 +270,7 @@ def run_gpu(args):
         barrier()
     launches = lib.khp_launch_count() - launches0
     ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms * 1e-3)
     bad = int(sum(int((s != 0).sum().item()) for s in statuses))
 

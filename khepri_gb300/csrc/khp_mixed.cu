@@ -3,10 +3,12 @@
 //
 // GB300 runs FP32 at ~58x its FP64 rate, but an all-FP32 solve misses |dR|, |dT| <= 1e-6 (errors
 // of a few 1e-6 on the 11x11 sweep).  This pipeline:
-//   1. modes: FP32 eigensolve of M = P Q, then two FP64 refinement steps of the eigenpairs:
+//   1. modes: FP32 eigensolve of M = P Q, then three FP64 refinement steps of the eigenpairs:
 //      E = W^-1 (M W - W mu) with the residual formed in FP64 and the solve in FP32,
-//      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i) (pairs closer than a relative
-//      1e-5 are left coupled: their coupling error is second order);  V = Q W / lam in FP64;
+//      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i); mutually nearest eigenvalues
+//      closer than 3e-3 max|mu| take the exact 2x2 update of their block of E instead (first
+//      order converges slowly there); other pairs closer than 1e-5 relative stay coupled
+//      (second-order error);  V = Q W / lam in FP64;
 //   2. the reflection-matrix recursion of khp_solve_batched on the FP32-rounded refined modes,
 //      keeping every factor it makes (LU factors, rho, Gamma at every gap, Gamma M^-1);
 //   3. iterative refinement of the interface-continuity system of the whole stack (the
@@ -32,6 +34,9 @@ namespace {
 using cf = cplx<float>;
 
 constexpr int kMaxLayers = 16;
+// Eigen-refinement steps.  From this FP32 solver's eigenvectors (relative residual ~1e-6 on the
+// 11x11 P.Q) three pair-aware steps reach ~1e-10 even for eigenvalue pairs 1e-4 apart.
+constexpr int kEigSteps = 3;
 
 // ------------------------------------------------------------------------------------------
 // Eigen-refinement kernels
@@ -48,30 +53,85 @@ __global__ void k_eig_residual(int64_t batch, int n, const cd* __restrict__ MW, 
   }
 }
 
-// mu_out = mu_in + diag(E); F_ij = E_ij / (mu_j - mu_i) for well-separated pairs (in place on E).
-__global__ void k_eig_update(int64_t batch, int n, const cd* __restrict__ mu_in, cf* E, cd* mu_out) {
+// Close eigenvalue pairs: pair[i] = j when i and j are each other's nearest eigenvalue and closer
+// than 3e-3 max|mu|, else -1.  One CTA per problem.
+__global__ void __launch_bounds__(256) k_find_pairs(int n, const cd* __restrict__ mu, int* pair, int* nearest) {
+  __shared__ TeamShared sh;
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  const cd* m = mu + b * n;
+  int* pr = pair + b * n;
+  int* nr = nearest + b * n;
+  double big = 0.0;
+  int bi = 0;
+  for (int i = t.tid(); i < n; i += t.size()) {
+    const double a = cabs(m[i]);
+    if (a > big) { big = a; bi = i; }
+    double best = 1e300;
+    int bj = -1;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const double d = cabs(m[j] - m[i]);
+      if (d < best) { best = d; bj = j; }
+    }
+    nr[i] = bj;
+  }
+  team_argmax(t, big, bi, &sh);  // big = max |mu| for every thread
+  t.sync();
+  for (int i = t.tid(); i < n; i += t.size()) {
+    const int j = nr[i];
+    pr[i] = (j >= 0 && nr[j] == i && cabs(m[j] - m[i]) < 3e-3 * big) ? j : -1;
+  }
+}
+
+// The 2x2 eigen-decomposition of K = [[a, b], [c, d]] (a, d: the pair's updated diagonal),
+// with eigenvectors scaled to unit diagonal: returns den with v12 = -b/den, v21 = c/den,
+// new eigenvalues a + bc/den and d - bc/den (the root near a first).
+__device__ __forceinline__ cd pair_den(cd a, cd b, cd c, cd d) {
+  const cd h = 0.5 * (a - d);
+  const cd sq = csqrt(h * h + b * c);
+  return (h.re * sq.re + h.im * sq.im >= 0.0) ? h + sq : h - sq;
+}
+
+// mu_out = mu_in + diag(E) and F_ij = E_ij / (mu_j - mu_i), except for close pairs, which take
+// the exact 2x2 update; other pairs closer than 1e-5 relative stay coupled (F = 0).
+__global__ void k_eig_update(int64_t batch, int n, const cd* __restrict__ mu_in, const cf* __restrict__ E, cf* F,
+                             cd* mu_out, const int* __restrict__ pair) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int rc = (int)(e % nn);
     const int i = rc / n, j = rc % n;
-    const cd mi = mu_in[b * n + i];
-    const cd mj = mu_in[b * n + j];
-    const cf ev = E[e];
-    const cd ed = mk((double)ev.re, (double)ev.im);
-    if (i == j) {
-      mu_out[b * n + i] = mi + ed;
-      E[e] = mk(0.f, 0.f);
-      continue;
-    }
-    const cd d = mj - mi;
-    const double scale = cabs(mi) + cabs(mj);
-    if (cabs(d) > 1e-5 * scale) {
-      const cd f = cdiv(ed, d);
-      E[e] = mk((float)f.re, (float)f.im);
+    const cf* Eb = E + b * nn;
+    const int pi = pair[b * n + i];
+    cd out = mk(0.0);
+    if (pi >= 0 && (i == j || pi == j)) {
+      const int p = i < pi ? i : pi, q = i < pi ? pi : i;  // the pair, p < q
+      const cf epp = Eb[(int64_t)p * n + p], eqq = Eb[(int64_t)q * n + q];
+      const cf epq = Eb[(int64_t)p * n + q], eqp = Eb[(int64_t)q * n + p];
+      const cd a = mu_in[b * n + p] + mk((double)epp.re, (double)epp.im);
+      const cd d = mu_in[b * n + q] + mk((double)eqq.re, (double)eqq.im);
+      const cd bq = mk((double)epq.re, (double)epq.im), cq = mk((double)eqp.re, (double)eqp.im);
+      const cd den = pair_den(a, bq, cq, d);
+      const bool ok = !(den.re == 0.0 && den.im == 0.0);
+      if (i == j) {
+        mu_out[b * n + i] = ok ? (i == p ? a + cdiv(bq * cq, den) : d - cdiv(bq * cq, den)) : (i == p ? a : d);
+      } else if (ok) {
+        out = i == p ? -cdiv(bq, den) : cdiv(cq, den);
+      }
     } else {
-      E[e] = mk(0.f, 0.f);
+      const cf ev = Eb[(int64_t)i * n + j];
+      const cd ed = mk((double)ev.re, (double)ev.im);
+      const cd mi = mu_in[b * n + i];
+      if (i == j) {
+        mu_out[b * n + i] = mi + ed;
+      } else {
+        const cd mj = mu_in[b * n + j];
+        const cd dd = mj - mi;
+        if (cabs(dd) > 1e-5 * (cabs(mi) + cabs(mj))) out = cdiv(ed, dd);
+      }
     }
+    F[e] = mk((float)out.re, (float)out.im);
   }
 }
 
@@ -535,6 +595,7 @@ struct MixedPlan {
   // modes scratch
   cf *M32, *Z32, *E32, *lu32;
   cd *M64, *MW64, *CW64, *Ct64, *mu64, *mu64b;
+  int *pair, *nearest;
   int* piv;
   // per layer
   std::vector<cf*> lu1, lu2, zr;
@@ -573,6 +634,8 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.Ct64 = nullptr;
   p.mu64 = a.take<cd>(batch * n);
   p.mu64b = a.take<cd>(batch * n);
+  p.pair = a.take<int>(batch * n);
+  p.nearest = a.take<int>(batch * n);
   p.piv = a.take<int>(batch * n);
   for (int l = 0; l < L; ++l) {
     p.lu1.push_back(a.take<cf>(batch * nn));
@@ -665,13 +728,16 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(launch_getrf<float>(batch, n, p.lu32, n, nn, p.piv, status, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
-    for (int step = 0; step < 2; ++step) {
+    for (int step = 0; step < kEigSteps; ++step) {
       MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
       MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], mu_a, p.E32);
       MX_TRY(launch_getrs<float>(batch, n, p.lu32, n, nn, p.piv, p.E32, n, nn, n, s));
-      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.E32, mu_b);
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.E32, n, nn, zero, p.M32, n, nn, s));
-      MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.M32, p.W32[m]);
+      k_find_pairs<<<(unsigned)batch, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
+      count_launches(1);
+      MX_TRY(cuda_status());
+      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.E32, p.M32, mu_b, p.pair);      // M32 <- F
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
+      MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.Z32, p.W32[m]);
       std::swap(mu_a, mu_b);
     }
     MX_EW(k_sqrt_mu, batch * n, batch * n, mu_a, p.lam64[m], p.lam32[m]);
