@@ -132,6 +132,7 @@ struct TeamSerial {
   KHP_HD int tid() const { return 0; }
   KHP_HD int size() const { return 1; }
   KHP_HD void sync() const {}
+  KHP_HD void warp_sync() const {}
 };
 
 #ifdef __CUDACC__
@@ -139,6 +140,8 @@ struct TeamCta {
   __device__ __forceinline__ int tid() const { return threadIdx.x; }
   __device__ __forceinline__ int size() const { return blockDim.x; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
+  // barrier among the 32 lanes of the calling warp (used by warp-0-only phases)
+  __device__ __forceinline__ void warp_sync() const { __syncwarp(); }
 };
 #endif
 

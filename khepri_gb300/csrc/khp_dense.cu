@@ -31,10 +31,11 @@ __global__ void __launch_bounds__(kTeamThreads) k_getrs(int n, const cplx<T>* A,
   team_getrs(t, A + b * bsA, lda, n, piv + b * n, B + b * bsB, ldb, m);
 }
 
+// Schur form and eigenvectors of the triangular factor (X left in A, Q in Z); the back-transform
+// W = Z X runs afterwards as a batched tiled product.
 template <typename T>
-__global__ void __launch_bounds__(kTeamThreads) k_geev(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
-                                                        cplx<T>* W, int64_t ldw, int64_t bsW, cplx<T>* lam,
-                                                        int64_t bsLam, int* info) {
+__global__ void __launch_bounds__(kTeamThreads) k_geev_schur(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
+                                                              cplx<T>* lam, int64_t bsLam, int* info) {
   __shared__ TeamShared sh;
   __shared__ cplx<T> win[(KHP_HQR_WIN + 2) * (KHP_HQR_WIN + 2)];
   __shared__ cplx<T> rs[KHP_HQR_WIN];
@@ -43,9 +44,26 @@ __global__ void __launch_bounds__(kTeamThreads) k_geev(int n, cplx<T>* A, int64_
   cplx<T>* vbuf = reinterpret_cast<cplx<T>*>(dyn);
   TeamCta t;
   const int64_t b = blockIdx.x;
-  const int st = team_geev(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, W + b * bsW, ldw, lam + b * bsLam,
-                           vbuf, win, rc, rs, &sh);
+  cplx<T>* Ab = A + b * bsA;
+  cplx<T>* Zb = Z + b * (int64_t)n * n;
+  team_gehrd(t, Ab, lda, n, Zb, n, vbuf, &sh);
+  const int st = team_hqr_win(t, Ab, lda, n, Zb, n, win, rc, rs, &sh);
+  team_trevc(t, Ab, lda, n, lam + b * bsLam);
   if (threadIdx.x == 0 && st) info[b] |= st;
+}
+
+// Scale every column of W to unit 2-norm (thread per column, coalesced along rows).
+template <typename T>
+__global__ void k_normalize_cols(int64_t batch, int n, cplx<T>* W, int64_t ldw, int64_t bsW) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / n;
+    const int k = (int)(e % n);
+    cplx<T>* w = W + b * bsW + k;
+    T s = T(0);
+    for (int i = 0; i < n; ++i) s += norm2(w[(int64_t)i * ldw]);
+    const T inv = s > T(0) ? T(1) / sqrt(s) : T(1);
+    for (int i = 0; i < n; ++i) w[(int64_t)i * ldw] = w[(int64_t)i * ldw] * inv;
+  }
 }
 
 // Tiled product: CTA tile BM x BN, 256 threads as 16 x 16, each thread TM x TN outputs
@@ -144,6 +162,128 @@ __global__ void k_axpby(int n, int m, cplx<T> a, const cplx<T>* A, int64_t lda, 
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Blocked LU / inverse: panels of KHP_NB columns factorised in shared memory, trailing updates
+// and block-triangular solves as batched tiled products.
+// ------------------------------------------------------------------------------------------
+constexpr int KHP_NB = 32;
+
+// Factor the panel A[kb:n, kb:kb+w] (w <= KHP_NB) with partial pivoting, in shared memory.
+// piv[kb + jj] receives the global row swapped with row kb + jj (rows swapped inside the panel).
+template <typename T>
+__global__ void __launch_bounds__(256) k_panel_lu(int n, int kb, int w, cplx<T>* A, int64_t lda, int64_t bsA, int* piv,
+                                                  int* info) {
+  __shared__ TeamShared sh;
+  extern __shared__ unsigned char dyn[];
+  cplx<T>* P = reinterpret_cast<cplx<T>*>(dyn);  // (n - kb) x w, row-major, ld w
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  cplx<T>* Ab = A + b * bsA;
+  const int rows = n - kb;
+  for (int e = t.tid(); e < rows * w; e += t.size()) P[e] = Ab[(int64_t)(kb + e / w) * lda + kb + e % w];
+  t.sync();
+  int st = 0;
+  for (int jj = 0; jj < w; ++jj) {
+    T best = T(-1);
+    int bi = jj;
+    for (int i = jj + t.tid(); i < rows; i += t.size()) {
+      const T v = abs1(P[i * w + jj]);
+      if (v > best) { best = v; bi = i; }
+    }
+    team_argmax(t, best, bi, &sh);
+    if (t.tid() == 0) piv[b * n + kb + jj] = kb + bi;
+    if (!(best > T(0))) {
+      st |= (best == T(0)) ? KHP_BIT_SINGULAR : KHP_BIT_NONFINITE;
+      t.sync();
+      continue;
+    }
+    if (bi != jj)
+      for (int c = t.tid(); c < w; c += t.size()) {
+        const cplx<T> a = P[jj * w + c];
+        P[jj * w + c] = P[bi * w + c];
+        P[bi * w + c] = a;
+      }
+    t.sync();
+    const cplx<T> pv = P[jj * w + jj];
+    for (int i = jj + 1 + t.tid(); i < rows; i += t.size()) P[i * w + jj] = cdiv(P[i * w + jj], pv);
+    t.sync();
+    const int cw = w - jj - 1;
+    for (int e = t.tid(); e < (rows - jj - 1) * cw; e += t.size()) {
+      const int i = jj + 1 + e / cw, c = jj + 1 + e % cw;
+      fms_acc(P[i * w + c], P[i * w + jj], P[jj * w + c]);
+    }
+    t.sync();
+  }
+  for (int e = t.tid(); e < rows * w; e += t.size()) Ab[(int64_t)(kb + e / w) * lda + kb + e % w] = P[e];
+  if (threadIdx.x == 0 && st) info[b] |= st;
+}
+
+// Apply the row interchanges piv[k0:k1] to columns [c0, c1) of A (thread per column, in order).
+template <typename T>
+__global__ void k_laswp(int64_t batch, int n, int k0, int k1, int c0, int c1, cplx<T>* A, int64_t lda, int64_t bsA,
+                        const int* piv) {
+  const int nc = c1 - c0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nc; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nc;
+    const int c = c0 + (int)(e % nc);
+    cplx<T>* Ab = A + b * bsA;
+    for (int k = k0; k < k1; ++k) {
+      const int p = piv[b * n + k];
+      if (p != k) {
+        const cplx<T> a = Ab[(int64_t)k * lda + c];
+        Ab[(int64_t)k * lda + c] = Ab[(int64_t)p * lda + c];
+        Ab[(int64_t)p * lda + c] = a;
+      }
+    }
+  }
+}
+
+// B[r0:r0+w, 0:m] <- T^-1 B[r0:r0+w, 0:m] with T = the diagonal block A[d0:d0+w, d0:d0+w]
+// (unit lower when lower, else upper with its diagonal).  Thread per column of B; T in smem.
+template <typename T>
+__global__ void k_trsm_block(int w, int d0, const cplx<T>* __restrict__ A, int64_t lda, int64_t bsA, int r0, int m,
+                             cplx<T>* B, int64_t ldb, int64_t bsB, int lower, int64_t batch) {
+  __shared__ cplx<T> Tb[KHP_NB * KHP_NB];
+  const int64_t b = blockIdx.y;
+  const cplx<T>* Ab = A + b * bsA;
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) Tb[e] = Ab[(int64_t)(d0 + e / w) * lda + d0 + e % w];
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  cplx<T>* Bb = B + b * bsB + (int64_t)r0 * ldb + j;
+  cplx<T> x[KHP_NB];
+#pragma unroll
+  for (int i = 0; i < KHP_NB; ++i)
+    if (i < w) x[i] = Bb[(int64_t)i * ldb];
+  if (lower) {
+#pragma unroll
+    for (int i = 0; i < KHP_NB; ++i) {
+      if (i >= w) break;
+      cplx<T> acc = x[i];
+#pragma unroll
+      for (int k = 0; k < KHP_NB; ++k)
+        if (k < i) fms_acc(acc, Tb[i * w + k], x[k]);
+      x[i] = acc;
+    }
+  } else {
+#pragma unroll
+    for (int ii = KHP_NB - 1; ii >= 0; --ii) {
+      if (ii >= w) continue;
+      cplx<T> acc = x[ii];
+#pragma unroll
+      for (int k = 0; k < KHP_NB; ++k)
+        if (k > ii && k < w) fms_acc(acc, Tb[ii * w + k], x[k]);
+      x[ii] = cdiv(acc, Tb[ii * w + ii]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < KHP_NB; ++i)
+    if (i < w) Bb[(int64_t)i * ldb] = x[i];
+}
+
+// Grid for a thread-per-column row interchange: one thread per column up to 8 CTAs per SM.
+inline unsigned swp_blocks(int64_t columns) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((columns + 255) / 256, 152 * 8)); }
+
 inline int ew_blocks(int n, int m) {
   const int64_t e = (int64_t)n * m;
   return (int)std::min<int64_t>((e + 255) / 256, 64);
@@ -189,7 +329,15 @@ int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx
                 int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
   const size_t smem = sizeof(cplx<T>) * (size_t)n;
-  k_geev<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, W, ldw, bsW, lam, bsLam, info);
+  k_geev_schur<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
+  count_launches(1);
+  int st = cuda_status();
+  if (st) return st;
+  // W = Z X (X unit upper triangular, stored in A) and unit columns
+  st = launch_gemm<T>(batch, n, n, n, mk(T(1)), Z, n, (int64_t)n * n, A, lda, bsA, mk(T(0)), W, ldw, bsW, s);
+  if (st) return st;
+  const int64_t cols = batch * n;
+  k_normalize_cols<T><<<(unsigned)std::min<int64_t>((cols + 127) / 128, 152 * 16), 128, 0, s>>>(batch, n, W, ldw, bsW);
   count_launches(1);
   return cuda_status();
 }
@@ -236,6 +384,102 @@ int launch_inverse(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, c
   return launch_getrs<T>(batch, n, A, lda, bsA, piv, Ainv, ldi, bsI, n, s);
 }
 
+template <typename T>
+int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv, int* info,
+                         cudaStream_t s) {
+  if (batch <= 0) return KHP_OK;
+  constexpr size_t kPanelSmem = 200 * 1024;
+  for (int kb = 0, w = 0; kb < n; kb += w) {
+    // panel width: KHP_NB columns, fewer when the (n - kb) x w panel would not fit in shared memory
+    w = (int)std::min<size_t>({(size_t)KHP_NB, (size_t)(n - kb), kPanelSmem / (sizeof(cplx<T>) * (size_t)(n - kb))});
+    if (w < 1) return KHP_ERR_TOO_LARGE;
+    const size_t smem = sizeof(cplx<T>) * (size_t)(n - kb) * w;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return KHP_ERR_CUDA;
+    k_panel_lu<T><<<(unsigned)batch, 256, smem, s>>>(n, kb, w, A, lda, bsA, piv, info);
+    count_launches(1);
+    // row swaps of this panel to the columns left and right of it
+    const int other = n - w;
+    if (other > 0) {
+      if (kb > 0) {
+        k_laswp<T><<<swp_blocks(batch * kb), 256, 0, s>>>(batch, n, kb, kb + w, 0, kb,
+                                                                                             A, lda, bsA, piv);
+        count_launches(1);
+      }
+      if (kb + w < n) {
+        k_laswp<T><<<swp_blocks(batch * (n - kb - w)), 256, 0, s>>>(batch, n, kb, kb + w, kb + w, n, A, lda, bsA, piv);
+        count_launches(1);
+      }
+    }
+    const int rest = n - kb - w;
+    if (rest > 0) {
+      // U12 = L11^-1 A12, then A22 -= L21 U12
+      for (int64_t off = 0; off < batch; off += kMaxGridY) {
+        const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
+        k_trsm_block<T><<<dim3((rest + 127) / 128, nb), 128, 0, s>>>(w, kb, A + off * bsA, lda, bsA, kb, rest,
+                                                                    A + off * bsA + kb + w, lda, bsA, 1, nb);
+        count_launches(1);
+      }
+      const int st = launch_gemm<T>(batch, rest, rest, w, mk(T(-1)), A + (int64_t)(kb + w) * lda + kb, lda, bsA,
+                                    A + (int64_t)kb * lda + kb + w, lda, bsA, mk(T(1)),
+                                    A + (int64_t)(kb + w) * lda + kb + w, lda, bsA, s);
+      if (st) return st;
+    }
+  }
+  return cuda_status();
+}
+
+// Solve A X = B (n x m) with launch_getrf_blocked's factors: pivots, then block forward and
+// backward substitution with products for the off-diagonal blocks.
+template <typename T>
+int launch_getrs_blocked(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv, cplx<T>* B,
+                         int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
+  if (batch <= 0) return KHP_OK;
+  k_laswp<T><<<swp_blocks(batch * m), 256, 0, s>>>(batch, n, 0, n, 0, m, B, ldb,
+                                                                                      bsB, piv);
+  count_launches(1);
+  auto trsm = [&](int kb, int w, int lower) {
+    for (int64_t off = 0; off < batch; off += kMaxGridY) {
+      const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
+      k_trsm_block<T><<<dim3((m + 127) / 128, nb), 128, 0, s>>>(w, kb, A + off * bsA, lda, bsA, kb, m,
+                                                               B + off * bsB, ldb, bsB, lower, nb);
+      count_launches(1);
+    }
+  };
+  for (int kb = 0; kb < n; kb += KHP_NB) {
+    const int w = std::min(KHP_NB, n - kb);
+    if (kb > 0) {
+      const int st = launch_gemm<T>(batch, w, m, kb, mk(T(-1)), A + (int64_t)kb * lda, lda, bsA, B, ldb, bsB, mk(T(1)),
+                                    B + (int64_t)kb * ldb, ldb, bsB, s);
+      if (st) return st;
+    }
+    trsm(kb, w, 1);
+  }
+  const int last = ((n - 1) / KHP_NB) * KHP_NB;
+  for (int kb = last; kb >= 0; kb -= KHP_NB) {
+    const int w = std::min(KHP_NB, n - kb);
+    const int rest = n - kb - w;
+    if (rest > 0) {
+      const int st = launch_gemm<T>(batch, w, m, rest, mk(T(-1)), A + (int64_t)kb * lda + kb + w, lda, bsA,
+                                    B + (int64_t)(kb + w) * ldb, ldb, bsB, mk(T(1)), B + (int64_t)kb * ldb, ldb, bsB, s);
+      if (st) return st;
+    }
+    trsm(kb, w, 0);
+  }
+  return cuda_status();
+}
+
+template <typename T>
+int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
+                           int64_t bsI, int* piv, int* info, cudaStream_t s) {
+  int st = launch_identity<T>(batch, n, n, Ainv, ldi, bsI, mk(T(1)), s);
+  if (st) return st;
+  st = launch_getrf_blocked<T>(batch, n, A, lda, bsA, piv, info, s);
+  if (st) return st;
+  return launch_getrs_blocked<T>(batch, n, A, lda, bsA, piv, Ainv, ldi, bsI, n, s);
+}
+
 #define KHP_INSTANTIATE(T)                                                                                       \
   template int launch_getrf<T>(int64_t, int, cplx<T>*, int64_t, int64_t, int*, int*, cudaStream_t);             \
   template int launch_getrs<T>(int64_t, int, const cplx<T>*, int64_t, int64_t, const int*, cplx<T>*, int64_t,   \
@@ -250,7 +494,12 @@ int launch_inverse(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, c
   template int launch_axpby<T>(int64_t, int, int, cplx<T>, const cplx<T>*, int64_t, int64_t, cplx<T>,           \
                                const cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t, cudaStream_t);     \
   template int launch_inverse<T>(int64_t, int, cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t, int*,    \
-                                 int*, cudaStream_t);
+                                 int*, cudaStream_t);                                                           \
+  template int launch_getrf_blocked<T>(int64_t, int, cplx<T>*, int64_t, int64_t, int*, int*, cudaStream_t);     \
+  template int launch_getrs_blocked<T>(int64_t, int, const cplx<T>*, int64_t, int64_t, const int*, cplx<T>*,    \
+                                       int64_t, int64_t, int, cudaStream_t);                                    \
+  template int launch_inverse_blocked<T>(int64_t, int, cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t,  \
+                                         int*, int*, cudaStream_t);
 
 KHP_INSTANTIATE(double)
 KHP_INSTANTIATE(float)

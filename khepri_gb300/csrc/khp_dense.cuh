@@ -14,6 +14,51 @@
 namespace khp {
 
 template <typename T> KHP_HD T tmax(T a, T b) { return a > b ? a : b; }
+
+// sum_l conj(x[l]) * y[l * sy] with four independent partial sums (memory-level parallelism).
+template <typename T>
+KHP_HD cplx<T> dotc4(const cplx<T>* x, const cplx<T>* y, int64_t sy, int m) {
+  cplx<T> a0 = mk(T(0)), a1 = mk(T(0)), a2 = mk(T(0)), a3 = mk(T(0));
+  int l = 0;
+  for (; l + 3 < m; l += 4) {
+    a0 += conj_mul(x[l], y[l * sy]);
+    a1 += conj_mul(x[l + 1], y[(l + 1) * sy]);
+    a2 += conj_mul(x[l + 2], y[(l + 2) * sy]);
+    a3 += conj_mul(x[l + 3], y[(l + 3) * sy]);
+  }
+  for (; l < m; ++l) a0 += conj_mul(x[l], y[l * sy]);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// sum_l x[l] * y[l * sy] with four independent partial sums.
+template <typename T>
+KHP_HD cplx<T> dotu4s(const cplx<T>* x, const cplx<T>* y, int64_t sy, int m) {
+  cplx<T> a0 = mk(T(0)), a1 = mk(T(0)), a2 = mk(T(0)), a3 = mk(T(0));
+  int l = 0;
+  for (; l + 3 < m; l += 4) {
+    fma_acc(a0, x[l], y[l * sy]);
+    fma_acc(a1, x[l + 1], y[(l + 1) * sy]);
+    fma_acc(a2, x[l + 2], y[(l + 2) * sy]);
+    fma_acc(a3, x[l + 3], y[(l + 3) * sy]);
+  }
+  for (; l < m; ++l) fma_acc(a0, x[l], y[l * sy]);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// sum_l x[l] * y[l] (contiguous) with four independent partial sums.
+template <typename T>
+KHP_HD cplx<T> dotu4(const cplx<T>* x, const cplx<T>* y, int m) {
+  cplx<T> a0 = mk(T(0)), a1 = mk(T(0)), a2 = mk(T(0)), a3 = mk(T(0));
+  int l = 0;
+  for (; l + 3 < m; l += 4) {
+    fma_acc(a0, x[l], y[l]);
+    fma_acc(a1, x[l + 1], y[l + 1]);
+    fma_acc(a2, x[l + 2], y[l + 2]);
+    fma_acc(a3, x[l + 3], y[l + 3]);
+  }
+  for (; l < m; ++l) fma_acc(a0, x[l], y[l]);
+  return (a0 + a1) + (a2 + a3);
+}
 template <typename T> KHP_HD T tmin(T a, T b) { return a < b ? a : b; }
 
 // ------------------------------------------------------------------------------------------
@@ -126,14 +171,11 @@ KHP_HD void team_getrs_right(const Team& t, const cplx<T>* A, int64_t lda, int n
   for (int i = t.tid(); i < m; i += t.size()) {
     cplx<T>* x = B + (int64_t)i * ldb;
     for (int j = 0; j < n; ++j) {  // z U = b
-      cplx<T> acc = x[j];
-      for (int k = 0; k < j; ++k) fms_acc(acc, x[k], A[(int64_t)k * lda + j]);
+      const cplx<T> acc = x[j] - dotu4s(x, A + j, lda, j);
       x[j] = cdiv(acc, A[(int64_t)j * lda + j]);
     }
     for (int j = n - 2; j >= 0; --j) {  // y L = z (L unit lower)
-      cplx<T> acc = x[j];
-      for (int k = j + 1; k < n; ++k) fms_acc(acc, x[k], A[(int64_t)k * lda + j]);
-      x[j] = acc;
+      x[j] = x[j] - dotu4s(x + j + 1, A + (int64_t)(j + 1) * lda + j, lda, n - j - 1);
     }
     for (int k = n - 1; k >= 0; --k) {  // x = y Pi: undo the interchanges, last first
       const int p = piv[k];
@@ -198,21 +240,15 @@ KHP_HD void team_gehrd(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z,
     // H <- P^H H on rows k+1.., columns k+1..
     const cplx<T> ctau = conj(tau);
     for (int j = k + 1 + t.tid(); j < n; j += t.size()) {
-      cplx<T> w = mk(T(0));
-      for (int l = 0; l < m; ++l) w += conj_mul(vbuf[l], H[(k + 1 + l) * ld + j]);
-      w = ctau * w;
+      cplx<T> w = ctau * dotc4(vbuf, H + (int64_t)(k + 1) * ld + j, ld, m);
       for (int l = 0; l < m; ++l) fms_acc(H[(k + 1 + l) * ld + j], vbuf[l], w);
     }
     t.sync();
     // H <- H P on all rows, columns k+1..; Z <- Z P
     for (int i = t.tid(); i < n; i += t.size()) {
-      cplx<T> y = mk(T(0));
-      for (int l = 0; l < m; ++l) fma_acc(y, H[i * ld + k + 1 + l], vbuf[l]);
-      y = tau * y;
+      const cplx<T> y = tau * dotu4(H + (int64_t)i * ld + k + 1, vbuf, m);
       for (int l = 0; l < m; ++l) H[i * ld + k + 1 + l] -= mul_conj(y, vbuf[l]);
-      cplx<T> yz = mk(T(0));
-      for (int l = 0; l < m; ++l) fma_acc(yz, Z[i * ldz + k + 1 + l], vbuf[l]);
-      yz = tau * yz;
+      const cplx<T> yz = tau * dotu4(Z + (int64_t)i * ldz + k + 1, vbuf, m);
       for (int l = 0; l < m; ++l) Z[i * ldz + k + 1 + l] -= mul_conj(yz, vbuf[l]);
     }
     t.sync();
@@ -393,46 +429,52 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
       win[i * WS + j] = H[(int64_t)(r0 + i) * ld + c0 + j];
     }
     t.sync();
-    for (int k = k0; k < k1; ++k) {
-      const int lk = k - r0;       // window row of k
-      const int ck = k - c0;       // window column of k
-      if (t.tid() == 0) {
-        cplx<T> x, y;
-        if (k == lo) {
-          x = win[lk * WS + ck] - mu;
-          y = win[(lk + 1) * WS + ck];
-        } else {
-          x = win[lk * WS + ck - 1];
-          y = win[(lk + 1) * WS + ck - 1];
+    // The chase touches only the window: warp 0 runs it with warp barriers between steps.
+    if (t.tid() < 32) {
+      const int lane = t.tid();
+      const int lanes = t.size() < 32 ? t.size() : 32;
+      for (int k = k0; k < k1; ++k) {
+        const int lk = k - r0;  // window row of k
+        const int ck = k - c0;  // window column of k
+        if (lane == 0) {
+          cplx<T> x, y;
+          if (k == lo) {
+            x = win[lk * WS + ck] - mu;
+            y = win[(lk + 1) * WS + ck];
+          } else {
+            x = win[lk * WS + ck - 1];
+            y = win[(lk + 1) * WS + ck - 1];
+          }
+          T c;
+          cplx<T> s, r;
+          givens(x, y, c, s, r);
+          if (k > lo) {
+            win[lk * WS + ck - 1] = r;
+            win[(lk + 1) * WS + ck - 1] = mk(T(0));
+          }
+          rc[k - k0] = c;
+          rs[k - k0] = s;
         }
-        T c;
-        cplx<T> s, r;
-        givens(x, y, c, s, r);
-        if (k > lo) {
-          win[lk * WS + ck - 1] = r;
-          win[(lk + 1) * WS + ck - 1] = mk(T(0));
+        t.warp_sync();
+        const T c = rc[k - k0];
+        const cplx<T> s = rs[k - k0];
+        // row rotation from column k (column k-1 already holds r and 0 when k > lo)
+        for (int j = ck + lane; j < nc; j += lanes) {
+          const cplx<T> h1 = win[lk * WS + j], h2 = win[(lk + 1) * WS + j];
+          win[lk * WS + j] = c * h1 + s * h2;
+          win[(lk + 1) * WS + j] = c * h2 - conj_mul(s, h1);
         }
-        rc[k - k0] = c;
-        rs[k - k0] = s;
+        t.warp_sync();
+        const int ilast = ((k + 2 < hi) ? k + 2 : hi) - r0;
+        for (int i = lane; i <= ilast; i += lanes) {
+          const cplx<T> g1 = win[i * WS + ck], g2 = win[i * WS + ck + 1];
+          win[i * WS + ck] = c * g1 + mul_conj(g2, s);
+          win[i * WS + ck + 1] = c * g2 - s * g1;
+        }
+        t.warp_sync();
       }
-      t.sync();
-      const T c = rc[k - k0];
-      const cplx<T> s = rs[k - k0];
-      // row rotation from column k (column k-1 already holds r and 0 when k > lo)
-      for (int j = ck + t.tid(); j < nc; j += t.size()) {
-        const cplx<T> h1 = win[lk * WS + j], h2 = win[(lk + 1) * WS + j];
-        win[lk * WS + j] = c * h1 + s * h2;
-        win[(lk + 1) * WS + j] = c * h2 - conj_mul(s, h1);
-      }
-      t.sync();
-      const int ilast = ((k + 2 < hi) ? k + 2 : hi) - r0;
-      for (int i = t.tid(); i <= ilast; i += t.size()) {
-        const cplx<T> g1 = win[i * WS + ck], g2 = win[i * WS + ck + 1];
-        win[i * WS + ck] = c * g1 + mul_conj(g2, s);
-        win[i * WS + ck + 1] = c * g2 - s * g1;
-      }
-      t.sync();
     }
+    t.sync();
     for (int e = t.tid(); e < nr * nc; e += t.size()) {
       const int i = e / nc, j = e % nc;
       H[(int64_t)(r0 + i) * ld + c0 + j] = win[i * WS + j];

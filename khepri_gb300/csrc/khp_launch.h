@@ -46,6 +46,18 @@ template <typename T>
 int launch_inverse(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
                    int64_t bsI, int* piv, int* info, cudaStream_t s);
 
+// Blocked forms: panel LU in shared memory, trailing updates and off-diagonal blocks of the
+// triangular solves as batched tiled products (fast for n >> 32).
+template <typename T>
+int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv, int* info,
+                         cudaStream_t s);
+template <typename T>
+int launch_getrs_blocked(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv, cplx<T>* B,
+                         int64_t ldb, int64_t bsB, int m, cudaStream_t s);
+template <typename T>
+int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
+                           int64_t bsI, int* piv, int* info, cudaStream_t s);
+
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 
 // Adds k to the process-wide launch counter reported by khp_launch_count().
