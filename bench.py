@@ -73,6 +73,9 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--refine", type=int, default=2)
     ap.add_argument("--plain", type=int, default=2, help="single-problem drop-in solves timed for comparison")
+    ap.add_argument("--grad-designs", type=int, default=64,
+                    help="inverse-design structures (x 16 frequencies) for the solve+grad measurement (0 = skip)")
+    ap.add_argument("--uneven", type=int, default=96, help="uneven structures for the many-structure measurement")
     return ap.parse_args()
 
 
@@ -199,6 +202,96 @@ def run_reference(args):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def bench_grad(args, struct11, st11, wl_all, kp_all):
+    """Solve + gradient through the public API (host inputs -> host R, T, per-order powers and
+    pixmap gradients), host wall clock, after one untimed pass of the same call:
+    (a) the 11x11 sweep structure, loss = sum of T (te) over one chunk of problems, gradient with
+        respect to its 256x256 pixmap; (b) inverse design 9x9: designs x 16 frequencies, normal
+        incidence, loss = mean over f of the zeroth-order T, gradient w.r.t. each design."""
+    from khepri_gb300 import batch, workloads
+    out = {}
+    B = args.batch
+    inside = np.flatnonzero(np.hypot(kp_all[:, 0], kp_all[:, 1]) < 2 * np.pi / wl_all)
+    idx = np.sort(np.random.default_rng(4).choice(inside, B, replace=False))
+    entries = [(st11.pw, st11.layers, st11.stack)]
+    nh = st11.pw[0] * st11.pw[1]
+    dT = np.ones((B, nh))
+
+    def g11():
+        return batch.solve_structures_grad(entries, wl_all[idx], kp_all[idx], which=np.zeros(B, int), dT=dT,
+                                           chunk=B, strict=False)
+
+    def s11():
+        return batch.solve_structures(entries, wl_all[idx], kp_all[idx], which=np.zeros(B, int), chunk=B,
+                                      strict=False)
+
+    g11()
+    _, tg = _timed(g11)
+    s11()
+    _, ts = _timed(s11)
+    out["sweep_11x11"] = {"solve_grad_per_s": B / tg, "solve_per_s_same_call_path": B / ts,
+                          "problems": B, "loss": "sum of T (te) over the chunk",
+                          "wrt": "the 256x256 pixmap shared by the 3 patterned layers"}
+    if args.grad_designs > 0:
+        thetas, structs, freqs = workloads.inverse_design(args.grad_designs, seed=0)
+        D, F = len(structs), len(freqs)
+        ents = [(s.pw, s.layers, s.stack) for s in structs]
+        which = np.repeat(np.arange(D), F)
+        wl = np.tile(1.0 / freqs, D)
+        kp = np.zeros((D * F, 2))
+        nh9 = 81
+        dT9 = np.zeros((D * F, nh9))
+        dT9[:, (nh9 - 1) // 2] = 1.0 / F
+
+        def g9():
+            return batch.solve_structures_grad(ents, wl, kp, which=which, dT=dT9, chunk=1024, strict=False)
+
+        def s9():
+            return batch.solve_structures(ents, wl, kp, which=which, chunk=1024, strict=False)
+
+        g9()
+        res, tg9 = _timed(g9)
+        s9()
+        _, ts9 = _timed(s9)
+        out["inverse_design_9x9"] = {"solve_grad_per_s": D * F / tg9, "solve_per_s_same_call_path": D * F / ts9,
+                                     "problems": D * F, "designs": D, "frequencies": F,
+                                     "problems_with_status": int((res[5] != 0).sum()),
+                                     "loss": "mean over f of the zeroth-order T (te, normal incidence)",
+                                     "wrt": "each design's 64x64 eps map (shared by its 2 patterned layers)"}
+    return out
+
+
+def bench_uneven(args):
+    """Many structures of different sizes (3x3..17x17 harmonics, 1-8 lossy smoothed layers of
+    128x128, one problem each) through solve_structures (mixed), host wall clock."""
+    from khepri_gb300 import batch, workloads
+    if args.uneven <= 0:
+        return None
+    sts = workloads.uneven_structures(args.uneven, seed=0)
+    ents = [(s.pw, s.layers, s.stack) for s, _, _ in sts]
+    wl = np.array([w for _, w, _ in sts])
+    kp = np.array([k for _, _, k in sts])
+    small = min(8, len(ents))
+
+    def run(n):
+        return batch.solve_structures(ents[:n], wl[:n], kp[:n], te=1.0, tm=1.0, chunk=64, strict=False)
+
+    run(small)
+    res, t = _timed(lambda: run(len(ents)))
+    return {"structures_per_s": len(ents) / t, "structures": len(ents), "seconds": t,
+            "problems_with_status": int((res[2] != 0).sum()),
+            "sizes": "pw 3..17 odd, 1..8 layers; grouped by shape into batched calls"}
+
+
 def run_gpu(args):
     import torch
 
@@ -255,6 +348,7 @@ def run_gpu(args):
     timer = engine.StageTimer()
     results = []
     launches0 = lib.khp_launch_count()
+    repairs0 = batch.STATS["fp64_repairs"]
     with ClockSampler(local) as clocks:
         barrier()
         torch.cuda.synchronize()
@@ -269,6 +363,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         barrier()
     launches = lib.khp_launch_count() - launches0
+    repairs = batch.STATS["fp64_repairs"] - repairs0
     ms = e0.elapsed_time(e1)
     ms = replicas.max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms * 1e-3)
@@ -359,6 +454,10 @@ def run_gpu(args):
                "sample": f"{args.cpu_sample} in-cone problems of the 11x11 sweep, both polarisations, CPU oracle "
                          f"(numpy/LAPACK), {t_cpu:.1f} s"}
 
+    grad_info = uneven_info = None
+    if rank == 0:
+        grad_info = bench_grad(args, struct, st, wl_all, kp_all)
+        uneven_info = bench_uneven(args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -379,7 +478,8 @@ def run_gpu(args):
                                  % ("_mixed" if prec == "mixed" else ""),
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
-                       "grad": "solve+grad/s not measured by this bench"},
+                       "fp64_repairs": repairs,
+                       "solve_grad": grad_info, "uneven": uneven_info},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": world * B * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -10,8 +10,9 @@
  *   - Every pointer is a DEVICE pointer.  Every call is asynchronous on `stream` (a
  *     cudaStream_t, NULL = legacy default stream) and returns 0 (KHP_OK) or an error code;
  *     khp_status_string() names it.  Per-problem status words (int32, OR-ed flags
- *     1 = singular pivot, 2 = eigensolver not converged, 4 = non-finite value) are written
- *     to device arrays and are never turned into traps.
+ *     1 = singular pivot, 2 = eigensolver not converged, 4 = non-finite value, 8 = mixed-
+ *     precision refinement not converged, 16 = per-problem input out of range) are written to
+ *     device arrays and are never turned into traps.
  *   - No call allocates device memory: scratch comes from the caller through `workspace`
  *     (size from the matching *_workspace function, 256-byte aligned base).
  *   - Calls are reentrant per stream and hold no host-global state.
@@ -122,6 +123,13 @@ int khp_star_product(int64_t batch, int32_t n, const double* SA, int64_t sa_stri
  * source columns (same continuity conditions; patterned layers handled in their mode basis).
  *   layer_kind, layer_map, layer_eps, layer_depth: HOST arrays [nlayers] from the incidence side;
  *     kind 0 = uniform (eps: complex pair), 1 = patterned (map index into conv/hx/hy);
+ *     patterned layers with equal layer_map share their modes;
+ *   problem_map, problem_depth: optional DEVICE arrays [nlayers][batch] (NULL = layer_map /
+ *     layer_depth for every problem) giving each problem its own map index and depth per layer,
+ *     so that one call solves many structures of one shape (one harmonic set and layer
+ *     count); layers sharing a layer_map value must share the per-problem map too (the first
+ *     such layer's entry is used).  A map index outside [0, nmaps) sets status bit 16 and is
+ *     read as 0;
  *   conv, hx, hy: device complex [nmaps][nh][nh] from khp_convmat / khp_structure_prep;
  *   kp: complex [batch][2]; k0: [batch]; te, tm: complex [batch][npol] (npol polarisations
  *   share one recursion);  R, T: real [batch][npol].
@@ -129,7 +137,8 @@ int khp_star_product(int64_t batch, int32_t n, const double* SA, int64_t sa_stri
 size_t khp_solve_batched_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
                                    const int32_t* layer_map);
 int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
-                      const int32_t* layer_map, const double* layer_eps, const double* layer_depth, int64_t nmaps,
+                      const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                      const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
                       const double* conv, const double* hx, const double* hy, const double* gx, const double* gy,
                       double epsi_re, double epsi_im, double epse_re, double epse_im, const double* kp,
                       const double* k0, int32_t npol, const double* te, const double* tm, double* R, double* T,
@@ -137,20 +146,63 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
 
 /*
  * Mixed-precision form of khp_solve_batched (same arguments plus refine_iters; at most 16
- * layers).  Every O(n^3) step runs in FP32; FP64 is used for one eigen-refinement step per
+ * layers).  Every O(n^3) step runs in FP32; FP64 is used for three eigen-refinement steps per
  * patterned-layer eigensolve (residual M W - W mu) and for the residual of the whole stack's
  * interface equations, which refine_iters rounds of iterative refinement drive to FP64
  * accuracy through the FP32 factors (0 = FP32 answer only; 2 is the default of the Python API).
+ * A problem whose refinement has not converged (estimated error of its reflected or
+ * transmitted amplitudes above 1e-9, e.g. an ill-conditioned system next to a Wood anomaly)
+ * gets status bit 8; its R, T must then be recomputed with khp_solve_batched (the Python API
+ * does this).
  */
 size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
                                          const int32_t* layer_map);
 int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
                             const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
-                            int64_t nmaps, const double* conv, const double* hx, const double* hy, const double* gx,
+                            const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                            const double* conv, const double* hx, const double* hy, const double* gx,
                             const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
                             const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
                             int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
                             size_t ws_bytes, void* stream);
+
+/*
+ * Solve + gradient: khp_solve_batched_mixed and, in the same call, the gradient of
+ *   L = sum_{b,p,g} dR[b][p][g] R_{b,p,g} + dT[b][p][g] T_{b,p,g}
+ * (per-order reflected / transmitted powers, crystal.py:363-396 with only_total=False) with
+ * respect to the convolution matrix of every map, by the adjoint method: one transposed solve
+ * of the stack's interface equations per problem (FP64 residual, FP32 transposed sweep,
+ * refine_iters + 3 rounds) and the Daleckii-Krein form of the eigen-decomposition's
+ * derivative, which stays finite for degenerate modes.  No counterpart in the reference (it has
+ * no gradient; its users take finite differences of whole solves).
+ *   ic: device complex [nmaps][nh][nh] = C^-1 (khp_structure_prep);
+ *   dR, dT: device real [batch][npol][nh] (NULL = 0);  R_orders, T_orders: device real
+ *   [batch][npol][nh] out (NULL = not written);  dconv: device complex [nmaps][nh][nh] out, in
+ *   the convention dL = Re sum(dconv o dC) (summed over the problems using each map);
+ *   refine_iters >= 1.  A problem whose forward refinement did not converge keeps status bit 8
+ *   (no FP64 re-solve here).
+ */
+size_t khp_solve_batched_mixed_grad_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
+                                              const int32_t* layer_map, int64_t nmaps);
+int khp_solve_batched_mixed_grad(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                                 const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                                 const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                                 const double* conv, const double* ic, const double* hx, const double* hy,
+                                 const double* gx, const double* gy, double epsi_re, double epsi_im, double epse_re,
+                                 double epse_im, const double* kp, const double* k0, int32_t npol, const double* te,
+                                 const double* tm, int32_t refine_iters, const double* dR, const double* dT, double* R,
+                                 double* T, double* R_orders, double* T_orders, double* dconv, int32_t* status,
+                                 void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Adjoint of khp_convmat: deps = gradient with respect to the pixmaps, given dconv (both in
+ * the convention dL = Re sum(d o delta)).  eps real: dL/deps = Re(deps).  Backward counterpart
+ * of tools.py:33-56 (no counterpart in the reference).
+ *   dconv: device complex [nmaps][nh][nh];  deps: device complex [nmaps][nx][ny].
+ */
+size_t khp_convmat_bwd_workspace(int64_t nmaps, int64_t ny, int32_t px, int32_t py);
+int khp_convmat_bwd(int64_t nmaps, int64_t nx, int64_t ny, const double* dconv, int32_t px, int32_t py, double* deps,
+                    void* workspace, size_t ws_bytes, void* stream);
 
 /*
  * Star product without a caller-supplied workspace.  No counterpart in the reference: it

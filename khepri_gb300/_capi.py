@@ -46,13 +46,24 @@ _SIGNATURES = {
                                           _c_p, _c_p, _c_p, _c_p]),
     "khp_fields_idft": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p]),
     "khp_solve_batched_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_p, _c_p]),
-    "khp_solve_batched": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p, _c_p,
+    "khp_solve_batched": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_i64,
+                                         _c_p, _c_p,
                                          _c_p, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_p, _c_p, _c_i32, _c_p, _c_p,
                                          _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_solve_batched_mixed_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_p, _c_p]),
-    "khp_solve_batched_mixed": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i64, _c_p,
+    "khp_solve_batched_mixed": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                               _c_i64, _c_p,
                                                _c_p, _c_p, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_p, _c_p, _c_i32,
                                                _c_p, _c_p, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_solve_batched_mixed_grad_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_p, _c_p, _c_i64]),
+    # batch, px, py, nlayers, kind, map, eps, depth, pmap, pdepth, nmaps, conv, ic, hx, hy, gx, gy, epsi (2),
+    # epse (2), kp, k0, npol, te, tm, refine, dR, dT, R, T, R_orders, T_orders, dconv, status, ws, ws_bytes, stream
+    "khp_solve_batched_mixed_grad": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                                    _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_d, _c_d,
+                                                    _c_d, _c_d, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_i32, _c_p, _c_p,
+                                                    _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_convmat_bwd_workspace": (_c_sz, [_c_i64, _c_i64, _c_i32, _c_i32]),
+    "khp_convmat_bwd": (ctypes.c_int, [_c_i64, _c_i64, _c_i64, _c_p, _c_i32, _c_i32, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
 }
@@ -111,7 +122,8 @@ def require_cuda():
     load()
 
 
-STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-finite value"}
+STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-finite value",
+               8: "mixed-precision refinement not converged", 16: "per-problem input out of range"}
 
 
 def decode_status(word: int) -> str:

@@ -101,11 +101,13 @@ def _host(a):
 
 
 def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None, precision="fp64",
-                      refine=2):
+                      refine=2, pmap=None, pdepth=None):
     """R, T of one chunk by the reflection-matrix recursion (khp_solve_batched).
 
     te, tm: optional [B, npol] complex device tensors (default: prob.te, prob.tm as one
     polarisation); the recursion runs once and every polarisation is read from it.
+    pmap, pdepth: optional device tensors [L, B] (int32 map index into plan's maps, float64
+    depth) giving every problem its own maps and depths.
     Returns R, T of shape [B] (one polarisation) or [B, npol].
     """
     B = prob.batch
@@ -120,8 +122,16 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
     lib = _capi.load()
     L = len(plan.kinds)
     epsi, epse = complex(epsi), complex(epse)
+    if pmap is not None:
+        pmap = pmap.to(torch.int32).contiguous()
+        assert tuple(pmap.shape) == (L, B)
+    if pdepth is not None:
+        pdepth = pdepth.to(torch.float64).contiguous()
+        assert tuple(pdepth.shape) == (L, B)
     common = (B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
-              _host(plan.depth), plan.nmaps, _capi.ptr(plan.conv), _capi.ptr(plan.hx), _capi.ptr(plan.hy),
+              _host(plan.depth), _capi.ptr(pmap) if pmap is not None else None,
+              _capi.ptr(pdepth) if pdepth is not None else None, plan.nmaps, _capi.ptr(plan.conv),
+              _capi.ptr(plan.hx), _capi.ptr(plan.hy),
               _capi.ptr(struct.gx), _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
               _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm))
     if precision == "mixed":
@@ -131,6 +141,7 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
             code = lib.khp_solve_batched_mixed(*common, int(refine), _capi.ptr(R), _capi.ptr(T), _capi.ptr(status),
                                                _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
         _capi.check(code, "khp_solve_batched_mixed")
+        _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap, pdepth)
     else:
         ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)),
                               dev)
@@ -141,6 +152,29 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
     if one_pol:
         return R[:, 0], T[:, 0]
     return R, T
+
+
+REFINE_BIT = 8
+STATS = {"fp64_repairs": 0}  # problems re-solved in FP64 after a non-converged mixed refinement
+
+
+def _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap=None, pdepth=None):
+    """Re-solve in FP64 (khp_solve_batched) the problems whose mixed-precision refinement did
+    not converge (status bit 8: an ill-conditioned stack, e.g. next to a Wood anomaly), and
+    write their R, T and status in place."""
+    flagged = (status & REFINE_BIT) != 0
+    if not bool(flagged.any()):
+        return
+    idx = torch.nonzero(flagged).flatten()
+    STATS["fp64_repairs"] += int(idx.numel())
+    sub = prob.subset(idx)
+    st = torch.zeros(idx.numel(), dtype=torch.int32, device=status.device)
+    r, t = solve_chunk_gamma(struct, plan, sub, st, epsi, epse, te[idx].contiguous(), tm[idx].contiguous(),
+                             precision="fp64", pmap=None if pmap is None else pmap[:, idx],
+                             pdepth=None if pdepth is None else pdepth[:, idx])
+    R[idx] = r
+    T[idx] = t
+    status[idx] = (status[idx] & ~REFINE_BIT) | st
 
 
 def both_pol_weights(B, device):
@@ -218,3 +252,241 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     if orders:
         return R, T, ro, to, st
     return R, T, st
+
+
+# ------------------------------------------------------------------------------------------
+# Many structures of one shape per launch
+# ------------------------------------------------------------------------------------------
+class _ChunkPlan:
+    """StackPlan-like description of one chunk of problems over several structures of one shape:
+    per-layer kinds and uniform eps shared, maps and depths per problem."""
+
+    def __init__(self, kinds, slots, eps, conv, hx, hy):
+        self.kinds = np.asarray(kinds, dtype=np.int32)
+        self.maps = np.asarray(slots, dtype=np.int32)
+        self.eps = np.asarray(eps, dtype=np.complex128)
+        self.depth = np.zeros(len(kinds), dtype=np.float64)  # per-problem depths are passed instead
+        self.nmaps = 0 if conv is None else int(conv.shape[0])
+        self.conv, self.hx, self.hy = conv, hx, hy
+
+
+def _shape_key(layers, stack):
+    """Layer kinds, uniform eps and which patterned layers share a pixmap (first-use slots)."""
+    kinds, slots, eps, digests = [], [], [], []
+    for name in stack:
+        kind, e, _ = layers[name]
+        if kind == "pixmap":
+            d = engine._digest(e)
+            if d not in digests:
+                digests.append(d)
+            kinds.append(1)
+            slots.append(digests.index(d))
+            eps.append(0j)
+        else:
+            kinds.append(0)
+            slots.append(0)
+            eps.append(complex(e))
+    return (tuple(kinds), tuple(slots), tuple(eps)), digests
+
+
+def prepare_maps(struct, eps_maps):
+    """C, C^-1, Hx, Hy of a stack of pixmaps [M, nx, ny] in two batched launches (khp_convmat,
+    khp_structure_prep).  Raises KhpError when a convolution matrix is singular."""
+    lib = _capi.load()
+    sp = _capi.stream_ptr()
+    eps = torch.as_tensor(np.asarray(eps_maps), device=struct.device).to(torch.complex128).contiguous()
+    M, nx, ny = eps.shape
+    px, py = struct.pw
+    nh = struct.nh
+    conv = torch.empty((M, nh, nh), dtype=torch.complex128, device=struct.device)
+    ws = engine.workspace(lib.khp_convmat_workspace(M, px, py), struct.device)
+    _capi.check(lib.khp_convmat(M, nx, ny, _capi.ptr(eps), px, py, _capi.ptr(conv), _capi.ptr(ws), ws.numel(), sp),
+                "khp_convmat")
+    ic, hx, hy = torch.empty_like(conv), torch.empty_like(conv), torch.empty_like(conv)
+    st = torch.zeros(M, dtype=torch.int32, device=struct.device)
+    ws = engine.workspace(lib.khp_structure_prep_workspace(M, nh), struct.device)
+    _capi.check(lib.khp_structure_prep(M, nh, _capi.ptr(conv), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
+                                       _capi.ptr(ic), _capi.ptr(hx), _capi.ptr(hy), _capi.ptr(st), _capi.ptr(ws),
+                                       ws.numel(), sp), "khp_structure_prep")
+    if bool(st.any()):
+        bad = int(torch.nonzero(st).flatten()[0])
+        raise _capi.KhpError(f"convolution matrix of pixmap {bad}: {_capi.decode_status(int(st[bad]))}")
+    return conv, ic, hx, hy
+
+
+def convmat_bwd(struct, dconv, nx, ny):
+    """Gradient with respect to pixmaps [M, nx, ny] from the convolution-matrix gradient
+    [M, nh, nh] (khp_convmat_bwd; both in the convention dL = Re sum(d o delta))."""
+    lib = _capi.load()
+    M = int(dconv.shape[0])
+    px, py = struct.pw
+    deps = torch.empty((M, nx, ny), dtype=torch.complex128, device=dconv.device)
+    ws = engine.workspace(lib.khp_convmat_bwd_workspace(M, ny, px, py), dconv.device)
+    _capi.check(lib.khp_convmat_bwd(M, nx, ny, _capi.ptr(dconv.contiguous()), px, py, _capi.ptr(deps), _capi.ptr(ws),
+                                    ws.numel(), _capi.stream_ptr()), "khp_convmat_bwd")
+    return deps
+
+
+def _group_chunks(structures, which, chunk, lattice, device):
+    """Yield (struct, idx, plan, pmap, pdepth, maps) for every chunk of every shape group:
+    ``maps`` lists the (structure, slot) of each prepared map, ``plan`` carries C, C^-1, Hx, Hy."""
+    keys, digests = [], []
+    for pw, layers, stack in structures:
+        k, d = _shape_key(layers, stack)
+        keys.append((tuple(pw),) + k)
+        digests.append(d)
+    lat = engine.lattice_vectors(lattice)
+    groups = {}
+    for p in range(len(which)):
+        groups.setdefault(keys[which[p]], []).append(p)
+    for key, members in groups.items():
+        pw, kinds, slots, eps = key[0], key[1], key[2], key[3]
+        struct = engine.StructureGPU(pw, lat, device)
+        members = np.asarray(members)
+        L = len(kinds)
+        for s in range(0, len(members), chunk):
+            idx = members[s:s + chunk]
+            B = len(idx)
+            mpos, eps_maps = {}, []
+            for sid in dict.fromkeys(which[idx].tolist()):
+                _, layers, stack = structures[sid]
+                for name in stack:
+                    kind, e, _ = layers[name]
+                    if kind != "pixmap":
+                        continue
+                    slot = digests[sid].index(engine._digest(e))
+                    if (sid, slot) not in mpos:
+                        mpos[(sid, slot)] = len(eps_maps)
+                        eps_maps.append(np.asarray(e))
+            conv = ic = hx = hy = None
+            if eps_maps:
+                conv, ic, hx, hy = prepare_maps(struct, np.stack(eps_maps))
+            pm = np.zeros((L, B), dtype=np.int32)
+            pd = np.zeros((L, B), dtype=np.float64)
+            for j, p in enumerate(idx):
+                sid = which[p]
+                _, layers, stack = structures[sid]
+                for l, name in enumerate(stack):
+                    pd[l, j] = layers[name][2]
+                    if kinds[l] == 1:
+                        pm[l, j] = mpos[(sid, slots[l])]
+            plan = _ChunkPlan(kinds, slots, eps, conv, hx, hy)
+            plan.ic = ic
+            maps = sorted(mpos, key=mpos.get)
+            yield (struct, idx, plan, torch.tensor(pm, device=struct.device), torch.tensor(pd, device=struct.device),
+                   maps, eps_maps)
+
+
+def _prep_args(wavelengths, kp, which, te, tm):
+    wl = np.atleast_1d(np.asarray(wavelengths, dtype=float))
+    P = wl.shape[0]
+    kpa = np.asarray(kp, dtype=complex).reshape(P, 2)
+    which = np.arange(P) if which is None else np.asarray(which, dtype=np.int64).reshape(P)
+    te = np.broadcast_to(np.asarray(te, dtype=complex), (P,))
+    tm = np.broadcast_to(np.asarray(tm, dtype=complex), (P,))
+    return wl, P, kpa, which, te, tm
+
+
+def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, lattice="square", epsi=1.0,
+                     epse=1.0, chunk=256, both_pols=False, method="mixed", refine=2, strict=True, device="cuda"):
+    """R and T of problems spread over many structures, batched across structures.
+
+    structures: list of (pw, layers, stack) (``layers`` as in solve_rt); which: [P] structure of
+    each problem (default: problem i uses structure i).  Structures with the same harmonic set,
+    layer kinds, uniform media and pixmap-sharing pattern form one group; each chunk of a group is
+    one khp_solve_batched(_mixed) call with per-problem maps and depths (maps of the chunk
+    prepared in one batched launch).  method: "mixed" (default) or "gamma" (FP64).
+    Returns R, T ([P] or [P, 2] with ``both_pols``) and status [P].
+    """
+    _capi.require_cuda()
+    wl, P, kpa, which, te, tm = _prep_args(wavelengths, kp, which, te, tm)
+    prec = "mixed" if method == "mixed" else "fp64"
+    R = np.empty((P, 2) if both_pols else P)
+    T = np.empty((P, 2) if both_pols else P)
+    st_all = np.zeros(P, dtype=np.int32)
+    for struct, idx, plan, pmap, pdepth, _, _ in _group_chunks(structures, which, chunk, lattice, device):
+        B = len(idx)
+        prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], struct.device)
+        status = torch.zeros(B, dtype=torch.int32, device=struct.device)
+        if both_pols:
+            tt, tmm = both_pol_weights(B, struct.device)
+            r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, tt, tmm, prec, refine, pmap, pdepth)
+        else:
+            r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine, pmap=pmap,
+                                     pdepth=pdepth)
+        R[idx] = r.cpu().numpy()
+        T[idx] = t.cpu().numpy()
+        st_all[idx] = status.cpu().numpy()
+    if strict and st_all.any():
+        bad = int(np.flatnonzero(st_all)[0])
+        raise _capi.KhpError(f"problem {bad}: {_capi.decode_status(int(st_all[bad]))}")
+    return R, T, st_all
+
+
+def solve_structures_grad(structures, wavelengths, kp, which=None, dR=None, dT=None, te=1.0, tm=0.0,
+                          lattice="square", epsi=1.0, epse=1.0, chunk=256, refine=2, strict=True, device="cuda"):
+    """Solve + gradient over many structures (khp_solve_batched_mixed_grad + khp_convmat_bwd).
+
+    dR, dT: [P, nh] weights of the per-order reflected / transmitted powers in the loss
+    L = sum dR * R_orders + dT * T_orders (None = 0); every structure in a call has the same
+    harmonic count.  Returns R [P], T [P], R_orders [P, nh], T_orders [P, nh], grads, status:
+    grads[s][name] = dL/d(eps map) of structure s's pixmap layer ``name`` as a complex [nx, ny]
+    array in the convention dL = Re sum(grad * d eps) (for a real map, dL/deps = grad.real);
+    layers sharing one pixmap get the total gradient with respect to that pixmap.
+    """
+    _capi.require_cuda()
+    wl, P, kpa, which, te, tm = _prep_args(wavelengths, kp, which, te, tm)
+    lib = _capi.load()
+    R = np.empty(P)
+    T = np.empty(P)
+    Ro = To = None
+    st_all = np.zeros(P, dtype=np.int32)
+    grads = [dict() for _ in structures]
+    for struct, idx, plan, pmap, pdepth, maps, eps_maps in _group_chunks(structures, which, chunk, lattice, device):
+        B, nh = len(idx), struct.nh
+        if Ro is None:
+            Ro, To = np.empty((P, nh)), np.empty((P, nh))
+        dev = struct.device
+        prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], dev)
+        status = torch.zeros(B, dtype=torch.int32, device=dev)
+        te_d, tm_d = prob.te.reshape(B, 1).contiguous(), prob.tm.reshape(B, 1).contiguous()
+        wr = None if dR is None else torch.tensor(np.asarray(dR, dtype=float)[idx].reshape(B, 1, nh), device=dev)
+        wt = None if dT is None else torch.tensor(np.asarray(dT, dtype=float)[idx].reshape(B, 1, nh), device=dev)
+        r = torch.empty((B, 1), dtype=torch.float64, device=dev)
+        t = torch.empty((B, 1), dtype=torch.float64, device=dev)
+        ro = torch.empty((B, 1, nh), dtype=torch.float64, device=dev)
+        to = torch.empty((B, 1, nh), dtype=torch.float64, device=dev)
+        L = len(plan.kinds)
+        dconv = torch.empty((plan.nmaps, nh, nh), dtype=torch.complex128, device=dev)
+        ws = engine.workspace(lib.khp_solve_batched_mixed_grad_workspace(B, nh, L, _host(plan.kinds),
+                                                                         _host(plan.maps), plan.nmaps), dev)
+        ei, ee = complex(epsi), complex(epse)
+        with engine._stage("khp_solve_batched_mixed_grad"):
+            code = lib.khp_solve_batched_mixed_grad(
+                B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
+                _host(plan.depth), _capi.ptr(pmap), _capi.ptr(pdepth), plan.nmaps, _capi.ptr(plan.conv),
+                _capi.ptr(plan.ic), _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
+                ei.real, ei.imag, ee.real, ee.imag, _capi.ptr(prob.kp), _capi.ptr(prob.k0), 1, _capi.ptr(te_d),
+                _capi.ptr(tm_d), int(refine), _capi.ptr(wr), _capi.ptr(wt), _capi.ptr(r), _capi.ptr(t), _capi.ptr(ro),
+                _capi.ptr(to), _capi.ptr(dconv), _capi.ptr(status), _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+        _capi.check(code, "khp_solve_batched_mixed_grad")
+        R[idx] = r[:, 0].cpu().numpy()
+        T[idx] = t[:, 0].cpu().numpy()
+        Ro[idx] = ro[:, 0].cpu().numpy()
+        To[idx] = to[:, 0].cpu().numpy()
+        st_all[idx] = status.cpu().numpy()
+        if maps:
+            shapes = {np.asarray(e).shape for e in eps_maps}
+            for shp in shapes:
+                sel = [k for k, e in enumerate(eps_maps) if np.asarray(e).shape == shp]
+                deps = convmat_bwd(struct, dconv[sel], shp[0], shp[1]).cpu().numpy()
+                for k, d in zip(sel, deps):
+                    sid, slot = maps[k]
+                    _, layers, stack = structures[sid]
+                    for l, name in enumerate(stack):
+                        if plan.kinds[l] == 1 and plan.maps[l] == slot:
+                            grads[sid][name] = grads[sid].get(name, 0) + d
+    if strict and st_all.any():
+        bad = int(np.flatnonzero(st_all)[0])
+        raise _capi.KhpError(f"problem {bad}: {_capi.decode_status(int(st_all[bad]))}")
+    return R, T, Ro, To, grads, st_all

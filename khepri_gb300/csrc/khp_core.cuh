@@ -49,6 +49,8 @@ enum StatusBit : int {
   KHP_BIT_SINGULAR = 1,
   KHP_BIT_NOT_CONVERGED = 2,
   KHP_BIT_NONFINITE = 4,
+  KHP_BIT_REFINE = 8,      // mixed-precision iterative refinement did not converge: re-solve in FP64
+  KHP_BIT_BAD_INPUT = 16,  // a per-problem input outside its range (e.g. a map index)
 };
 
 // ---- complex scalar with the memory layout of numpy/torch complex64 / complex128 ----------

@@ -72,13 +72,14 @@ template <typename T, int BM, int BN, int BK>
 __global__ void __launch_bounds__(256) k_gemm(int n, int m, int k, cplx<T> alpha, const cplx<T>* __restrict__ A,
                                               int64_t lda, int64_t bsA, const cplx<T>* __restrict__ B, int64_t ldb,
                                               int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
-                                              int64_t boff, const int* __restrict__ aidx) {
+                                              int64_t boff, const int* __restrict__ aidx,
+                                              const int* __restrict__ bidx) {
   constexpr int TM = BM / 16, TN = BN / 16;
   __shared__ cplx<T> As[BK][BM];
   __shared__ cplx<T> Bs[BK][BN];
   const int64_t b = blockIdx.z + boff;
   A += (aidx ? (int64_t)aidx[b] : b) * bsA;
-  B += b * bsB;
+  B += (bidx ? (int64_t)bidx[b] : b) * bsB;
   C += b * bsC;
   const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -311,14 +312,14 @@ int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bs
 template <typename T>
 int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda, int64_t bsA,
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
-                cudaStream_t s, const int* aidx) {
+                cudaStream_t s, const int* aidx, const int* bidx) {
   if (batch <= 0 || n <= 0 || m <= 0) return KHP_OK;
   constexpr int BM = 32, BN = 32, BK = 16;
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     dim3 grid((m + BN - 1) / BN, (n + BM - 1) / BM, nb);
     k_gemm<T, BM, BN, BK><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
-                                                aidx);
+                                                aidx, bidx);
     count_launches(1);
   }
   return cuda_status();
@@ -485,7 +486,8 @@ int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_
   template int launch_getrs<T>(int64_t, int, const cplx<T>*, int64_t, int64_t, const int*, cplx<T>*, int64_t,   \
                                int64_t, int, cudaStream_t);                                                     \
   template int launch_gemm<T>(int64_t, int, int, int, cplx<T>, const cplx<T>*, int64_t, int64_t, const cplx<T>*, \
-                              int64_t, int64_t, cplx<T>, cplx<T>*, int64_t, int64_t, cudaStream_t, const int*); \
+                              int64_t, int64_t, cplx<T>, cplx<T>*, int64_t, int64_t, cudaStream_t, const int*, \
+                              const int*);                                                                      \
   template int launch_geev<T>(int64_t, int, cplx<T>*, int64_t, int64_t, cplx<T>*, cplx<T>*, int64_t, int64_t,  \
                               cplx<T>*, int64_t, int*, cudaStream_t);                                           \
   template int launch_copy<T>(int64_t, int, int, const cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t,  \

@@ -55,8 +55,9 @@ struct GammaPlan {
   // per distinct map
   std::vector<cplx<T>*> W, V, lam, Wi, Q0, Vt;
   // modes scratch (reused per map)
-  cplx<T> *M, *Z, *CW, *Ct, *lu;
+  cplx<T> *M, *Z, *CW, *lu;
   int* piv;
+  std::vector<int*> midx;  // per distinct map: the map index of every problem
   // per layer
   std::vector<cplx<T>*> lu1, lu2;
   std::vector<int*> piv1, piv2;
@@ -78,11 +79,11 @@ GammaPlan<T> plan_gamma(Arena& a, int64_t batch, int nh, int nlayers, const int*
     p.Wi.push_back(a.take<cplx<T>>(batch * nn));
     p.Q0.push_back(a.take<cplx<T>>(batch * nn));
     p.Vt.push_back(a.take<cplx<T>>(batch * nn));
+    p.midx.push_back(a.take<int>(batch));
   }
   p.M = a.take<cplx<T>>(batch * nn);
   p.Z = a.take<cplx<T>>(batch * nn);
   p.CW = a.take<cplx<T>>(batch * nn);
-  p.Ct = a.take<cplx<T>>((size_t)nh * nh);
   p.lu = a.take<cplx<T>>(batch * nn);
   p.piv = a.take<int>(batch * n);
   for (int l = 0; l < nlayers; ++l) {
@@ -136,14 +137,15 @@ int launch_getrs_right(int64_t batch, int n, const cplx<T>* A, int64_t lda, int6
 
 template <typename T>
 int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, const int* maps, const double* eps,
-                const double* depths, const double* conv, const double* hx, const double* hy, const double* gx,
-                const double* gy, cd epsi, cd epse, const double* kp, const double* k0, int npol,
-                const double* te, const double* tm, double* R, double* Tt, int* status, void* workspace,
-                size_t ws_bytes, cudaStream_t s) {
+                const double* depths, const int* pmap, const double* pdepth, int64_t nmaps, const double* conv,
+                const double* hx, const double* hy, const double* gx, const double* gy, cd epsi, cd epse,
+                const double* kp, const double* k0, int npol, const double* te, const double* tm, double* R,
+                double* Tt, int* status, void* workspace, size_t ws_bytes, cudaStream_t s) {
+  static_assert(sizeof(T) == sizeof(double), "the FP64 recursion reads the caller's FP64 maps directly");
   const int nh = px * py, n = 2 * nh;
   const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh, hn = (int64_t)nh * n;
   // distinct maps in use, in order of first appearance
-  std::vector<int> used;
+  std::vector<int> used, first;
   std::vector<int> slot(nlayers, -1);
   for (int l = 0; l < nlayers; ++l) {
     if (kinds[l] != 1) continue;
@@ -153,9 +155,11 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     if (sidx < 0) {
       sidx = (int)used.size();
       used.push_back(maps[l]);
+      first.push_back(l);
     }
     slot[l] = sidx;
   }
+  auto depth_of = [&](int l) { return DepthSel{pdepth ? pdepth + (int64_t)l * batch : nullptr, depths[l]}; };
   Arena a{static_cast<char*>(workspace), ws_bytes};
   GammaPlan<T> p = plan_gamma<T>(a, batch, nh, nlayers, kinds, (int)used.size());
   if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
@@ -163,17 +167,17 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
 
   // ---- modes of every distinct pixmap, and W^-1, V^-1 V0, V0^-1 V ----
   for (size_t m = 0; m < used.size(); ++m) {
-    const cd* C = reinterpret_cast<const cd*>(conv) + used[m] * hh;
-    const cd* HX = reinterpret_cast<const cd*>(hx) + used[m] * hh;
-    const cd* HY = reinterpret_cast<const cd*>(hy) + used[m] * hh;
-    GT_EW(k_assemble_pq_t<T>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M);
+    const cd* Cm = reinterpret_cast<const cd*>(conv);
+    GT_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps, p.midx[m],
+          status);
+    GT_EW(k_assemble_pq_t<T>, batch * nn, batch, nh, Cm, reinterpret_cast<const cd*>(hx),
+          reinterpret_cast<const cd*>(hy), p.midx[m], gx, gy, kp, k0, p.M);
     GT_TRY(launch_geev<T>(batch, n, p.M, n, nn, p.Z, p.W[m], n, nn, p.lam[m], n, status, s));
     GT_EW(k_sqrt_lam_t<T>, batch * n, batch * n, p.lam[m]);
-    GT_EW(k_convert<T>, hh, hh, C, p.Ct);
     cplx<T>* CWt = p.CW;
     cplx<T>* CWb = p.CW + batch * hn;
-    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, p.Ct, nh, 0, p.W[m], n, nn, zero, CWt, n, hn, s));
-    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, p.Ct, nh, 0, p.W[m] + hn, n, nn, zero, CWb, n, hn, s));
+    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m], n, nn, zero, CWt, n, hn, s, p.midx[m]));
+    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m] + hn, n, nn, zero, CWb, n, hn, s, p.midx[m]));
     GT_EW(k_modes_v_t<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, p.lam[m], p.V[m], status);
     GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.lu, n, nn, s));
     GT_TRY(launch_inverse<T>(batch, n, p.lu, n, nn, p.Wi[m], n, nn, p.piv, status, s));
@@ -183,11 +187,11 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     GT_EW(k_v0inv_left<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.V[m], p.Vt[m]);
   }
   // ---- homogeneous media blocks ----
-  GT_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, 0.0, gx, gy, kp, k0, p.inc, status);
-  GT_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, 0.0, gx, gy, kp, k0, p.trn, status);
+  GT_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
+  GT_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.trn, status);
   for (int l = 0; l < nlayers; ++l)
     if (kinds[l] != 1)
-      GT_EW(k_homog_blocks, batch * nh, batch, nh, 0, mk(eps[2 * l], eps[2 * l + 1]), depths[l], gx, gy, kp, k0,
+      GT_EW(k_homog_blocks, batch * nh, batch, nh, 0, mk(eps[2 * l], eps[2 * l + 1]), depth_of(l), gx, gy, kp, k0,
             p.blocks[l], status);
   // ---- backward pass ----
   GT_EW(k_gamma_from_blocks<T>, batch * nn, batch, nh, p.trn, 0, p.G);
@@ -208,7 +212,7 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
       GT_EW(k_diff_sum<T>, batch * nn, batch * nn, p.F, p.Gb, p.lu1[l]);  // lu1 = F - G, F <- F + G
       GT_TRY(launch_getrf<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
       GT_TRY(launch_getrs_right<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], p.F, n, nn, n, s));  // rho
-      GT_EW(k_xmx_t<T>, batch * nn, batch, n, p.lam[m], depths[l], k0, p.F);                    // rho_L
+      GT_EW(k_xmx_t<T>, batch * nn, batch, n, p.lam[m], depth_of(l), k0, p.F);                  // rho_L
       GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.Gb, n, nn, s));
       GT_TRY(launch_gemm<T>(batch, n, n, n, one, p.W[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));    // P1
       GT_TRY(launch_copy<T>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));
@@ -235,7 +239,7 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     } else {
       const int m = slot[l];
       GT_TRY(launch_getrs<T>(batch, n, p.lu2[l], n, nn, p.piv2[l], p.u, 2, 2 * n, 2, s));
-      GT_EW(k_vec_x4<T>, batch * n * 2, batch, n, p.lam[m], depths[l], k0, p.u);
+      GT_EW(k_vec_x4<T>, batch * n * 2, batch, n, p.lam[m], depth_of(l), k0, p.u);
       GT_TRY(launch_getrs<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], p.u, 2, 2 * n, 2, s));
     }
   }
@@ -270,7 +274,8 @@ size_t khp_solve_batched_workspace(int64_t batch, int32_t nh, int32_t nlayers, c
 }
 
 int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
-                      const int32_t* layer_map, const double* layer_eps, const double* layer_depth, int64_t nmaps,
+                      const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                      const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
                       const double* conv, const double* hx, const double* hy, const double* gx, const double* gy,
                       double epsi_re, double epsi_im, double epse_re, double epse_im, const double* kp,
                       const double* k0, int32_t npol, const double* te, const double* tm, double* R, double* T,
@@ -285,9 +290,10 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
       return KHP_ERR_INVALID_ARG;
   }
   if (batch == 0) return KHP_OK;
-  return solve_gamma<double>(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, conv, hx, hy, gx,
-                             gy, mk(epsi_re, epsi_im), mk(epse_re, epse_im), kp, k0, npol, te, tm, R, T, status,
-                             workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+  return solve_gamma<double>(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, problem_map,
+                             problem_depth, nmaps, conv, hx, hy, gx, gy, mk(epsi_re, epsi_im), mk(epse_re, epse_im),
+                             kp, k0, npol, te, tm, R, T, status, workspace, ws_bytes,
+                             reinterpret_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

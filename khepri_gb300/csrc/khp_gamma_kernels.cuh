@@ -18,6 +18,26 @@ namespace {
 using cd = cplx<double>;
 using phys::M2;
 
+// Per-problem depth of a layer: p[b] when the caller gave per-problem depths, else `fixed`.
+struct DepthSel {
+  const double* p;
+  double fixed;
+  __device__ __forceinline__ double at(int64_t b) const { return p ? p[b] : fixed; }
+};
+
+// Map index of every problem for one map slot: pm[b] from the caller's per-problem map table
+// (column of the slot's first layer) or `fixed`; an index outside [0, nmaps) is replaced by 0
+// and flags the problem (KHP_BIT_BAD_INPUT), so that no later kernel reads outside the maps.
+__global__ void k_select_maps(int64_t batch, const int* __restrict__ pm, int fixed, int64_t nmaps, int* out,
+                              int* status) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+    const int m = pm ? pm[b] : fixed;
+    const bool ok = m >= 0 && m < nmaps;
+    out[b] = ok ? m : 0;
+    if (!ok) atomicOr(status + b, KHP_BIT_BAD_INPUT);
+  }
+}
+
 inline int grid_for(int64_t total) { return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 32)); }
 
 template <typename T>
@@ -42,11 +62,12 @@ __global__ void k_convert(int64_t count, const cd* __restrict__ in, cplx<T>* out
     out[e] = to_t<T>(in[e]);
 }
 
-// M = P Q of one pixmap for every problem (same identity as khp_layer_modes).
+// M = P Q of one pixmap for every problem (same identity as khp_layer_modes); problem b uses
+// map midx[b] of the [nmaps][nh][nh] arrays C, Hx, Hy.
 template <typename T>
-__global__ void k_assemble_pq_t(int64_t batch, int nh, const cd* __restrict__ C, const cd* __restrict__ Hx,
-                                const cd* __restrict__ Hy, const double* gx, const double* gy, const double* kp,
-                                const double* k0, cplx<T>* M) {
+__global__ void k_assemble_pq_t(int64_t batch, int nh, const cd* __restrict__ Cm, const cd* __restrict__ Hxm,
+                                const cd* __restrict__ Hym, const int* __restrict__ midx, const double* gx,
+                                const double* gy, const double* kp, const double* k0, cplx<T>* M) {
   const int n = 2 * nh;
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
@@ -56,6 +77,10 @@ __global__ void k_assemble_pq_t(int64_t batch, int nh, const cd* __restrict__ C,
     const int i = r % nh, j = c % nh;
     const int bi = r / nh, bj = c / nh;
     const int64_t mo = (int64_t)i * nh + j;
+    const int64_t moff = (int64_t)midx[b] * nh * nh;
+    const cd* C = Cm + moff;
+    const cd* Hx = Hxm + moff;
+    const cd* Hy = Hym + moff;
     const double k = k0[b];
     const cd ax = mk(kp[4 * b + 0] / k, kp[4 * b + 1] / k), ay = mk(kp[4 * b + 2] / k, kp[4 * b + 3] / k);
     cd kxi, kyi;
@@ -142,7 +167,7 @@ __global__ void k_v0inv_left(int64_t batch, int nh, const double* gx, const doub
 }
 
 // Homogeneous media: per problem and harmonic the four 2x2 blocks of S (double), [batch][nh][4].
-__global__ void k_homog_blocks(int64_t batch, int nh, int kind, cd eps, double depth, const double* gx, const double* gy,
+__global__ void k_homog_blocks(int64_t batch, int nh, int kind, cd eps, DepthSel depth, const double* gx, const double* gy,
                                const double* kp, const double* k0, M2* out, int* status) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nh; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nh;
@@ -151,7 +176,7 @@ __global__ void k_homog_blocks(int64_t batch, int nh, int kind, cd eps, double d
     phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
     M2 s[4], vm;
     cd lm;
-    phys::homogeneous_blocks(kind, kx, ky, eps, depth * k0[b], s, vm, lm);
+    phys::homogeneous_blocks(kind, kx, ky, eps, depth.at(b) * k0[b], s, vm, lm);
     bool fin = true;
     for (int q = 0; q < 4; ++q) {
       out[e * 4 + q] = s[q];
@@ -226,14 +251,15 @@ __global__ void k_diff_sum(int64_t count, cplx<T>* f, const cplx<T>* __restrict_
   }
 }
 
-// rho <- X rho X, X = exp(-lam k0 d) (one depth for the batch).
+// rho <- X rho X, X = exp(-lam k0 d).
 template <typename T>
-__global__ void k_xmx_t(int64_t batch, int n, const cplx<T>* __restrict__ lam, double depth, const double* k0, cplx<T>* M) {
+__global__ void k_xmx_t(int64_t batch, int n, const cplx<T>* __restrict__ lam, DepthSel depth, const double* k0,
+                        cplx<T>* M) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int rc = (int)(e % nn);
-    const double dk = depth * k0[b];
+    const double dk = depth.at(b) * k0[b];
     const cd xi = cexp(-(to_d(lam[b * n + rc / n]) * dk)), xj = cexp(-(to_d(lam[b * n + rc % n]) * dk));
     M[e] = to_t<T>(xi * to_d(M[e]) * xj);
   }
@@ -273,11 +299,12 @@ __global__ void k_block_apply(int64_t batch, int nh, const M2* __restrict__ S, i
 
 // u <- 4 X u (patterned layer, forward pass).
 template <typename T>
-__global__ void k_vec_x4(int64_t batch, int n, const cplx<T>* __restrict__ lam, double depth, const double* k0, cplx<T>* u) {
+__global__ void k_vec_x4(int64_t batch, int n, const cplx<T>* __restrict__ lam, DepthSel depth, const double* k0,
+                         cplx<T>* u) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n * 2; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / (2 * n);
     const int r = (int)((e / 2) % n);
-    const cd x = cexp(-(to_d(lam[b * n + r]) * (depth * k0[b])));
+    const cd x = cexp(-(to_d(lam[b * n + r]) * (depth.at(b) * k0[b])));
     u[e] = to_t<T>((4.0 * x) * to_d(u[e]));
   }
 }

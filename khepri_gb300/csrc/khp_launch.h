@@ -19,11 +19,11 @@ int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bs
                  int64_t ldb, int64_t bsB, int m, cudaStream_t s);
 
 // C = alpha A B + beta C (A n x k, B k x m).  A batch stride of 0 broadcasts one matrix;
-// aidx (optional, device int[batch]) picks A[aidx[b]] for problem b.
+// aidx / bidx (optional, device int[batch]) pick A[aidx[b]] / B[bidx[b]] for problem b.
 template <typename T>
 int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda, int64_t bsA,
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
-                cudaStream_t s, const int* aidx = nullptr);
+                cudaStream_t s, const int* aidx = nullptr, const int* bidx = nullptr);
 
 // Eigen-decomposition A W = W diag(lam); A destroyed; Z: batch x n x n scratch (ld n).
 template <typename T>

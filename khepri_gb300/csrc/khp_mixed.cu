@@ -10,7 +10,8 @@
 //      order converges slowly there); other pairs closer than 1e-5 relative stay coupled
 //      (second-order error);  V = Q W / lam in FP64;
 //   2. the reflection-matrix recursion of khp_solve_batched on the FP32-rounded refined modes,
-//      keeping every factor it makes (LU factors, rho, Gamma at every gap, Gamma M^-1);
+//      keeping every factor it makes (the explicit inverses, rho, Gamma at every gap, Gamma M^-1),
+//      with every O(n^3) step a blocked LU / inverse or a tiled product;
 //   3. iterative refinement of the interface-continuity system of the whole stack (the
 //      equations the reference's S-matrix chain encodes, crystal.py:180-206 / layer.py:35-60),
 //      for the two source columns: residual in FP64 with the refined FP64 modes and the FP64
@@ -37,6 +38,8 @@ constexpr int kMaxLayers = 16;
 // Eigen-refinement steps.  From this FP32 solver's eigenvectors (relative residual ~1e-6 on the
 // 11x11 P.Q) three pair-aware steps reach ~1e-10 even for eigenvalue pairs 1e-4 apart.
 constexpr int kEigSteps = 3;
+// Refinement rounds beyond the requested ones, run only for problems not yet converged.
+constexpr int kExtraRounds = 12;
 
 // ------------------------------------------------------------------------------------------
 // Eigen-refinement kernels
@@ -149,10 +152,15 @@ __global__ void k_to_double(int64_t count, const cf* __restrict__ in, cd* out) {
     out[e] = mk((double)in[e].re, (double)in[e].im);
 }
 
-// lam64 = sqrt(mu64) (principal), lam32 = round(lam64)
+// lam64 = sqrt(mu64), lam32 = round(lam64).  Principal root (alternative.py:173), except that a
+// root within 1e-8 relative of the imaginary axis is taken with Im >= 0: mu on (or rounded
+// across) the negative real axis then gets one branch, so that degenerate propagating pairs
+// share it.  The sign of a mode's lam does not change the layer's scattering (the pair +-lam
+// spans the same fields), and the gradient's divided differences need the shared branch.
 __global__ void k_sqrt_mu(int64_t count, const cd* __restrict__ mu64, cd* lam64, cf* lam32) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
-    const cd l = csqrt(mu64[e]);
+    cd l = csqrt(mu64[e]);
+    if (fabs(l.re) <= 1e-8 * cabs(l) && l.im < 0.0) l = mk(-l.re, -l.im);
     lam64[e] = l;
     lam32[e] = mk((float)l.re, (float)l.im);
   }
@@ -169,13 +177,11 @@ __global__ void k_round(int64_t count, const cd* __restrict__ in, cf* out) {
 struct Elem {
   int kind;  // 0 homogeneous layer, 1 patterned layer
   int slot;  // map slot (patterned)
-  double depth;
+  DepthSel dep;
   const M2* blocks;  // homogeneous: [batch][nh][4] (FP64)
-  const cf* lu1;     // homogeneous: LU of M; patterned: LU of F - G
-  const int* piv1;
-  const cf* lu2;  // patterned: LU of P1 - P2
-  const int* piv2;
-  const cf* zr;  // homogeneous: Gamma M^-1;  patterned: rho
+  const cf* inv1;  // homogeneous: M^-1; patterned: (F - G)^-1
+  const cf* inv2;  // patterned: (P1 - P2)^-1
+  const cf* zr;    // homogeneous: Gamma M^-1;  patterned: rho
 };
 
 struct MapPtrs {
@@ -195,8 +201,7 @@ struct Table {
   int64_t batch;
   const M2* inc;
   const M2* trn;
-  const cf* lu0;   // LU of I - S22_inc Gamma_0
-  const int* piv0;
+  const cf* inv0;  // (I - S22_inc Gamma_0)^-1
   const cf* gam;   // Gamma at gaps 0..L: [L+1][batch][n][n]
   Elem e[kMaxLayers];
   MapPtrs m[kMaxLayers];
@@ -247,9 +252,10 @@ __device__ __forceinline__ cd xprop(const cd* lam64, int i, double dk) { return 
 __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* gx, const double* gy,
                                                         const double* kp, const double* k0v, const cd* __restrict__ X,
                                                         const cd* __restrict__ XA, const cd* __restrict__ RT,
-                                                        cd* RES, cd* scratch) {
+                                                        cd* RES, cd* scratch, const int* active) {
   TeamCta t;
   const int64_t b = blockIdx.x;
+  if (active && !active[b]) return;
   const int nh = tb.nh, n = 2 * nh, L = tb.L;
   const int64_t nn = (int64_t)n * n;
   const int64_t xs = (int64_t)(2 * (L + 1)) * 2 * n, xas = (int64_t)2 * L * 2 * n;
@@ -295,7 +301,7 @@ __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* 
     const cd* W = M.W64 + b * nn;
     const cd* V = M.V64 + b * nn;
     const cd* lam = M.lam64 + b * n;
-    const double dk = E.depth * k0;
+    const double dk = E.dep.at(b) * k0;
     const cd* ap = xa + (2 * pl) * 2 * n;
     const cd* am = xa + (2 * pl + 1) * 2 * n;
     // w1 = a+ + X a-, w2 = X a- - a+, w3 = X a+ + a-, w4 = a- - X a+
@@ -350,8 +356,11 @@ __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* 
 // Per problem workspace (FP32, [..][n][2]): s at every gap (L+1), per layer 5 vectors, 6 temps.
 __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx, const double* gy, const double* kp,
                                                      const double* k0v, const cd* __restrict__ RES, cd* X, cd* XA,
-                                                     cd* RT, cf* WS) {
+                                                     cd* RT, cf* WS, double* corr, const int* active) {
+  __shared__ TeamShared sh;
   TeamCta t;
+  if (active && !active[blockIdx.x]) return;
+  double cmax = 0.0;  // largest |correction| of r and t (this thread)
   const int64_t b = blockIdx.x;
   const int nh = tb.nh, n = 2 * nh, L = tb.L;
   const int64_t nn = (int64_t)n * n;
@@ -411,7 +420,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
     const MapPtrs& M = tb.m[E.slot];
     const cd* f3 = rsl(l + 1, 2);
     const cd* f4 = rsl(l + 1, 3);
-    const double dk = E.depth * k0;
+    const double dk = E.dep.at(b) * k0;
     // T0 = f3 - s ; T1 = f4 - V0 s
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
@@ -487,14 +496,20 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
       dcp[e] = mk((float)v.re, (float)v.im);
     }
     t.sync();
-    team_getrs(t, tb.lu0 + b * nn, n, n, tb.piv0 + b * n, dcp, 2, 2);
+    team_mv2(t, tb.inv0 + b * nn, n, dcp, T1);
+    t.sync();
+    for (int e = t.tid(); e < 2 * n; e += t.size()) dcp[e] = T1[e];
+    t.sync();
     team_mv2(t, gam(0), n, dcp, T0);
     t.sync();
     for (int e = t.tid(); e < 2 * n; e += t.size()) dcm[e] = T0[e] + s0[e];
     t.sync();
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
-      r[e] += blk_mv(S, 1, nh, i, c, dcm) + rA[e];
+      const cd d = blk_mv(S, 1, nh, i, c, dcm) + rA[e];
+      r[e] += d;
+      const double m = cabs(d);
+      cmax = m == m ? fmax(cmax, m) : INFINITY;
       x[e] += ld2(dcp, i, c);
       x[2 * n + e] += ld2(dcm, i, c);
     }
@@ -514,8 +529,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
         T0[e] = mk((float)v.re, (float)v.im);
       }
       t.sync();
-      team_getrs(t, E.lu1 + b * nn, n, n, E.piv1 + b * n, T0, 2, 2);
-      for (int e = t.tid(); e < 2 * n; e += t.size()) dcp[e] = T0[e];
+      team_mv2(t, E.inv1 + b * nn, n, T0, dcp);
       t.sync();
     } else {
       const MapPtrs& M = tb.m[E.slot];
@@ -523,13 +537,14 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
       const cf* h = LV(l, 1);
       const cf* k1 = LV(l, 2);
       const cf* k2 = LV(l, 3);
-      const double dk = E.depth * k0;
+      const double dk = E.dep.at(b) * k0;
       const cf* lam = M.lam32 + b * n;
       cd* ap = xa + (2 * pl) * 2 * n;
       cd* am = xa + (2 * pl + 1) * 2 * n;
-      for (int e = t.tid(); e < 2 * n; e += t.size()) T0[e] = mk(2.f, 0.f) * dcp[e] - k1[e] + k2[e];
+      for (int e = t.tid(); e < 2 * n; e += t.size()) T3[e] = mk(2.f, 0.f) * dcp[e] - k1[e] + k2[e];
       t.sync();
-      team_getrs(t, E.lu2 + b * nn, n, n, E.piv2 + b * n, T0, 2, 2);  // a+
+      team_mv2(t, E.inv2 + b * nn, n, T3, T0);  // a+
+      t.sync();
       for (int e = t.tid(); e < 2 * n; e += t.size()) {
         const cd xi = cexp(-(mk((double)lam[e / 2].re, (double)lam[e / 2].im) * dk));
         const cd xa_ = xi * ld2(T0, e / 2, e % 2);
@@ -538,13 +553,12 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
         T2[e] = mk((float)v.re, (float)v.im);
       }
       t.sync();
-      team_getrs(t, E.lu1 + b * nn, n, n, E.piv1 + b * n, T2, 2, 2);  // c+ right
-      team_mv2(t, E.zr + b * nn, n, T1, T3);                           // rho X a+
+      team_mv2(t, E.inv1 + b * nn, n, T2, dcp);  // c+ right
+      team_mv2(t, E.zr + b * nn, n, T1, T3);     // rho X a+
       t.sync();
       for (int e = t.tid(); e < 2 * n; e += t.size()) {
         ap[e] += ld2(T0, e / 2, e % 2);
         am[e] += ld2(T3, e / 2, e % 2) + ld2(h, e / 2, e % 2);
-        dcp[e] = T2[e];
       }
       t.sync();
       ++pl;
@@ -567,10 +581,120 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
     const cd* rB = rsl(L + 1, 1);
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
-      tt[e] += blk_mv(S, 2, nh, i, c, dcp) + rB[e];
+      const cd d = blk_mv(S, 2, nh, i, c, dcp) + rB[e];
+      tt[e] += d;
+      const double m = cabs(d);
+      cmax = m == m ? fmax(cmax, m) : INFINITY;
     }
   }
+  int where = 0;
+  team_argmax(t, cmax, where, &sh);
+  if (t.tid() == 0) corr[b] = cmax;
 }
+
+// Convergence of the iterative refinement from the last two correction sizes: with linear
+// convergence at rate c1 / c0 the remaining error is about c1^2 / (c0 - c1).  A problem stays
+// active (needs more rounds) while its estimate exceeds 1e-9, its corrections do not shrink,
+// or they are not finite; only problems already active are examined (null: all).
+__global__ void k_check_refine(int64_t batch, const double* __restrict__ c0, const double* __restrict__ c1,
+                               int* active) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+    if (!active[b]) continue;
+    const double a = c0[b], z = c1[b];
+    const bool ok = z == 0.0 || (z < a && z * z <= 1e-9 * (a - z));
+    active[b] = ok ? 0 : 1;
+  }
+}
+
+__global__ void k_flag_unconverged(int64_t batch, const int* __restrict__ active, int* status) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x)
+    if (active[b]) status[b] |= KHP_BIT_REFINE;
+}
+
+#include "khp_adjoint.cuh"
+
+// ------------------------------------------------------------------------------------------
+// Gradient stage: per-problem M-bar^T = W H^T W^-1, then the convolution-matrix gradient.
+// With N = M-bar^T (blocks N_ab, nh x nh), A1 = N21 Kx + N22 Ky, A2 = N11 Kx + N12 Ky
+// (column scalings, normalised k), the transposed gradient of C for one problem is
+//   A1 C^-1 Ky + A2 C^-1 Kx - N11 - N22 + QDT21 - QDT12 - C^-1 (Ky C A1 + Kx C A2) C^-1,
+// from M = P Q with P, Q of alternative.py:158-178 (the diagonal-only terms cancel); QDT is
+// the transposed direct term of Y = Q M^-1/2.  Sums over the problems that share a map are
+// taken before the two products with C^-1 on the outside.
+// ------------------------------------------------------------------------------------------
+__global__ void k_make_a12(int64_t batch, int nh, const cf* __restrict__ N, const double* gx, const double* gy,
+                           const double* kp, const double* k0, cf* A1, cf* A2) {
+  const int n = 2 * nh;
+  const int64_t hh = (int64_t)nh * nh, nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * hh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / hh;
+    const int ij = (int)(e % hh);
+    const int i = ij / nh, j = ij % nh;
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, j, kx, ky);
+    const cf* Nb = N + b * nn;
+    const cd n11 = to_d(Nb[(int64_t)i * n + j]), n12 = to_d(Nb[(int64_t)i * n + nh + j]);
+    const cd n21 = to_d(Nb[(int64_t)(nh + i) * n + j]), n22 = to_d(Nb[(int64_t)(nh + i) * n + nh + j]);
+    A1[e] = to_f(n21 * kx + n22 * ky);
+    A2[e] = to_f(n11 * kx + n12 * ky);
+  }
+}
+
+// E1 = G1 Ky + G2 Kx - N11 - N22 + QDT21 - QDT12 (column scalings), E2 = Ky G3 + Kx G4 (row
+// scalings), with G1 = A1 C^-1, G2 = A2 C^-1, G3 = C A1, G4 = C A2.
+__global__ void k_make_e12(int64_t batch, int nh, const cf* __restrict__ N, const cd* __restrict__ QDT,
+                           const cf* __restrict__ G1, const cf* __restrict__ G2, const cf* __restrict__ G3,
+                           const cf* __restrict__ G4, const double* gx, const double* gy, const double* kp,
+                           const double* k0, cd* E1, cd* E2) {
+  const int n = 2 * nh;
+  const int64_t hh = (int64_t)nh * nh, nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * hh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / hh;
+    const int ij = (int)(e % hh);
+    const int i = ij / nh, j = ij % nh;
+    cd kxj, kyj, kxi, kyi;
+    phys::kvec(kp, k0, gx, gy, b, j, kxj, kyj);
+    phys::kvec(kp, k0, gx, gy, b, i, kxi, kyi);
+    const cf* Nb = N + b * nn;
+    const cd* Qb = QDT + b * nn;
+    const cd n11 = to_d(Nb[(int64_t)i * n + j]), n22 = to_d(Nb[(int64_t)(nh + i) * n + nh + j]);
+    const cd q21 = Qb[(int64_t)(nh + i) * n + j], q12 = Qb[(int64_t)i * n + nh + j];
+    E1[e] = to_d(G1[e]) * kyj + to_d(G2[e]) * kxj - n11 - n22 + q21 - q12;
+    E2[e] = kyi * to_d(G3[e]) + kxi * to_d(G4[e]);
+  }
+}
+
+// S[m] += sum of E[b] over the problems b with midx[b] == m (fixed order: deterministic).
+__global__ void k_reduce_maps(int64_t batch, int64_t hh, int64_t nmaps, const int* __restrict__ midx,
+                              const cd* __restrict__ E, cd* S) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nmaps * hh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / hh, k = e % hh;
+    cd acc = mk(0.0);
+    for (int64_t b = 0; b < batch; ++b)
+      if (midx[b] == m) acc += E[b * hh + k];
+    S[e] += acc;
+  }
+}
+
+// dconv[m][r][c] = -2 CT[m][c][r]: the gradient in the convention dL = Re sum(dconv o dC).
+__global__ void k_dconv_out(int64_t nmaps, int nh, const cd* __restrict__ CT, cd* dconv) {
+  const int64_t hh = (int64_t)nh * nh;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nmaps * hh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / hh;
+    const int rc = (int)(e % hh);
+    const int r = rc / nh, c = rc % nh;
+    dconv[e] = CT[m * hh + (int64_t)c * nh + r] * -2.0;
+  }
+}
+
+struct GradArgs {
+  const double* ic;  // C^-1 of every map, complex [nmaps][nh][nh]
+  const double* wR;  // dL/dR per order, [batch][npol][nh] (null: 0)
+  const double* wT;  // dL/dT per order
+  double* Ro;        // per-order powers out, [batch][npol][nh] (null: not written)
+  double* To;
+  double* dconv;     // complex [nmaps][nh][nh] out
+};
 
 // ------------------------------------------------------------------------------------------
 struct Arena {
@@ -597,16 +721,17 @@ struct MixedPlan {
   cd *M64, *MW64, *CW64, *Ct64, *mu64, *mu64b;
   int *pair, *nearest;
   int* piv;
+  std::vector<int*> midx;  // per map slot: the map index of every problem
   // per layer
-  std::vector<cf*> lu1, lu2, zr;
-  std::vector<int*> piv1, piv2;
+  std::vector<cf*> inv1, inv2, zr;
   std::vector<M2*> blocks;
   M2 *inc, *trn;
-  cf *gam, *F, *Gb, *P, *lu0;
-  int* piv0;
+  cf *gam, *F, *Gb, *P, *inv0;
   // vectors
   cd *X, *XA, *RT, *RES, *scr;
   cf* SW;
+  double* corr;  // [2][batch]: correction sizes of the last two refinement rounds
+  int* active;   // [batch]: refinement not yet converged
 };
 
 MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, int nmaps_used) {
@@ -623,6 +748,7 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
     p.W64.push_back(a.take<cd>(batch * nn));
     p.V64.push_back(a.take<cd>(batch * nn));
     p.lam64.push_back(a.take<cd>(batch * n));
+    p.midx.push_back(a.take<int>(batch));
   }
   p.M32 = a.take<cf>(batch * nn);
   p.Z32 = a.take<cf>(batch * nn);
@@ -638,16 +764,13 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.nearest = a.take<int>(batch * n);
   p.piv = a.take<int>(batch * n);
   for (int l = 0; l < L; ++l) {
-    p.lu1.push_back(a.take<cf>(batch * nn));
-    p.piv1.push_back(a.take<int>(batch * n));
+    p.inv1.push_back(a.take<cf>(batch * nn));
     p.zr.push_back(a.take<cf>(batch * nn));
     if (kinds[l] == 1) {
-      p.lu2.push_back(a.take<cf>(batch * nn));
-      p.piv2.push_back(a.take<int>(batch * n));
+      p.inv2.push_back(a.take<cf>(batch * nn));
       p.blocks.push_back(nullptr);
     } else {
-      p.lu2.push_back(nullptr);
-      p.piv2.push_back(nullptr);
+      p.inv2.push_back(nullptr);
       p.blocks.push_back(a.take<M2>(batch * nh * 4));
     }
   }
@@ -657,15 +780,55 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.F = a.take<cf>(batch * nn);
   p.Gb = a.take<cf>(batch * nn);
   p.P = a.take<cf>(batch * nn);
-  p.lu0 = a.take<cf>(batch * nn);
-  p.piv0 = a.take<int>(batch * n);
+  p.inv0 = a.take<cf>(batch * nn);
   p.X = a.take<cd>(batch * (size_t)(2 * (L + 1)) * 2 * n);
   p.XA = a.take<cd>(batch * (size_t)(2 * std::max(L, 1)) * 2 * n);
   p.RT = a.take<cd>(batch * 4 * n);
   p.RES = a.take<cd>(batch * (size_t)(L + 2) * 4 * 2 * n);
   p.scr = a.take<cd>(batch * 4 * 2 * n);
   p.SW = a.take<cf>(batch * (size_t)(L + 1 + 5 * L + 6) * 2 * n);
+  p.corr = a.take<double>(2 * (size_t)batch);
+  p.active = a.take<int>(batch);
   return p;
+}
+
+struct GradPlan {
+  cd *Y, *RX, *RXA, *RRT, *GR, *GT, *scr4, *VEC, *HT, *QDT, *E1, *E2, *S1, *S2, *CT, *TMP;
+  cf *SWT, *H32, *T32, *N32, *A1, *A2, *G1, *G2, *G3, *G4, *C32, *IC32;
+};
+
+GradPlan plan_grad(Arena& a, int64_t batch, int nh, int L, int64_t nmaps) {
+  const size_t n = 2 * (size_t)nh, nn = n * n, hh = (size_t)nh * nh;
+  GradPlan g;
+  g.Y = a.take<cd>(batch * (size_t)(L + 2) * 4 * 2 * n);
+  g.RX = a.take<cd>(batch * (size_t)(2 * (L + 1)) * 2 * n);
+  g.RXA = a.take<cd>(batch * (size_t)(2 * std::max(L, 1)) * 2 * n);
+  g.RRT = a.take<cd>(batch * 4 * n);
+  g.GR = a.take<cd>(batch * 2 * n);
+  g.GT = a.take<cd>(batch * 2 * n);
+  g.scr4 = a.take<cd>(batch * 4 * 2 * n);
+  g.VEC = a.take<cd>(batch * 20 * n);
+  g.HT = a.take<cd>(batch * nn);
+  g.QDT = a.take<cd>(batch * nn);
+  g.E1 = a.take<cd>(batch * hh);
+  g.E2 = a.take<cd>(batch * hh);
+  g.S1 = a.take<cd>(nmaps * hh);
+  g.S2 = a.take<cd>(nmaps * hh);
+  g.CT = a.take<cd>(nmaps * hh);
+  g.TMP = a.take<cd>(nmaps * hh);
+  g.SWT = a.take<cf>(batch * (size_t)(L + 1 + 4 * L + 8) * 2 * n);
+  g.H32 = a.take<cf>(batch * nn);
+  g.T32 = a.take<cf>(batch * nn);
+  g.N32 = a.take<cf>(batch * nn);
+  g.A1 = a.take<cf>(batch * hh);
+  g.A2 = a.take<cf>(batch * hh);
+  g.G1 = a.take<cf>(batch * hh);
+  g.G2 = a.take<cf>(batch * hh);
+  g.G3 = a.take<cf>(batch * hh);
+  g.G4 = a.take<cf>(batch * hh);
+  g.C32 = a.take<cf>(nmaps * hh);
+  g.IC32 = a.take<cf>(nmaps * hh);
+  return g;
 }
 
 #define MX_TRY(x)        \
@@ -680,21 +843,92 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
     MX_TRY(cuda_status());                                               \
   } while (0)
 
-int launch_getrs_right_f(int64_t batch, int n, const cf* A, int64_t lda, int64_t bsA, const int* piv, cf* B,
-                         int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
-  k_getrs_right<float><<<(unsigned)batch, 256, 0, s>>>(n, A, lda, bsA, piv, B, ldb, bsB, m);
+// Backward stage of khp_solve_batched_mixed_grad (after the forward refinement): loss seeds,
+// the adjoint solve (FP64 transposed residual + FP32 transposed sweep, refine + 3 rounds), the
+// per-layer M-gradients and the convolution-matrix gradient of every map.
+template <class DepthOf>
+int grad_mixed(const Table& tb, MixedPlan& p, GradPlan& g, const GradArgs& ga, int64_t batch, int nh, int L,
+               const int* kinds, const std::vector<int>& slot, const std::vector<int>& used, DepthOf depth_of,
+               int64_t nmaps, const double* conv, const double* gx, const double* gy, const double* kp,
+               const double* k0, int npol, const double* te, const double* tm, cd epsi, cd epse, int refine, double* R,
+               double* Tt, cudaStream_t s) {
+  const int n = 2 * nh;
+  const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh;
+  const cf one = mk(1.f), zero = mk(0.f);
+  const cd done = mk(1.0), dzero = mk(0.0), dmone = mk(-1.0);
+  k_flux_grad<<<(unsigned)batch, 128, 0, s>>>(nh, npol, p.RT, p.RT + batch * 2 * n, gx, gy, kp, k0,
+                                              reinterpret_cast<const cd*>(te), reinterpret_cast<const cd*>(tm), epsi,
+                                              epse, ga.wR, ga.wT, R, Tt, ga.Ro, ga.To, g.GR, g.GT);
   count_launches(1);
+  MX_TRY(cuda_status());
+  // ---- adjoint: F^T y = g ----
+  if (cudaMemsetAsync(g.Y, 0, sizeof(cd) * batch * (size_t)(L + 2) * 4 * 2 * n, s) != cudaSuccess)
+    return KHP_ERR_CUDA;
+  for (int it = 0; it < refine + 3; ++it) {
+    k_stack_residual_T<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, g.Y, g.GR, g.GT, g.RX, g.RXA, g.RRT,
+                                                       g.scr4);
+    count_launches(1);
+    MX_TRY(cuda_status());
+    k_stack_sweep_T<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, g.RX, g.RXA, g.RRT, g.Y, g.SWT);
+    count_launches(1);
+    MX_TRY(cuda_status());
+  }
+  // ---- per map slot: H^T, QD^T over its layers, then N = W H^T W^-1 and the C-gradient ----
+  const cd* Cm = reinterpret_cast<const cd*>(conv);
+  const cd* ICm = reinterpret_cast<const cd*>(ga.ic);
+  MX_EW(k_round, nmaps * hh, nmaps * hh, Cm, g.C32);
+  MX_EW(k_round, nmaps * hh, nmaps * hh, ICm, g.IC32);
+  if (cudaMemsetAsync(g.S1, 0, sizeof(cd) * nmaps * hh, s) != cudaSuccess) return KHP_ERR_CUDA;
+  if (cudaMemsetAsync(g.S2, 0, sizeof(cd) * nmaps * hh, s) != cudaSuccess) return KHP_ERR_CUDA;
+  const int64_t ys_stride = (int64_t)(L + 2) * 4 * 2 * n;
+  const int64_t xas = (int64_t)2 * std::max(L, 1) * 2 * n;
+  for (size_t m = 0; m < used.size(); ++m) {
+    if (cudaMemsetAsync(g.HT, 0, sizeof(cd) * batch * nn, s) != cudaSuccess) return KHP_ERR_CUDA;
+    if (cudaMemsetAsync(g.QDT, 0, sizeof(cd) * batch * nn, s) != cudaSuccess) return KHP_ERR_CUDA;
+    int pl = 0;
+    for (int l = 0; l < L; ++l) {
+      if (kinds[l] != 1) continue;
+      if (slot[l] == (int)m) {
+        k_layer_vectors<<<(unsigned)batch, 256, 0, s>>>(tb, l, pl, k0, p.XA, g.Y, g.VEC);
+        count_launches(1);
+        MX_TRY(cuda_status());
+        MX_EW(k_layer_accum, batch * nn, batch, n, p.lam64[m], depth_of(l), k0, p.XA, xas, pl, g.Y, ys_stride,
+              (int64_t)(l + 1) * 4 * 2 * n, g.VEC, g.HT, g.QDT);
+      }
+      ++pl;
+    }
+    MX_EW(k_round, batch * nn, batch * nn, g.HT, g.H32);
+    MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, g.H32, n, nn, zero, g.T32, n, nn, s));
+    MX_TRY(launch_gemm<float>(batch, n, n, n, one, g.T32, n, nn, p.Wi[m], n, nn, zero, g.N32, n, nn, s));
+    MX_EW(k_make_a12, batch * hh, batch, nh, g.N32, gx, gy, kp, k0, g.A1, g.A2);
+    const int* mi = p.midx[m];
+    MX_TRY(launch_gemm<float>(batch, nh, nh, nh, one, g.A1, nh, hh, g.IC32, nh, hh, zero, g.G1, nh, hh, s, nullptr,
+                              mi));
+    MX_TRY(launch_gemm<float>(batch, nh, nh, nh, one, g.A2, nh, hh, g.IC32, nh, hh, zero, g.G2, nh, hh, s, nullptr,
+                              mi));
+    MX_TRY(launch_gemm<float>(batch, nh, nh, nh, one, g.C32, nh, hh, g.A1, nh, hh, zero, g.G3, nh, hh, s, mi));
+    MX_TRY(launch_gemm<float>(batch, nh, nh, nh, one, g.C32, nh, hh, g.A2, nh, hh, zero, g.G4, nh, hh, s, mi));
+    MX_EW(k_make_e12, batch * hh, batch, nh, g.N32, g.QDT, g.G1, g.G2, g.G3, g.G4, gx, gy, kp, k0, g.E1, g.E2);
+    MX_EW(k_reduce_maps, nmaps * hh, batch, hh, nmaps, mi, g.E1, g.S1);
+    MX_EW(k_reduce_maps, nmaps * hh, batch, hh, nmaps, mi, g.E2, g.S2);
+  }
+  // ---- per map: CT = S1 - C^-1 S2 C^-1, dconv = -2 CT^T ----
+  MX_TRY(launch_gemm<double>(nmaps, nh, nh, nh, done, g.S2, nh, hh, ICm, nh, hh, dzero, g.TMP, nh, hh, s));
+  MX_TRY(launch_copy<double>(nmaps, nh, nh, g.S1, nh, hh, g.CT, nh, hh, s));
+  MX_TRY(launch_gemm<double>(nmaps, nh, nh, nh, dmone, ICm, nh, hh, g.TMP, nh, hh, done, g.CT, nh, hh, s));
+  MX_EW(k_dconv_out, nmaps * hh, nmaps, nh, g.CT, reinterpret_cast<cd*>(ga.dconv));
   return cuda_status();
 }
 
 int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const int* maps, const double* eps,
-                const double* depths, const double* conv, const double* hx, const double* hy, const double* gx,
+                const double* depths, const int* pmap, const double* pdepth, int64_t nmaps, const double* conv,
+                const double* hx, const double* hy, const double* gx,
                 const double* gy, cd epsi, cd epse, const double* kp, const double* k0, int npol, const double* te,
                 const double* tm, int refine, double* R, double* Tt, int* status, void* workspace, size_t ws_bytes,
-                cudaStream_t s) {
+                cudaStream_t s, const GradArgs* grad = nullptr) {
   const int nh = px * py, n = 2 * nh;
   const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh, hn = (int64_t)nh * n;
-  std::vector<int> used, slot(L, -1);
+  std::vector<int> used, first, slot(L, -1);
   for (int l = 0; l < L; ++l) {
     if (kinds[l] != 1) continue;
     int sidx = -1;
@@ -703,39 +937,45 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     if (sidx < 0) {
       sidx = (int)used.size();
       used.push_back(maps[l]);
+      first.push_back(l);
     }
     slot[l] = sidx;
   }
+  auto depth_of = [&](int l) { return DepthSel{pdepth ? pdepth + (int64_t)l * batch : nullptr, depths[l]}; };
   Arena a{static_cast<char*>(workspace), ws_bytes};
   MixedPlan p = plan_mixed(a, batch, nh, L, kinds, (int)used.size());
+  GradPlan gp{};
+  if (grad) gp = plan_grad(a, batch, nh, L, nmaps);
   if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
   const cf one = mk(1.f), zero = mk(0.f), mone = mk(-1.f);
   const cd done = mk(1.0), dzero = mk(0.0);
 
   // ---- 1. modes: FP32 eigensolve + FP64 refinement ----
   for (size_t m = 0; m < used.size(); ++m) {
-    const cd* C = reinterpret_cast<const cd*>(conv) + used[m] * hh;
-    const cd* HX = reinterpret_cast<const cd*>(hx) + used[m] * hh;
-    const cd* HY = reinterpret_cast<const cd*>(hy) + used[m] * hh;
-    MX_EW(k_assemble_pq_t<float>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M32);
+    const cd* Cm = reinterpret_cast<const cd*>(conv);
+    const cd* HX = reinterpret_cast<const cd*>(hx);
+    const cd* HY = reinterpret_cast<const cd*>(hy);
+    MX_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps, p.midx[m],
+          status);
+    MX_EW(k_assemble_pq_t<float>, batch * nn, batch, nh, Cm, HX, HY, p.midx[m], gx, gy, kp, k0, p.M32);
     MX_TRY(launch_geev<float>(batch, n, p.M32, n, nn, p.Z32, p.W32[m], n, nn, p.lam32[m], n, status, s));
-    // Two refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 factors of the FP32 W),
-    // mu += diag(E), W += W F.
-    MX_EW(k_assemble_pq_t<double>, batch * nn, batch, nh, C, HX, HY, gx, gy, kp, k0, p.M64);
+    // Refinement steps: R = M W - W mu in FP64, E = W0^-1 R (FP32 inverse of the FP32 solver's
+    // W0, held in Wi until the final inverse), mu += diag(E), W += W F.
+    MX_EW(k_assemble_pq_t<double>, batch * nn, batch, nh, Cm, HX, HY, p.midx[m], gx, gy, kp, k0, p.M64);
     MX_EW(k_to_double, batch * nn, batch * nn, p.W32[m], p.W64[m]);
     MX_EW(k_to_double, batch * n, batch * n, p.lam32[m], p.mu64);
     MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_getrf<float>(batch, n, p.lu32, n, nn, p.piv, status, s));
+    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
     for (int step = 0; step < kEigSteps; ++step) {
       MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
       MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], mu_a, p.E32);
-      MX_TRY(launch_getrs<float>(batch, n, p.lu32, n, nn, p.piv, p.E32, n, nn, n, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
       k_find_pairs<<<(unsigned)batch, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
       count_launches(1);
       MX_TRY(cuda_status());
-      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.E32, p.M32, mu_b, p.pair);      // M32 <- F
+      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.Z32, p.M32, mu_b, p.pair);      // M32 <- F
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
       MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.Z32, p.W32[m]);
       std::swap(mu_a, mu_b);
@@ -744,36 +984,37 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
     cd* CWb = p.CW64 + batch * hn;
-    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, C, nh, 0, p.W64[m], n, nn, dzero, CWt, n, hn, s));
-    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, C, nh, 0, p.W64[m] + hn, n, nn, dzero, CWb, n, hn, s));
+    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, Cm, nh, hh, p.W64[m], n, nn, dzero, CWt, n, hn, s, p.midx[m]));
+    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, Cm, nh, hh, p.W64[m] + hn, n, nn, dzero, CWb, n, hn, s,
+                               p.midx[m]));
     MX_EW(k_modes_v_t<double>, batch * nn, batch, nh, gx, gy, kp, k0, p.W64[m], CWt, CWb, p.lam64[m], p.V64[m],
           status);
     MX_EW(k_round, batch * nn, batch * nn, p.V64[m], p.V32[m]);
     // FP32 inverses and V0 products
     MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_inverse<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
+    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
     MX_TRY(launch_copy<float>(batch, n, n, p.V32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_inverse<float>(batch, n, p.lu32, n, nn, p.Vi[m], n, nn, p.piv, status, s));
+    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Vi[m], n, nn, p.piv, status, s));
     MX_EW(k_v0_right<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.Vi[m], p.Q0[m]);
     MX_EW(k_v0inv_left<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.V32[m], p.Vt[m]);
   }
   // ---- homogeneous blocks (FP64) ----
-  MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, 0.0, gx, gy, kp, k0, p.inc, status);
-  MX_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, 0.0, gx, gy, kp, k0, p.trn, status);
+  MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
+  MX_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.trn, status);
   for (int l = 0; l < L; ++l)
     if (kinds[l] != 1)
-      MX_EW(k_homog_blocks, batch * nh, batch, nh, 0, mk(eps[2 * l], eps[2 * l + 1]), depths[l], gx, gy, kp, k0,
+      MX_EW(k_homog_blocks, batch * nh, batch, nh, 0, mk(eps[2 * l], eps[2 * l + 1]), depth_of(l), gx, gy, kp, k0,
             p.blocks[l], status);
-  // ---- 2. FP32 backward recursion, keeping every factor ----
+  // ---- 2. FP32 backward recursion, keeping every factor (explicit inverses: every O(n^3) step
+  //         is then a blocked factorisation or a tiled product) ----
   auto gam = [&](int g) { return p.gam + (int64_t)g * batch * nn; };
   MX_EW(k_gamma_from_blocks<float>, batch * nn, batch, nh, p.trn, 0, gam(L));
   for (int l = L - 1; l >= 0; --l) {
     cf* G = gam(l + 1);
     if (kinds[l] != 1) {
-      MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.blocks[l], G, p.lu1[l]);
-      MX_TRY(launch_getrf<float>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
-      MX_TRY(launch_copy<float>(batch, n, n, G, n, nn, p.zr[l], n, nn, s));
-      MX_TRY(launch_getrs_right_f(batch, n, p.lu1[l], n, nn, p.piv1[l], p.zr[l], n, nn, n, s));
+      MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.blocks[l], G, p.lu32);
+      MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, G, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));
       MX_EW(k_sandwich<float>, batch * nn, batch, nh, p.blocks[l], p.zr[l], gam(l));
     } else {
       const int m = slot[l];
@@ -781,23 +1022,22 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, G, n, nn, one, p.F, n, nn, s));
       MX_TRY(launch_copy<float>(batch, n, n, p.Q0[m], n, nn, p.Gb, n, nn, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Q0[m], n, nn, G, n, nn, mone, p.Gb, n, nn, s));
-      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.F, p.Gb, p.lu1[l]);
-      MX_TRY(launch_getrf<float>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
-      MX_TRY(launch_getrs_right_f(batch, n, p.lu1[l], n, nn, p.piv1[l], p.F, n, nn, n, s));  // rho
-      MX_TRY(launch_copy<float>(batch, n, n, p.F, n, nn, p.zr[l], n, nn, s));
-      MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.lam32[m], depths[l], k0, p.F);
+      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.F, p.Gb, p.lu32);
+      MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.F, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));  // rho
+      MX_TRY(launch_copy<float>(batch, n, n, p.zr[l], n, nn, p.F, n, nn, s));
+      MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.lam32[m], depth_of(l), k0, p.F);
       MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.Gb, n, nn, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));
       MX_TRY(launch_copy<float>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Vt[m], n, nn, p.F, n, nn, mone, p.P, n, nn, s));
-      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.Gb, p.P, p.lu2[l]);
-      MX_TRY(launch_getrf<float>(batch, n, p.lu2[l], n, nn, p.piv2[l], status, s));
-      MX_TRY(launch_getrs_right_f(batch, n, p.lu2[l], n, nn, p.piv2[l], p.Gb, n, nn, n, s));
-      MX_TRY(launch_copy<float>(batch, n, n, p.Gb, n, nn, gam(l), n, nn, s));
+      MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.Gb, p.P, p.lu32);
+      MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv2[l], n, nn, p.piv, status, s));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Gb, n, nn, p.inv2[l], n, nn, zero, gam(l), n, nn, s));
     }
   }
-  MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.inc, gam(0), p.lu0);
-  MX_TRY(launch_getrf<float>(batch, n, p.lu0, n, nn, p.piv0, status, s));
+  MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.inc, gam(0), p.lu32);
+  MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv0, n, nn, p.piv, status, s));
   // ---- 3. iterative refinement of the stack equations ----
   Table tb;
   tb.L = L;
@@ -805,19 +1045,16 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   tb.batch = batch;
   tb.inc = p.inc;
   tb.trn = p.trn;
-  tb.lu0 = p.lu0;
-  tb.piv0 = p.piv0;
+  tb.inv0 = p.inv0;
   tb.gam = p.gam;
   for (int l = 0; l < L; ++l) {
     Elem& E = tb.e[l];
     E.kind = kinds[l] == 1 ? 1 : 0;
     E.slot = slot[l];
-    E.depth = depths[l];
+    E.dep = depth_of(l);
     E.blocks = p.blocks[l];
-    E.lu1 = p.lu1[l];
-    E.piv1 = p.piv1[l];
-    E.lu2 = p.lu2[l];
-    E.piv2 = p.piv2[l];
+    E.inv1 = p.inv1[l];
+    E.inv2 = p.inv2[l];
     E.zr = p.zr[l];
   }
   for (size_t m = 0; m < used.size(); ++m) {
@@ -836,19 +1073,35 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   if (cudaMemsetAsync(p.XA, 0, sizeof(cd) * batch * (size_t)(2 * std::max(L, 1)) * 2 * n, s) != cudaSuccess)
     return KHP_ERR_CUDA;
   if (cudaMemsetAsync(p.RT, 0, sizeof(cd) * batch * 4 * n, s) != cudaSuccess) return KHP_ERR_CUDA;
-  for (int it = 0; it <= refine; ++it) {
-    k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr);
+  // refine rounds for every problem, then up to kExtraRounds more for the problems whose
+  // estimated error is still above 1e-9 (the others skip them); problems still unconverged get
+  // status bit 8.
+  const int total = refine >= 1 ? refine + kExtraRounds : 0;
+  for (int it = 0; it <= total; ++it) {
+    const int* act = it > refine ? p.active : nullptr;
+    k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr, act);
     count_launches(1);
     MX_TRY(cuda_status());
-    k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW);
+    k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW,
+                                                   p.corr + (it & 1) * batch, act);
     count_launches(1);
     MX_TRY(cuda_status());
+    if (it == refine && refine >= 1) {
+      if (cudaMemsetAsync(p.active, 0xff, sizeof(int) * batch, s) != cudaSuccess) return KHP_ERR_CUDA;
+    }
+    if (it >= refine && refine >= 1)
+      MX_EW(k_check_refine, batch, batch, p.corr + ((it - 1) & 1) * batch, p.corr + (it & 1) * batch, p.active);
   }
-  k_flux_cols<double><<<(unsigned)batch, 128, 0, s>>>(nh, npol, p.RT, p.RT + batch * 2 * n, gx, gy, kp, k0,
-                                                       reinterpret_cast<const cd*>(te), reinterpret_cast<const cd*>(tm),
-                                                       epsi, epse, R, Tt);
-  count_launches(1);
-  return cuda_status();
+  if (refine >= 1) MX_EW(k_flag_unconverged, batch, batch, p.active, status);
+  if (!grad) {
+    k_flux_cols<double><<<(unsigned)batch, 128, 0, s>>>(nh, npol, p.RT, p.RT + batch * 2 * n, gx, gy, kp, k0,
+                                                         reinterpret_cast<const cd*>(te),
+                                                         reinterpret_cast<const cd*>(tm), epsi, epse, R, Tt);
+    count_launches(1);
+    return cuda_status();
+  }
+  return grad_mixed(tb, p, gp, *grad, batch, nh, L, kinds, slot, used, depth_of, nmaps, conv, gx, gy, kp, k0, npol,
+                    te, tm, epsi, epse, refine, R, Tt, s);
 }
 
 }  // namespace
@@ -874,7 +1127,8 @@ size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlay
 
 int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
                             const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
-                            int64_t nmaps, const double* conv, const double* hx, const double* hy, const double* gx,
+                            const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                            const double* conv, const double* hx, const double* hy, const double* gx,
                             const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
                             const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
                             int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
@@ -890,9 +1144,49 @@ int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlaye
       return KHP_ERR_INVALID_ARG;
   }
   if (batch == 0) return KHP_OK;
-  return solve_mixed(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, conv, hx, hy, gx, gy,
+  return solve_mixed(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, problem_map,
+                     problem_depth, nmaps, conv, hx, hy, gx, gy,
                      mk(epsi_re, epsi_im), mk(epse_re, epse_im), kp, k0, npol, te, tm, refine_iters, R, T, status,
                      workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+size_t khp_solve_batched_mixed_grad_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
+                                              const int32_t* layer_map, int64_t nmaps) {
+  const size_t fwd = khp_solve_batched_mixed_workspace(batch, nh, nlayers, layer_kind, layer_map);
+  if (fwd == 0 || nmaps < 1) return 0;
+  Arena a{nullptr, 0};
+  a.off = fwd;
+  plan_grad(a, batch, nh, nlayers, nmaps);
+  return a.off;
+}
+
+int khp_solve_batched_mixed_grad(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                                 const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                                 const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                                 const double* conv, const double* ic, const double* hx, const double* hy,
+                                 const double* gx, const double* gy, double epsi_re, double epsi_im, double epse_re,
+                                 double epse_im, const double* kp, const double* k0, int32_t npol, const double* te,
+                                 const double* tm, int32_t refine_iters, const double* dR, const double* dT, double* R,
+                                 double* T, double* R_orders, double* T_orders, double* dconv, int32_t* status,
+                                 void* workspace, size_t ws_bytes, void* stream) {
+  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 1 || refine_iters > 8 || !gx ||
+      !gy || !kp || !k0 || !te || !tm || !R || !T || !status || !dconv || !ic || nmaps < 1)
+    return KHP_ERR_INVALID_ARG;
+  if (nlayers > kMaxLayers) return KHP_ERR_TOO_LARGE;
+  if (nlayers > 0 && (!layer_kind || !layer_map || !layer_eps || !layer_depth)) return KHP_ERR_INVALID_ARG;
+  for (int l = 0; l < nlayers; ++l) {
+    if (layer_kind[l] != 0 && layer_kind[l] != 1) return KHP_ERR_INVALID_ARG;
+    if (layer_kind[l] == 1 && (layer_map[l] < 0 || layer_map[l] >= nmaps || !conv || !hx || !hy))
+      return KHP_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t hh = (int64_t)px * py * px * py;
+  if (cudaMemsetAsync(dconv, 0, sizeof(double) * 2 * nmaps * hh, s) != cudaSuccess) return KHP_ERR_CUDA;
+  if (batch == 0) return KHP_OK;
+  GradArgs ga{ic, dR, dT, R_orders, T_orders, dconv};
+  return solve_mixed(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, problem_map,
+                     problem_depth, nmaps, conv, hx, hy, gx, gy, mk(epsi_re, epsi_im), mk(epse_re, epse_im), kp, k0,
+                     npol, te, tm, refine_iters, R, T, status, workspace, ws_bytes, s, &ga);
 }
 
 }  // extern "C"

@@ -140,6 +140,57 @@ __global__ void k_convmat_gather(int64_t nmaps, int px, int py, const cd* __rest
   }
 }
 
+// Adjoint of k_convmat_gather: dF[map][dx][dy] = sum of dC over the (r, c) with
+// p_r - p_c = dx, q_r - q_c = dy (fixed order).
+__global__ void k_convmat_bwd_gather(int64_t nmaps, int px, int py, const cd* __restrict__ dC, cd* dF) {
+  const int nh = px * py, ndx = 2 * px - 1, ndy = 2 * py - 1;
+  const int64_t total = nmaps * (int64_t)ndx * ndy;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t map = e / ((int64_t)ndx * ndy);
+    const int k = (int)(e % ((int64_t)ndx * ndy));
+    const int dx = k / ndy - (px - 1), dy = k % ndy - (py - 1);
+    cd acc = mk(0.0);
+    for (int qc = 0; qc < py; ++qc) {
+      const int qr = qc + dy;
+      if (qr < 0 || qr >= py) continue;
+      for (int pc = 0; pc < px; ++pc) {
+        const int pr = pc + dx;
+        if (pr < 0 || pr >= px) continue;
+        acc += dC[map * (int64_t)nh * nh + (int64_t)(qr * px + pr) * nh + (qc * px + pc)];
+      }
+    }
+    dF[e] = acc;
+  }
+}
+
+// Adjoint of k_convmat_dft, first stage: h[map][dxi][y] = sum_dy dF[map][dxi][dy] e^{-2 pi i dy y / ny}.
+__global__ void k_convmat_bwd_dft_y(int64_t nmaps, int px, int py, int64_t ny, const cd* __restrict__ dF, cd* h) {
+  const int ndx = 2 * px - 1, ndy = 2 * py - 1;
+  const int64_t total = nmaps * (int64_t)ndx * ny;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t y = e % ny, md = e / ny;  // md = map * ndx + dxi
+    cd acc = mk(0.0);
+    for (int dyi = 0; dyi < ndy; ++dyi) fma_acc(acc, dF[md * ndy + dyi], twiddle(dyi - (py - 1), y, ny));
+    h[e] = acc;
+  }
+}
+
+// Second stage: deps[map][x][y] = sum_dx h[map][dxi][y] e^{-2 pi i dx x / nx} / (nx ny).
+__global__ void k_convmat_bwd_dft_x(int64_t nmaps, int px, int64_t nx, int64_t ny, const cd* __restrict__ h,
+                                    cd* deps) {
+  const int ndx = 2 * px - 1;
+  const int64_t total = nmaps * nx * ny;
+  const double inv = 1.0 / ((double)nx * (double)ny);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t map = e / (nx * ny);
+    const int64_t xy = e % (nx * ny);
+    const int64_t x = xy / ny, y = xy % ny;
+    cd acc = mk(0.0);
+    for (int dxi = 0; dxi < ndx; ++dxi) fma_acc(acc, h[(map * ndx + dxi) * ny + y], twiddle(dxi - (px - 1), x, nx));
+    deps[e] = acc * inv;
+  }
+}
+
 // tmp = diag(g) C  (row scaling), batch of maps
 __global__ void k_row_scale_real(int64_t nmaps, int nh, const double* __restrict__ g, const cd* __restrict__ C, cd* out) {
   const int64_t total = nmaps * (int64_t)nh * nh;
@@ -582,6 +633,34 @@ int khp_convmat(int64_t nmaps, int64_t nx, int64_t ny, const double* eps, int32_
   count_launches(1);
   const int64_t total = nmaps * (int64_t)px * py * px * py;
   k_convmat_gather<<<ew_grid(total), 256, 0, s>>>(nmaps, px, py, w.F, (cd*)conv);
+  count_launches(1);
+  return cuda_status();
+}
+
+size_t khp_convmat_bwd_workspace(int64_t nmaps, int64_t ny, int32_t px, int32_t py) {
+  if (nmaps < 0 || ny < 1 || px < 1 || py < 1) return 0;
+  Arena a{nullptr, 0};
+  a.take<cd>(nmaps * (size_t)(2 * px - 1) * (2 * py - 1));
+  a.take<cd>(nmaps * (size_t)(2 * px - 1) * (size_t)ny);
+  return a.off;
+}
+
+int khp_convmat_bwd(int64_t nmaps, int64_t nx, int64_t ny, const double* dconv, int32_t px, int32_t py, double* deps,
+                    void* workspace, size_t ws_bytes, void* stream) {
+  if (nmaps < 0 || px < 1 || py < 1 || (px % 2) == 0 || (py % 2) == 0) return KHP_ERR_INVALID_ARG;
+  if (nx < 2 * px - 1 || ny < 2 * py - 1 || !dconv || !deps) return KHP_ERR_INVALID_ARG;
+  if (nmaps == 0) return KHP_OK;
+  Arena a{static_cast<char*>(workspace), ws_bytes};
+  cd* dF = a.take<cd>(nmaps * (size_t)(2 * px - 1) * (2 * py - 1));
+  cd* h = a.take<cd>(nmaps * (size_t)(2 * px - 1) * (size_t)ny);
+  if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
+  cudaStream_t s = as_stream(stream);
+  k_convmat_bwd_gather<<<ew_grid(nmaps * (int64_t)(2 * px - 1) * (2 * py - 1)), 256, 0, s>>>(nmaps, px, py,
+                                                                                            (const cd*)dconv, dF);
+  count_launches(1);
+  k_convmat_bwd_dft_y<<<ew_grid(nmaps * (int64_t)(2 * px - 1) * ny), 256, 0, s>>>(nmaps, px, py, ny, dF, h);
+  count_launches(1);
+  k_convmat_bwd_dft_x<<<ew_grid(nmaps * nx * ny), 256, 0, s>>>(nmaps, px, nx, ny, h, (cd*)deps);
   count_launches(1);
   return cuda_status();
 }

@@ -208,6 +208,11 @@ class Problems:
     def batch(self):
         return int(self.k0.shape[0])
 
+    def subset(self, idx: torch.Tensor) -> "Problems":
+        """The problems at device indices ``idx``."""
+        return Problems(k0=self.k0[idx].contiguous(), kp=self.kp[idx].contiguous(), te=self.te[idx].contiguous(),
+                        tm=self.tm[idx].contiguous())
+
     @classmethod
     def make(cls, wavelengths, kp, te, tm, device):
         wl = np.atleast_1d(np.asarray(wavelengths, dtype=float))

@@ -23,3 +23,15 @@ def golden():
         return np.load(os.path.join(GOLDEN, name + ".npz"))
 
     return load
+
+
+@pytest.fixture(scope="session")
+def khp():
+    """The built package on a CUDA device (GPU tests only)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from khepri_gb300 import build as kb
+    kb.build()
+    import khepri_gb300
+    return khepri_gb300

@@ -13,17 +13,6 @@ RT_TOL = 1e-6       # the path's parity bar on R and T
 TIGHT = 1e-9        # what the FP64 kernels actually deliver on these small cases
 
 
-@pytest.fixture(scope="module")
-def khp():
-    import torch
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
-    from khepri_gb300 import build as kb
-    kb.build()
-    import khepri_gb300
-    return khepri_gb300
-
-
 def _crystal(khp, pw, layers, stack, mask=False, **kw):
     cl = khp.Crystal(pw, **kw)
     for name, (kind, eps, depth) in layers.items():
@@ -310,3 +299,59 @@ def test_mixed_precision_small_cases(khp, golden):
         R, T, s = batch.solve_rt((5, 5), layers, ["P1", "U1", "P2", "U2", "P3"], [g["wavelength"][i]], [kp],
                                  g["te"][i], g["tm"][i], epsi=g["epsi"][i], epse=g["epse"][i], method="mixed")
         assert abs(R[0] - g["R"][i]) < RT_TOL and abs(T[0] - g["T"][i]) < RT_TOL
+
+
+def test_mixed_precision_repairs_ill_conditioned_problem(khp):
+    """A sweep problem next to a Wood anomaly (f index 49, k index 341 of the 11x11 sweep) whose
+    FP32-preconditioned refinement converges too slowly: the mixed path must flag it (status
+    bit 8) and re-solve it in FP64, so that it still meets |dR|, |dT| <= 1e-6."""
+    from khepri_gb300 import batch, workloads
+    st = workloads.batched_structure(0)
+    wl, kp = workloads.batched_problems()
+    inside = np.flatnonzero(np.hypot(kp[:, 0], kp[:, 1]) < 2 * np.pi / wl)
+    idx = np.concatenate([[50517, 38308, 47259], inside[inside > 20000][:3]])
+    before = batch.STATS["fp64_repairs"]
+    Rm, Tm, sm = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="mixed")
+    assert batch.STATS["fp64_repairs"] > before
+    assert not sm.any()
+    Rg, Tg, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="gamma")
+    assert np.isfinite(Rg).all() and np.isfinite(Tg).all()
+    err = max(np.abs(Rm - Rg).max(), np.abs(Tm - Tg).max())
+    print("mixed (with FP64 repair) vs fp64 max |dR|,|dT| =", err)
+    assert err < RT_TOL
+
+
+def test_solve_structures_uneven_golden(khp, golden):
+    """Many lossy structures of different sizes and layer counts through the multi-structure
+    batched path (grouped by shape, per-problem maps and depths), FP64 and mixed, against the
+    reference's complex128 values."""
+    from khepri_gb300 import batch, workloads
+    g = golden("uneven_small")
+    structs = workloads.uneven_structures(int(g["count"]), seed=int(g["seed"]), n_pix=int(g["n_pix"]),
+                                          max_pw=int(g["max_pw"]), max_layers=int(g["max_layers"]))
+    entries = [(st.pw, st.layers, st.stack) for st, _, _ in structs]
+    wl = np.array([w for _, w, _ in structs])
+    kp = np.array([k for _, _, k in structs])
+    for method, tol in (("gamma", 1e-8), ("mixed", RT_TOL)):
+        R, T, s = batch.solve_structures(entries, wl, kp, te=1.0, tm=1.0, method=method, chunk=5)
+        assert not s.any()
+        np.testing.assert_allclose(R, g["R"], atol=tol)
+        np.testing.assert_allclose(T, g["T"], atol=tol)
+
+
+def test_solve_structures_designs_golden(khp, golden):
+    """Inverse-design structures x frequencies (problem -> structure map) in one batched call per
+    chunk, against the reference's complex128 values."""
+    from khepri_gb300 import batch, workloads
+    g = golden("design_9x9")
+    _, structs, freqs = workloads.inverse_design(int(g["count"]), seed=int(g["seed"]))
+    entries = [(st.pw, st.layers, st.stack) for st in structs]
+    f = freqs[[0, 7, 15]]
+    which = np.repeat(np.arange(len(structs)), len(f))
+    wl = np.tile(1.0 / f, len(structs))
+    kp = np.zeros((len(wl), 2))
+    for method, tol in (("gamma", 1e-8), ("mixed", RT_TOL)):
+        R, T, s = batch.solve_structures(entries, wl, kp, which=which, method=method)
+        assert not s.any()
+        np.testing.assert_allclose(R, g["R"], atol=tol)
+        np.testing.assert_allclose(T, g["T"], atol=tol)
