@@ -75,7 +75,9 @@ def parse():
     ap.add_argument("--plain", type=int, default=2, help="single-problem drop-in solves timed for comparison")
     ap.add_argument("--grad-designs", type=int, default=64,
                     help="inverse-design structures (x 16 frequencies) for the solve+grad measurement (0 = skip)")
-    ap.add_argument("--uneven", type=int, default=96, help="uneven structures for the many-structure measurement")
+    ap.add_argument("--uneven", type=int, default=0, help="uneven structures for the many-structure measurement")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
 
 
@@ -368,6 +370,12 @@ def run_gpu(args):
     ms = replicas.max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms * 1e-3)
     bad = int(sum(int((s != 0).sum().item()) for s in statuses))
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": ms / args.steps, "kernels_only": True,
+                              "config": {"batch": B, "problems_with_status": bad}}), flush=True)
+        return
 
     # roofline of the entry point with the largest share of the timed region
     totals = timer.totals_ms()

@@ -480,15 +480,31 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
       H[(int64_t)(r0 + i) * ld + c0 + j] = win[i * WS + j];
     }
     const int nrot = k1 - k0;
+    // Each thread's strip is rotated in chunks of RB elements: the chunk's loads are issued
+    // together (one memory latency per chunk instead of one per rotation), the running element
+    // `a` is carried from chunk to chunk.
+    constexpr int RB = 8;
     // rows k0..k1, columns right of the window: left rotations, rolling down the column
     for (int j = k1 + 1 + t.tid(); j < n; j += t.size()) {
       cplx<T> a = H[(int64_t)k0 * ld + j];
-      for (int q = 0; q < nrot; ++q) {
-        const T c = rc[q];
-        const cplx<T> s = rs[q];
-        const cplx<T> b = H[(int64_t)(k0 + q + 1) * ld + j];
-        H[(int64_t)(k0 + q) * ld + j] = c * a + s * b;
-        a = c * b - conj_mul(s, a);
+      for (int q0 = 0; q0 < nrot; q0 += RB) {
+        cplx<T> v[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u)
+          if (q0 + u < nrot) v[u] = H[(int64_t)(k0 + q0 + u + 1) * ld + j];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+          if (q0 + u < nrot) {
+            const T c = rc[q0 + u];
+            const cplx<T> s = rs[q0 + u];
+            const cplx<T> b = v[u];
+            v[u] = c * a + s * b;  // new value of row k0 + q0 + u
+            a = c * b - conj_mul(s, a);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u)
+          if (q0 + u < nrot) H[(int64_t)(k0 + q0 + u) * ld + j] = v[u];
       }
       H[(int64_t)k1 * ld + j] = a;
     }
@@ -496,12 +512,24 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
     for (int i = t.tid(); i < r0 + n; i += t.size()) {
       cplx<T>* row = (i < r0) ? H + (int64_t)i * ld : Z + (int64_t)(i - r0) * ldz;
       cplx<T> a = row[k0];
-      for (int q = 0; q < nrot; ++q) {
-        const T c = rc[q];
-        const cplx<T> s = rs[q];
-        const cplx<T> b = row[k0 + q + 1];
-        row[k0 + q] = c * a + mul_conj(b, s);
-        a = c * b - s * a;
+      for (int q0 = 0; q0 < nrot; q0 += RB) {
+        cplx<T> v[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u)
+          if (q0 + u < nrot) v[u] = row[k0 + q0 + u + 1];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+          if (q0 + u < nrot) {
+            const T c = rc[q0 + u];
+            const cplx<T> s = rs[q0 + u];
+            const cplx<T> b = v[u];
+            v[u] = c * a + mul_conj(b, s);  // new value of column k0 + q0 + u
+            a = c * b - s * a;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u)
+          if (q0 + u < nrot) row[k0 + q0 + u] = v[u];
       }
       row[k1] = a;
     }

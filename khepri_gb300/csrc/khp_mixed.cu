@@ -166,6 +166,25 @@ __global__ void k_sqrt_mu(int64_t count, const cd* __restrict__ mu64, cd* lam64,
   }
 }
 
+// Per-matrix copies of kp ([batch][2] complex) and k0 for the slot-major modes batch.
+__global__ void k_expand_problems(int64_t total, int64_t batch, int S, const double* __restrict__ kp,
+                                  const double* __restrict__ k0, double* kpx, double* k0x) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < total; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = v % batch;
+    for (int q = 0; q < 4; ++q) kpx[4 * v + q] = kp[4 * b + q];
+    k0x[v] = k0[b];
+  }
+}
+
+// status[b] |= statx[m][b] over the S slots.
+__global__ void k_or_status(int64_t batch, int S, const int* __restrict__ statx, int* status) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x) {
+    int w = 0;
+    for (int m = 0; m < S; ++m) w |= statx[(int64_t)m * batch + b];
+    status[b] |= w;
+  }
+}
+
 __global__ void k_round(int64_t count, const cd* __restrict__ in, cf* out) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = mk((float)in[e].re, (float)in[e].im);
@@ -722,6 +741,10 @@ struct MixedPlan {
   int *pair, *nearest;
   int* piv;
   std::vector<int*> midx;  // per map slot: the map index of every problem
+  // the modes of all map slots run as one batch of S x batch matrices (slot-major): per-matrix
+  // copies of kp, k0 and a per-matrix status
+  double *kpx, *k0x;
+  int* statx;
   // per layer
   std::vector<cf*> inv1, inv2, zr;
   std::vector<M2*> blocks;
@@ -737,32 +760,39 @@ struct MixedPlan {
 MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, int nmaps_used) {
   const size_t n = 2 * (size_t)nh, nn = n * n;
   MixedPlan p;
-  for (int m = 0; m < nmaps_used; ++m) {
-    p.W32.push_back(a.take<cf>(batch * nn));
-    p.V32.push_back(a.take<cf>(batch * nn));
-    p.lam32.push_back(a.take<cf>(batch * n));
-    p.Wi.push_back(a.take<cf>(batch * nn));
-    p.Vi.push_back(a.take<cf>(batch * nn));
-    p.Q0.push_back(a.take<cf>(batch * nn));
-    p.Vt.push_back(a.take<cf>(batch * nn));
-    p.W64.push_back(a.take<cd>(batch * nn));
-    p.V64.push_back(a.take<cd>(batch * nn));
-    p.lam64.push_back(a.take<cd>(batch * n));
-    p.midx.push_back(a.take<int>(batch));
-  }
-  p.M32 = a.take<cf>(batch * nn);
-  p.Z32 = a.take<cf>(batch * nn);
-  p.E32 = a.take<cf>(batch * nn);
-  p.lu32 = a.take<cf>(batch * nn);
-  p.M64 = a.take<cd>(batch * nn);
-  p.MW64 = a.take<cd>(batch * nn);
-  p.CW64 = a.take<cd>(batch * nn);
+  const size_t S = std::max(nmaps_used, 1);
+  const size_t bm = S * batch;  // matrices of the modes stage
+  // per-slot arrays are slices of one slot-major block each
+  auto slices = [&](auto* base, size_t per, auto& vec) {
+    for (int m = 0; m < nmaps_used; ++m) vec.push_back(base ? base + m * per : nullptr);
+  };
+  slices(a.take<cf>(bm * nn), batch * nn, p.W32);
+  slices(a.take<cf>(bm * nn), batch * nn, p.V32);
+  slices(a.take<cf>(bm * n), batch * n, p.lam32);
+  slices(a.take<cf>(bm * nn), batch * nn, p.Wi);
+  slices(a.take<cf>(bm * nn), batch * nn, p.Vi);
+  slices(a.take<cf>(bm * nn), batch * nn, p.Q0);
+  slices(a.take<cf>(bm * nn), batch * nn, p.Vt);
+  slices(a.take<cd>(bm * nn), batch * nn, p.W64);
+  slices(a.take<cd>(bm * nn), batch * nn, p.V64);
+  slices(a.take<cd>(bm * n), batch * n, p.lam64);
+  slices(a.take<int>(bm), batch, p.midx);
+  p.M32 = a.take<cf>(bm * nn);
+  p.Z32 = a.take<cf>(bm * nn);
+  p.E32 = a.take<cf>(bm * nn);
+  p.lu32 = a.take<cf>(bm * nn);
+  p.M64 = a.take<cd>(bm * nn);
+  p.MW64 = a.take<cd>(bm * nn);
+  p.CW64 = a.take<cd>(bm * nn);
   p.Ct64 = nullptr;
-  p.mu64 = a.take<cd>(batch * n);
-  p.mu64b = a.take<cd>(batch * n);
-  p.pair = a.take<int>(batch * n);
-  p.nearest = a.take<int>(batch * n);
-  p.piv = a.take<int>(batch * n);
+  p.mu64 = a.take<cd>(bm * n);
+  p.mu64b = a.take<cd>(bm * n);
+  p.pair = a.take<int>(bm * n);
+  p.nearest = a.take<int>(bm * n);
+  p.piv = a.take<int>(bm * n);
+  p.kpx = a.take<double>(bm * 4);
+  p.k0x = a.take<double>(bm);
+  p.statx = a.take<int>(bm);
   for (int l = 0; l < L; ++l) {
     p.inv1.push_back(a.take<cf>(batch * nn));
     p.zr.push_back(a.take<cf>(batch * nn));
@@ -950,53 +980,69 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   const cf one = mk(1.f), zero = mk(0.f), mone = mk(-1.f);
   const cd done = mk(1.0), dzero = mk(0.0);
 
-  // ---- 1. modes: FP32 eigensolve + FP64 refinement ----
-  for (size_t m = 0; m < used.size(); ++m) {
+  // ---- 1. modes: FP32 eigensolve + FP64 refinement, every map slot in one batch ----
+  const int S = (int)used.size();
+  if (S > 0) {
+    const int64_t bm = (int64_t)S * batch;
     const cd* Cm = reinterpret_cast<const cd*>(conv);
     const cd* HX = reinterpret_cast<const cd*>(hx);
     const cd* HY = reinterpret_cast<const cd*>(hy);
-    MX_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps, p.midx[m],
-          status);
-    MX_EW(k_assemble_pq_t<float>, batch * nn, batch, nh, Cm, HX, HY, p.midx[m], gx, gy, kp, k0, p.M32);
-    MX_TRY(launch_geev<float>(batch, n, p.M32, n, nn, p.Z32, p.W32[m], n, nn, p.lam32[m], n, status, s));
+    int* const midx = p.midx[0];  // [S][batch]
+    cf* const W32 = p.W32[0];
+    cf* const V32 = p.V32[0];
+    cf* const lam32 = p.lam32[0];
+    cf* const Wi = p.Wi[0];
+    cf* const Vi = p.Vi[0];
+    cd* const W64 = p.W64[0];
+    cd* const V64 = p.V64[0];
+    cd* const lam64 = p.lam64[0];
+    const double* kpx = p.kpx;
+    const double* k0x = p.k0x;
+    int* sx = p.statx;
+    MX_EW(k_expand_problems, bm, bm, batch, S, kp, k0, p.kpx, p.k0x);
+    if (cudaMemsetAsync(sx, 0, sizeof(int) * bm, s) != cudaSuccess) return KHP_ERR_CUDA;
+    for (int m = 0; m < S; ++m)
+      MX_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps,
+            midx + (int64_t)m * batch, sx + (int64_t)m * batch);
+    MX_EW(k_assemble_pq_t<float>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32);
+    MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s));
     // Refinement steps: R = M W - W mu in FP64, E = W0^-1 R (FP32 inverse of the FP32 solver's
     // W0, held in Wi until the final inverse), mu += diag(E), W += W F.
-    MX_EW(k_assemble_pq_t<double>, batch * nn, batch, nh, Cm, HX, HY, p.midx[m], gx, gy, kp, k0, p.M64);
-    MX_EW(k_to_double, batch * nn, batch * nn, p.W32[m], p.W64[m]);
-    MX_EW(k_to_double, batch * n, batch * n, p.lam32[m], p.mu64);
-    MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
+    MX_EW(k_assemble_pq_t<double>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M64);
+    MX_EW(k_to_double, bm * nn, bm * nn, W32, W64);
+    MX_EW(k_to_double, bm * n, bm * n, lam32, p.mu64);
+    MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
     for (int step = 0; step < kEigSteps; ++step) {
-      MX_TRY(launch_gemm<double>(batch, n, n, n, done, p.M64, n, nn, p.W64[m], n, nn, dzero, p.MW64, n, nn, s));
-      MX_EW(k_eig_residual, batch * nn, batch, n, p.MW64, p.W64[m], mu_a, p.E32);
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
-      k_find_pairs<<<(unsigned)batch, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
+      MX_TRY(launch_gemm<double>(bm, n, n, n, done, p.M64, n, nn, W64, n, nn, dzero, p.MW64, n, nn, s));
+      MX_EW(k_eig_residual, bm * nn, bm, n, p.MW64, W64, mu_a, p.E32);
+      MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
+      k_find_pairs<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
       count_launches(1);
       MX_TRY(cuda_status());
-      MX_EW(k_eig_update, batch * nn, batch, n, mu_a, p.Z32, p.M32, mu_b, p.pair);      // M32 <- F
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
-      MX_EW(k_add_correction, batch * nn, batch * nn, p.W64[m], p.Z32, p.W32[m]);
+      MX_EW(k_eig_update, bm * nn, bm, n, mu_a, p.Z32, p.M32, mu_b, p.pair);  // M32 <- F
+      MX_TRY(launch_gemm<float>(bm, n, n, n, one, W32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
+      MX_EW(k_add_correction, bm * nn, bm * nn, W64, p.Z32, W32);
       std::swap(mu_a, mu_b);
     }
-    MX_EW(k_sqrt_mu, batch * n, batch * n, mu_a, p.lam64[m], p.lam32[m]);
+    MX_EW(k_sqrt_mu, bm * n, bm * n, mu_a, lam64, lam32);
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
-    cd* CWb = p.CW64 + batch * hn;
-    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, Cm, nh, hh, p.W64[m], n, nn, dzero, CWt, n, hn, s, p.midx[m]));
-    MX_TRY(launch_gemm<double>(batch, nh, n, nh, done, Cm, nh, hh, p.W64[m] + hn, n, nn, dzero, CWb, n, hn, s,
-                               p.midx[m]));
-    MX_EW(k_modes_v_t<double>, batch * nn, batch, nh, gx, gy, kp, k0, p.W64[m], CWt, CWb, p.lam64[m], p.V64[m],
-          status);
-    MX_EW(k_round, batch * nn, batch * nn, p.V64[m], p.V32[m]);
+    cd* CWb = p.CW64 + bm * hn;
+    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64, n, nn, dzero, CWt, n, hn, s, midx));
+    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64 + hn, n, nn, dzero, CWb, n, hn, s, midx));
+    MX_EW(k_modes_v_t<double>, bm * nn, bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, lam64, V64, sx);
+    MX_EW(k_round, bm * nn, bm * nn, V64, V32);
     // FP32 inverses and V0 products
-    MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Wi[m], n, nn, p.piv, status, s));
-    MX_TRY(launch_copy<float>(batch, n, n, p.V32[m], n, nn, p.lu32, n, nn, s));
-    MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.Vi[m], n, nn, p.piv, status, s));
-    MX_EW(k_v0_right<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.Vi[m], p.Q0[m]);
-    MX_EW(k_v0inv_left<float>, batch * nn, batch, nh, gx, gy, kp, k0, p.V32[m], p.Vt[m]);
+    MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
+    MX_TRY(launch_copy<float>(bm, n, n, V32, n, nn, p.lu32, n, nn, s));
+    MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Vi, n, nn, p.piv, sx, s));
+    MX_EW(k_v0_right<float>, bm * nn, bm, nh, gx, gy, kpx, k0x, Vi, p.Q0[0]);
+    MX_EW(k_v0inv_left<float>, bm * nn, bm, nh, gx, gy, kpx, k0x, V32, p.Vt[0]);
+    MX_EW(k_or_status, batch, batch, S, sx, status);
   }
   // ---- homogeneous blocks (FP64) ----
   MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
