@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--grad-designs", type=int, default=64,
                     help="inverse-design structures (x 16 frequencies) for the solve+grad measurement (0 = skip)")
     ap.add_argument("--uneven", type=int, default=0, help="uneven structures for the many-structure measurement")
+    ap.add_argument("--twisted", type=int, default=16,
+                    help="twisted-bilayer problems (5x5 base harmonics, n = 1250) for the extended-crystal measurement")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -294,6 +296,27 @@ def bench_uneven(args):
             "sizes": "pw 3..17 odd, 1..8 layers; grouped by shape into batched calls"}
 
 
+def bench_twisted(args):
+    """Twisted bilayers at 5x5 base harmonics (product expansion of 625 orders, n = 1250): a disc
+    grating (eps 12 in 1, 128x128 map, depth 0.3) on each side of a gap (d 0.3), twist 13 deg,
+    frequencies 0.4-0.7 at normal incidence, both polarisations; host wall clock through
+    TwistedBilayer.solve_rt after one untimed problem."""
+    from khepri_gb300 import twisted
+    if args.twisted <= 0:
+        return None
+    x = np.linspace(-0.5, 0.5, 128)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    disc = np.where(X ** 2 + Y ** 2 < 0.3 ** 2, 12.0, 1.0)
+    tw = twisted.TwistedBilayer((5, 5), "square", np.deg2rad(13.0), [("pixmap", disc, 0.3)],
+                                [("uniform", 1.0, 0.3)], [("pixmap", disc, 0.3)])
+    f = np.linspace(0.4, 0.7, args.twisted)
+    tw.solve_rt(1.0 / f[:1], np.zeros((1, 2)), both_pols=True)
+    res, t = _timed(lambda: tw.solve_rt(1.0 / f, np.zeros((len(f), 2)), both_pols=True, chunk=16, strict=False))
+    R, T, st = res
+    return {"solves_per_s": len(f) / t, "problems": len(f), "seconds": t, "n_extended": 1250,
+            "max_abs_R_plus_T_minus_1": float(np.abs(R + T - 1).max()), "problems_with_status": int((st != 0).sum())}
+
+
 def run_gpu(args):
     import torch
 
@@ -462,10 +485,11 @@ def run_gpu(args):
                "sample": f"{args.cpu_sample} in-cone problems of the 11x11 sweep, both polarisations, CPU oracle "
                          f"(numpy/LAPACK), {t_cpu:.1f} s"}
 
-    grad_info = uneven_info = None
+    grad_info = uneven_info = twisted_info = None
     if rank == 0:
         grad_info = bench_grad(args, struct, st, wl_all, kp_all)
         uneven_info = bench_uneven(args)
+        twisted_info = bench_twisted(args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -487,7 +511,7 @@ def run_gpu(args):
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
                        "fp64_repairs": repairs,
-                       "solve_grad": grad_info, "uneven": uneven_info},
+                       "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": world * B * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

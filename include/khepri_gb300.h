@@ -57,6 +57,20 @@ int khp_convmat(int64_t nmaps, int64_t nx, int64_t ny, const double* eps, int32_
                 void* workspace, size_t ws_bytes, void* stream);
 
 /*
+ * Convolution matrices of analytical layers (Layer.analytical, khepri/layer.py:161-168): closed-
+ * form Fourier transforms of disc and rectangle islands in a host medium (fourier.py:23-58,
+ * 145-159), then the same Toeplitz rule as khp_convmat.
+ *   islands: device [nislands][8] doubles = map index, type (0 disc: center0, center1, radius;
+ *     1 rectangle: ll0, ll1, ur0, ur1; in the reference's Drawing.islands() coordinates),
+ *     eps re, eps im, params[4];  eps_host: device complex [nmaps];
+ *   b1, b2: reciprocal basis (2 pi convention); cell_area: |a1 x a2|;  conv: complex [nmaps][nh][nh].
+ */
+size_t khp_convmat_islands_workspace(int64_t nmaps, int32_t px, int32_t py);
+int khp_convmat_islands(int64_t nmaps, int32_t px, int32_t py, int32_t nislands, const double* islands,
+                        const double* eps_host, double b1x, double b1y, double b2x, double b2y, double cell_area,
+                        double* conv, void* workspace, size_t ws_bytes, void* stream);
+
+/*
  * Per-structure preparation of a patterned layer (done once, reused for every wavelength and
  * k-point): ic = C^-1 (the reference's Layer.IC, khepri/layer.py:158) and the products
  * hx = C^-1 diag(gx) C, hy = C^-1 diag(gy) C that make P*Q assemble in O(n^2) per problem.
@@ -203,6 +217,25 @@ int khp_solve_batched_mixed_grad(int64_t batch, int32_t px, int32_t py, int32_t 
 size_t khp_convmat_bwd_workspace(int64_t nmaps, int64_t ny, int32_t px, int32_t py);
 int khp_convmat_bwd(int64_t nmaps, int64_t nx, int64_t ny, const double* dconv, int32_t px, int32_t py, double* deps,
                     void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Twisted bilayers: R and T of an extended crystal over the product expansion e1 + e2
+ * (khepri/expansion.py:52-73, khepri/extension.py:10-126, crystal.py:180-206, 363-396), from the
+ * base-size chains.  s_left: device complex [batch][nbase][2][2][2 nbase][2 nbase], the chain
+ * (incidence half-space * layers on e1 * uniform layers) solved on e1 at kp + g2[m] for every
+ * harmonic m of e2; s_right: the chain (layers on e2 * emergence half-space) on e2 at kp + g1[m].
+ * Only the final product is dense (n = 2 nbase^2): t = B21 (I - A22 B11)^-1 A21 c,
+ * r = A11 c + A12 B11 (I - A22 B11)^-1 A21 c, with one FP64 LU per problem.
+ *   gx, gy: the product expansion's G vectors [nbase^2] (index p nbase + q: e1 harmonic p,
+ *   e2 harmonic q);  te, tm: complex [batch][npol];  R, T: [batch][npol];  rv, tv: optional
+ *   complex [batch][2 nbase^2][2] out (reflected / transmitted amplitudes of the two unit
+ *   sources, NULL = not kept).
+ */
+size_t khp_twisted_rt_workspace(int64_t batch, int32_t nbase);
+int khp_twisted_rt(int64_t batch, int32_t nbase, const double* s_left, const double* s_right, const double* gx,
+                   const double* gy, const double* kp, const double* k0, int32_t npol, const double* te,
+                   const double* tm, double epsi_re, double epsi_im, double epse_re, double epse_im, double* R,
+                   double* T, double* rv, double* tv, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 /*
  * Star product without a caller-supplied workspace.  No counterpart in the reference: it

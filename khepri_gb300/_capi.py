@@ -62,8 +62,14 @@ _SIGNATURES = {
                                                     _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_d, _c_d,
                                                     _c_d, _c_d, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_i32, _c_p, _c_p,
                                                     _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_convmat_islands_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32]),
+    "khp_convmat_islands": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_d,
+                                           _c_p, _c_p, _c_sz, _c_p]),
     "khp_convmat_bwd_workspace": (_c_sz, [_c_i64, _c_i64, _c_i32, _c_i32]),
     "khp_convmat_bwd": (ctypes.c_int, [_c_i64, _c_i64, _c_i64, _c_p, _c_i32, _c_i32, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_twisted_rt_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_twisted_rt": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_d, _c_d,
+                                      _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
 }

@@ -17,8 +17,16 @@ from . import _capi, engine
 from .engine import LayerSpec
 
 
+def _spec(kind, eps, depth):
+    """("pixmap", map, d) | ("uniform", eps, d) | ("analytical", (islands, eps_host) or AnalyticalMap, d)."""
+    if kind == "analytical":
+        amap = eps if isinstance(eps, engine.AnalyticalMap) else engine.AnalyticalMap(*eps)
+        return LayerSpec("pixmap", amap, depth)
+    return LayerSpec(kind, eps, depth)
+
+
 def _specs(layers, epsi, epse):
-    specs = {name: LayerSpec(kind, eps, depth) for name, (kind, eps, depth) in layers.items()}
+    specs = {name: _spec(kind, eps, depth) for name, (kind, eps, depth) in layers.items()}
     specs["__inc__"] = LayerSpec("inc", epsi, 0.0)
     specs["__trn__"] = LayerSpec("trn", epse, 0.0)
     return specs
@@ -90,10 +98,11 @@ class StackPlan:
         self.nmaps = len(entries)
         if entries:
             self.conv = torch.cat([e["conv"] for e in entries]).contiguous()
+            self.ic = torch.cat([e["ic"] for e in entries]).contiguous()
             self.hx = torch.cat([e["hx"] for e in entries]).contiguous()
             self.hy = torch.cat([e["hy"] for e in entries]).contiguous()
         else:
-            self.conv = self.hx = self.hy = None
+            self.conv = self.ic = self.hx = self.hy = None
 
 
 def _host(a):
@@ -268,6 +277,7 @@ class _ChunkPlan:
         self.depth = np.zeros(len(kinds), dtype=np.float64)  # per-problem depths are passed instead
         self.nmaps = 0 if conv is None else int(conv.shape[0])
         self.conv, self.hx, self.hy = conv, hx, hy
+        self.ic = None
 
 
 def _shape_key(layers, stack):

@@ -51,6 +51,11 @@ class Layer:
         return cls.pixmap(expansion, pixmap, depth)
 
     @classmethod
+    def analytical(cls, expansion, islands_description, eps_host, depth):
+        """layer.py:121-129: islands (Drawing.islands()) in a host medium, closed-form transforms."""
+        return cls("pixmap", engine.AnalyticalMap(islands_description, eps_host), depth)
+
+    @classmethod
     def half_infinite(cls, expansion, type, epsilon):
         if type == "reflexion":
             return cls("inc", epsilon, 0)
@@ -93,6 +98,10 @@ class Crystal:
 
     def add_layer_pixmap(self, name, epsilon, depth):
         self.layers[name] = Layer("pixmap", epsilon, depth)
+
+    def add_layer_analytical(self, name, epsilon, epsilon_host, depth):
+        """crystal.py:119-123: ``epsilon`` is an islands description (Drawing.islands())."""
+        self.layers[name] = Layer.analytical(None, epsilon, epsilon_host, depth)
 
     def add_layer(self, name, layer, extended=False):
         if extended:

@@ -202,9 +202,7 @@ __global__ void __launch_bounds__(256) k_stack_residual_T(Table tb, const double
       const cd xi = xprop(lam, i, dk);
       rap[e] = p1[e] - p2[e] + xi * (p3[e] - p4[e]);
       ram[e] = xi * (p1[e] + p2[e]) + p3[e] + p4[e];
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 v0 = phys::v0_block(kx, ky);
+      const M2 v0 = tb.v0b[b * nh + g];
       const cd v2 = m2T_apply(v0, rb, g, nh, c, y2);
       const cd v4 = m2T_apply(v0, rb, g, nh, c, y4);
       cpt[e] += -y1[e] + v2;
@@ -413,9 +411,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep_T(Table tb, const double* g
       k1b[e] = k1b[e] + T0[e] - T1[e];
       k2b[e] = k2b[e] + T0[e] + T1[e];
       f1[e] += ld2(k1b, i, c);
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 vi = phys::inv2(phys::v0_block(kx, ky));
+      const M2 vi = tb.v0ib[b * nh + g];
       const cd z = m2T_apply(vi, rb, g, nh, c, k2b);
       f2[e] += z;
       T2[e] = to_f(z);
@@ -447,9 +443,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep_T(Table tb, const double* g
       const int g = i % nh, rb = i / nh;
       f3[e] += ld2(T2, i, c);
       f4[e] += ld2(T3, i, c);
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 v0 = phys::v0_block(kx, ky);
+      const M2 v0 = tb.v0b[b * nh + g];
       const cd sv = ld2(sj, i, c) - ld2(T2, i, c) - m2T_apply(v0, rb, g, nh, c, T3);
       sj[e] = to_f(sv);
     }

@@ -161,7 +161,17 @@ template <typename T> KHP_HD T team_sum(const TeamSerial&, T v, TeamShared*) { r
 // Largest v over the team with its index (ties -> smallest index), returned to every thread.
 template <typename T> KHP_HD void team_argmax(const TeamSerial&, T& v, int& idx, TeamShared*) {}
 
+// Sum of a complex value over the 32 lanes of a warp, returned to every lane (TeamSerial: itself).
+template <typename T> KHP_HD cplx<T> warp_sum(const TeamSerial&, cplx<T> v) { return v; }
+
 #ifdef __CUDACC__
+template <typename T> __device__ __forceinline__ cplx<T> warp_sum(const TeamCta&, cplx<T> v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.re += __shfl_xor_sync(0xffffffffu, v.re, o);
+    v.im += __shfl_xor_sync(0xffffffffu, v.im, o);
+  }
+  return v;
+}
 template <typename T> __device__ __forceinline__ T team_sum(const TeamCta&, T v, TeamShared* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;

@@ -314,12 +314,18 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
                 cudaStream_t s, const int* aidx, const int* bidx) {
   if (batch <= 0 || n <= 0 || m <= 0) return KHP_OK;
-  constexpr int BM = 32, BN = 32, BK = 16;
+  // 64 x 64 tiles (4 x 4 outputs per thread) once both output dimensions reach 64, else 32 x 32
+  const bool big = n >= 64 && m >= 64;
+  const int BM = big ? 64 : 32, BN = big ? 64 : 32;
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     dim3 grid((m + BN - 1) / BN, (n + BM - 1) / BM, nb);
-    k_gemm<T, BM, BN, BK><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
+    if (big)
+      k_gemm<T, 64, 64, 8><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
                                                 aidx, bidx);
+    else
+      k_gemm<T, 32, 32, 16><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
+                                                 aidx, bidx);
     count_launches(1);
   }
   return cuda_status();
@@ -329,7 +335,10 @@ template <typename T>
 int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
                 int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
-  const size_t smem = sizeof(cplx<T>) * (size_t)n;
+  const size_t smem = sizeof(cplx<T>) * (size_t)n;  // Householder vector
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_geev_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return KHP_ERR_CUDA;
   k_geev_schur<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
   count_launches(1);
   int st = cuda_status();

@@ -244,7 +244,8 @@ KHP_HD void team_gehrd(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z,
       for (int l = 0; l < m; ++l) fms_acc(H[(k + 1 + l) * ld + j], vbuf[l], w);
     }
     t.sync();
-    // H <- H P on all rows, columns k+1..; Z <- Z P
+    // H <- H P on all rows, columns k+1..; Z <- Z P (thread per row: the row is read once for
+    // the product and again, from L1, for the update)
     for (int i = t.tid(); i < n; i += t.size()) {
       const cplx<T> y = tau * dotu4(H + (int64_t)i * ld + k + 1, vbuf, m);
       for (int l = 0; l < m; ++l) H[i * ld + k + 1 + l] -= mul_conj(y, vbuf[l]);
@@ -307,6 +308,35 @@ KHP_HD void givens(cplx<T> x, cplx<T> y, T& c, cplx<T>& s, cplx<T>& r) {
   c = ax / rho;
   s = ph * conj(y) * (T(1) / rho);
   r = ph * rho;
+}
+
+// FP32 form with reciprocal square roots instead of hypot and divisions (the rotation sits on
+// the serial chain of the QR sweep): rho^2 = |x|^2 + |y|^2 in FP32 (the matrices here are far
+// from the FP32 overflow / underflow range; a |x|^2 or |y|^2 that underflows to 0 is treated as
+// an exact zero).  Unitary to FP32 rounding.
+KHP_HD float khp_rsqrt(float v) {
+#ifdef __CUDA_ARCH__
+  return rsqrtf(v);
+#else
+  return 1.0f / std::sqrt(v);
+#endif
+}
+template <>
+KHP_HD void givens<float>(cplx<float> x, cplx<float> y, float& c, cplx<float>& s, cplx<float>& r) {
+  const float ax2 = x.re * x.re + x.im * x.im, ay2 = y.re * y.re + y.im * y.im;
+  if (ay2 == 0.f) { c = 1.f; s = mk(0.f); r = x; return; }
+  if (ax2 == 0.f) {
+    const float iy = khp_rsqrt(ay2);
+    c = 0.f;
+    s = conj(y) * iy;
+    r = mk(ay2 * iy);
+    return;
+  }
+  const float t2 = ax2 + ay2;
+  const float ir = khp_rsqrt(t2), ia = khp_rsqrt(ax2);
+  c = ax2 * ia * ir;                 // |x| / rho
+  s = x * conj(y) * (ia * ir);       // (x / |x|) conj(y) / rho
+  r = x * (t2 * ir * ia);            // (x / |x|) rho
 }
 
 template <class Team, typename T>
@@ -547,6 +577,8 @@ KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z
   if (t.tid() == 0) {
     sh->bi[2] = n - 1;  // hi
     sh->bi[3] = 0;      // status
+    sh->bi[4] = 0;      // sweeps done (diagnostic)
+    sh->bi[5] = 0;      // rotations done (diagnostic)
   }
   t.sync();
   while (true) {
@@ -578,6 +610,8 @@ KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z
           sh->bi[0] = 2;
         } else {
           const cplx<T> mu = hqr_shift(H, ld, l, hi, its);
+          sh->bi[4] += 1;
+          sh->bi[5] += hi - l;
           sh->bi[0] = 0;
           sh->bi[1] = l;
           sh->bd[0] = (double)mu.re;

@@ -66,6 +66,7 @@ struct GammaPlan {
   cplx<T> *G, *F, *Gb, *P;
   cplx<T> *u, *tmp, *rv, *tv;
   int* pivs;
+  M2 *v0b, *v0ib;  // free-space blocks per problem and harmonic
 };
 
 template <typename T>
@@ -112,6 +113,8 @@ GammaPlan<T> plan_gamma(Arena& a, int64_t batch, int nh, int nlayers, const int*
   p.rv = a.take<cplx<T>>(batch * n * 2);
   p.tv = a.take<cplx<T>>(batch * n * 2);
   p.pivs = a.take<int>(batch * n);
+  p.v0b = a.take<M2>(batch * nh);
+  p.v0ib = a.take<M2>(batch * nh);
   return p;
 }
 
@@ -165,6 +168,7 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
   if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
   const cplx<T> one = mk(T(1)), zero = mk(T(0)), mone = mk(T(-1));
 
+  GT_EW(k_v0_blocks, batch * nh, batch, nh, gx, gy, kp, k0, p.v0b, p.v0ib);
   // ---- modes of every distinct pixmap, and W^-1, V^-1 V0, V0^-1 V ----
   for (size_t m = 0; m < used.size(); ++m) {
     const cd* Cm = reinterpret_cast<const cd*>(conv);
@@ -178,13 +182,13 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     cplx<T>* CWb = p.CW + batch * hn;
     GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m], n, nn, zero, CWt, n, hn, s, p.midx[m]));
     GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m] + hn, n, nn, zero, CWb, n, hn, s, p.midx[m]));
-    GT_EW(k_modes_v_t<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, p.lam[m], p.V[m], status);
+    GT_EW(k_modes_v_t<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, hn, p.lam[m], p.V[m], status);
     GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.lu, n, nn, s));
     GT_TRY(launch_inverse<T>(batch, n, p.lu, n, nn, p.Wi[m], n, nn, p.piv, status, s));
     GT_TRY(launch_copy<T>(batch, n, n, p.V[m], n, nn, p.lu, n, nn, s));
     GT_TRY(launch_inverse<T>(batch, n, p.lu, n, nn, p.Z, n, nn, p.piv, status, s));  // Z = V^-1
-    GT_EW(k_v0_right<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.Z, p.Q0[m]);
-    GT_EW(k_v0inv_left<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.V[m], p.Vt[m]);
+    GT_EW(k_v0_right<T>, batch * nn, batch, nh, p.v0b, p.Z, p.Q0[m]);
+    GT_EW(k_v0inv_left<T>, batch * nn, batch, nh, p.v0ib, p.V[m], p.Vt[m]);
   }
   // ---- homogeneous media blocks ----
   GT_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
@@ -212,7 +216,8 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
       GT_EW(k_diff_sum<T>, batch * nn, batch * nn, p.F, p.Gb, p.lu1[l]);  // lu1 = F - G, F <- F + G
       GT_TRY(launch_getrf<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
       GT_TRY(launch_getrs_right<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], p.F, n, nn, n, s));  // rho
-      GT_EW(k_xmx_t<T>, batch * nn, batch, n, p.lam[m], depth_of(l), k0, p.F);                  // rho_L
+      GT_EW(k_xvec<T>, batch * n, batch, n, p.lam[m], depth_of(l), k0, p.u);                      // scratch
+      GT_EW(k_xmx_t<T>, batch * nn, batch, n, p.u, p.F);                                           // rho_L
       GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.Gb, n, nn, s));
       GT_TRY(launch_gemm<T>(batch, n, n, n, one, p.W[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));    // P1
       GT_TRY(launch_copy<T>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));

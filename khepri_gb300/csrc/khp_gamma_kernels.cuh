@@ -103,13 +103,15 @@ __global__ void k_sqrt_lam_t(int64_t count, cplx<T>* lam) {
     lam[e] = to_t<T>(csqrt(to_d(lam[e])));
 }
 
-// V = Q W / lam (alternative.py:167-176), CWt = C W_top, CWb = C W_bottom.
+// V = Q W / lam (alternative.py:167-176), CWt = C W_top, CWb = C W_bottom ([nh][n] each, batch
+// stride cws).
 template <typename T>
 __global__ void k_modes_v_t(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
                             const double* k0, const cplx<T>* __restrict__ W, const cplx<T>* __restrict__ CWt,
-                            const cplx<T>* __restrict__ CWb, const cplx<T>* __restrict__ lam, cplx<T>* V, int* status) {
+                            const cplx<T>* __restrict__ CWb, int64_t cws, const cplx<T>* __restrict__ lam, cplx<T>* V,
+                            int* status) {
   const int n = 2 * nh;
-  const int64_t nn = (int64_t)n * n, hn = (int64_t)nh * n;
+  const int64_t nn = (int64_t)n * n, hn = cws;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int rc = (int)(e % nn);
@@ -128,10 +130,25 @@ __global__ void k_modes_v_t(int64_t batch, int nh, const double* gx, const doubl
   }
 }
 
-// out = A V0 (V0: free-space modes, one 2x2 block per harmonic).
+// Free-space V0 blocks and their inverses per problem and harmonic, [batch][nh] (FP64; computed
+// once so that the element-wise products below do no square roots or divisions).
+__global__ void k_v0_blocks(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
+                            const double* k0, M2* v0, M2* v0i) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nh; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nh;
+    const int g = (int)(e % nh);
+    cd kx, ky;
+    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
+    const M2 v = phys::v0_block(kx, ky);
+    v0[e] = v;
+    v0i[e] = phys::inv2(v);
+  }
+}
+
+// out = A V0 (V0: free-space modes, one 2x2 block per harmonic, from k_v0_blocks).
 template <typename T>
-__global__ void k_v0_right(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
-                           const double* k0, const cplx<T>* __restrict__ A, cplx<T>* out) {
+__global__ void k_v0_right(int64_t batch, int nh, const M2* __restrict__ v0b, const cplx<T>* __restrict__ A,
+                           cplx<T>* out) {
   const int n = 2 * nh;
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
@@ -139,9 +156,7 @@ __global__ void k_v0_right(int64_t batch, int nh, const double* gx, const double
     const int rc = (int)(e % nn);
     const int r = rc / n, c = rc % n;
     const int g = c % nh, cb = c / nh;
-    cd kx, ky;
-    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
-    const M2 v0 = phys::v0_block(kx, ky);
+    const M2& v0 = v0b[b * nh + g];
     const cd a0 = to_d(A[b * nn + (int64_t)r * n + g]), a1 = to_d(A[b * nn + (int64_t)r * n + nh + g]);
     out[e] = to_t<T>(a0 * blk(v0, 0, cb) + a1 * blk(v0, 1, cb));
   }
@@ -149,8 +164,8 @@ __global__ void k_v0_right(int64_t batch, int nh, const double* gx, const double
 
 // out = V0^-1 A.
 template <typename T>
-__global__ void k_v0inv_left(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
-                             const double* k0, const cplx<T>* __restrict__ A, cplx<T>* out) {
+__global__ void k_v0inv_left(int64_t batch, int nh, const M2* __restrict__ v0ib, const cplx<T>* __restrict__ A,
+                             cplx<T>* out) {
   const int n = 2 * nh;
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
@@ -158,9 +173,7 @@ __global__ void k_v0inv_left(int64_t batch, int nh, const double* gx, const doub
     const int rc = (int)(e % nn);
     const int r = rc / n, c = rc % n;
     const int g = r % nh, rb = r / nh;
-    cd kx, ky;
-    phys::kvec(kp, k0, gx, gy, b, g, kx, ky);
-    const M2 vi = phys::inv2(phys::v0_block(kx, ky));
+    const M2& vi = v0ib[b * nh + g];
     const cd a0 = to_d(A[b * nn + (int64_t)g * n + c]), a1 = to_d(A[b * nn + (int64_t)(nh + g) * n + c]);
     out[e] = to_t<T>(blk(vi, rb, 0) * a0 + blk(vi, rb, 1) * a1);
   }
@@ -251,17 +264,24 @@ __global__ void k_diff_sum(int64_t count, cplx<T>* f, const cplx<T>* __restrict_
   }
 }
 
-// rho <- X rho X, X = exp(-lam k0 d).
+// x = exp(-lam k0 d) per problem and mode, [batch][n].
 template <typename T>
-__global__ void k_xmx_t(int64_t batch, int n, const cplx<T>* __restrict__ lam, DepthSel depth, const double* k0,
-                        cplx<T>* M) {
+__global__ void k_xvec(int64_t batch, int n, const cplx<T>* __restrict__ lam, DepthSel depth, const double* k0,
+                       cplx<T>* xv) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / n;
+    xv[e] = to_t<T>(cexp(-(to_d(lam[e]) * (depth.at(b) * k0[b]))));
+  }
+}
+
+// rho <- X rho X with X = diag(xv) from k_xvec.
+template <typename T>
+__global__ void k_xmx_t(int64_t batch, int n, const cplx<T>* __restrict__ xv, cplx<T>* M) {
   const int64_t nn = (int64_t)n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = e / nn;
     const int rc = (int)(e % nn);
-    const double dk = depth.at(b) * k0[b];
-    const cd xi = cexp(-(to_d(lam[b * n + rc / n]) * dk)), xj = cexp(-(to_d(lam[b * n + rc % n]) * dk));
-    M[e] = to_t<T>(xi * to_d(M[e]) * xj);
+    M[e] = xv[b * n + rc / n] * M[e] * xv[b * n + rc % n];
   }
 }
 

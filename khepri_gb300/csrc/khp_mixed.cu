@@ -124,18 +124,31 @@ __global__ void k_eig_update(int64_t batch, int n, const cd* __restrict__ mu_in,
       }
     } else {
       const cf ev = Eb[(int64_t)i * n + j];
-      const cd ed = mk((double)ev.re, (double)ev.im);
       const cd mi = mu_in[b * n + i];
       if (i == j) {
-        mu_out[b * n + i] = mi + ed;
+        mu_out[b * n + i] = mi + mk((double)ev.re, (double)ev.im);
       } else {
+        // the difference in FP64 (no cancellation for close pairs), the quotient in FP32
         const cd mj = mu_in[b * n + j];
         const cd dd = mj - mi;
-        if (cabs(dd) > 1e-5 * (cabs(mi) + cabs(mj))) out = cdiv(ed, dd);
+        const cf d32 = mk((float)dd.re, (float)dd.im);
+        const float ad = cabs(d32);
+        const float am = cabs(mk((float)mi.re, (float)mi.im)) + cabs(mk((float)mj.re, (float)mj.im));
+        if (ad > 1e-5f * am) {
+          const cf q = cdiv(ev, d32);
+          F[e] = q;
+          continue;
+        }
       }
     }
     F[e] = mk((float)out.re, (float)out.im);
   }
+}
+
+// A64 += D32
+__global__ void k_accumulate(int64_t count, cd* A64, const cf* __restrict__ D) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    A64[e] += mk((double)D[e].re, (double)D[e].im);
 }
 
 // W64 += D32 ; W32 = round(W64)
@@ -222,6 +235,8 @@ struct Table {
   const M2* trn;
   const cf* inv0;  // (I - S22_inc Gamma_0)^-1
   const cf* gam;   // Gamma at gaps 0..L: [L+1][batch][n][n]
+  const M2* v0b;   // free-space V0 and V0^-1 blocks per problem and harmonic, [batch][nh]
+  const M2* v0ib;
   Elem e[kMaxLayers];
   MapPtrs m[kMaxLayers];
 };
@@ -344,9 +359,7 @@ __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* 
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
       const int g = i % nh, rb = i / nh;
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 v0 = phys::v0_block(kx, ky);
+      const M2 v0 = tb.v0b[b * nh + g];
       const cd dl0 = cml[2 * g + c] - cpl[2 * g + c], dl1 = cml[2 * (nh + g) + c] - cpl[2 * (nh + g) + c];
       const cd dr0 = cmr[2 * g + c] - cpr[2 * g + c], dr1 = cmr[2 * (nh + g) + c] - cpr[2 * (nh + g) + c];
       r1[e] = r1[e] - cpl[e] - cml[e];
@@ -444,9 +457,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
       const int g = i % nh, rb = i / nh;
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 v0 = phys::v0_block(kx, ky);
+      const M2 v0 = tb.v0b[b * nh + g];
       const cd v0s = blk(v0, rb, 0) * ld2(sj, g, c) + blk(v0, rb, 1) * ld2(sj, nh + g, c);
       const cd a = f3[e] - ld2(sj, i, c);
       const cd bb = f4[e] - v0s;
@@ -486,9 +497,7 @@ __global__ void __launch_bounds__(256) k_stack_sweep(Table tb, const double* gx,
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
       const int g = i % nh, rb = i / nh;
-      cd kx, ky;
-      phys::kvec(kp, k0v, gx, gy, b, g, kx, ky);
-      const M2 vi = phys::inv2(phys::v0_block(kx, ky));
+      const M2 vi = tb.v0ib[b * nh + g];
       const cd a1 = ld2(T0, i, c) + f1p[e];
       const cd u0 = ld2(T1, g, c) + f2p[2 * g + c], u1 = ld2(T1, nh + g, c) + f2p[2 * (nh + g) + c];
       const cd a2 = blk(vi, rb, 0) * u0 + blk(vi, rb, 1) * u1;
@@ -745,6 +754,8 @@ struct MixedPlan {
   // copies of kp, k0 and a per-matrix status
   double *kpx, *k0x;
   int* statx;
+  M2 *v0b, *v0ib;  // free-space blocks per matrix of the modes batch ([batch][nh] first: per problem)
+  cf* xv;          // [batch][n] propagator diagonal
   // per layer
   std::vector<cf*> inv1, inv2, zr;
   std::vector<M2*> blocks;
@@ -793,6 +804,9 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.kpx = a.take<double>(bm * 4);
   p.k0x = a.take<double>(bm);
   p.statx = a.take<int>(bm);
+  p.v0b = a.take<M2>(bm * nh);
+  p.v0ib = a.take<M2>(bm * nh);
+  p.xv = a.take<cf>(batch * n);
   for (int l = 0; l < L; ++l) {
     p.inv1.push_back(a.take<cf>(batch * nn));
     p.zr.push_back(a.take<cf>(batch * nn));
@@ -1006,8 +1020,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
             midx + (int64_t)m * batch, sx + (int64_t)m * batch);
     MX_EW(k_assemble_pq_t<float>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32);
     MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s));
-    // Refinement steps: R = M W - W mu in FP64, E = W0^-1 R (FP32 inverse of the FP32 solver's
-    // W0, held in Wi until the final inverse), mu += diag(E), W += W F.
+    // Refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 inverse of the current W, held
+    // in Wi until the final inverse), mu += diag(E), W += W F.
     MX_EW(k_assemble_pq_t<double>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M64);
     MX_EW(k_to_double, bm * nn, bm * nn, W32, W64);
     MX_EW(k_to_double, bm * n, bm * n, lam32, p.mu64);
@@ -1015,8 +1029,20 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
+    // M W in FP64 for the first and the last step; in between, after W += dW = W32 F, it is
+    // updated as M W += round(M W) F in FP32.  That update is only FP32-accurate where F is large
+    // (close eigenvalues), so the last step's residual is formed from scratch.  (The structured
+    // product P (Q W) costs less but cancels terms of size k^4 / eps for the evanescent orders.)
     for (int step = 0; step < kEigSteps; ++step) {
-      MX_TRY(launch_gemm<double>(bm, n, n, n, done, p.M64, n, nn, W64, n, nn, dzero, p.MW64, n, nn, s));
+      const bool last = step == kEigSteps - 1;
+      if (step > 0) {
+        // E with the inverse of the current W: the first step can rotate the vectors of a close
+        // pair by ~1e-3, after which W0^-1 would make the later steps converge only linearly
+        MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
+        MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
+      }
+      if (step == 0 || last)
+        MX_TRY(launch_gemm<double>(bm, n, n, n, done, p.M64, n, nn, W64, n, nn, dzero, p.MW64, n, nn, s));
       MX_EW(k_eig_residual, bm * nn, bm, n, p.MW64, W64, mu_a, p.E32);
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
       k_find_pairs<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
@@ -1025,24 +1051,32 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_EW(k_eig_update, bm * nn, bm, n, mu_a, p.Z32, p.M32, mu_b, p.pair);  // M32 <- F
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, W32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
       MX_EW(k_add_correction, bm * nn, bm * nn, W64, p.Z32, W32);
+      if (!last) {
+        MX_EW(k_round, bm * nn, bm * nn, p.MW64, p.E32);
+        MX_TRY(launch_gemm<float>(bm, n, n, n, one, p.E32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
+        MX_EW(k_accumulate, bm * nn, bm * nn, p.MW64, p.Z32);
+      }
       std::swap(mu_a, mu_b);
     }
     MX_EW(k_sqrt_mu, bm * n, bm * n, mu_a, lam64, lam32);
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
-    cd* CWb = p.CW64 + bm * hn;
-    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64, n, nn, dzero, CWt, n, hn, s, midx));
-    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64 + hn, n, nn, dzero, CWb, n, hn, s, midx));
-    MX_EW(k_modes_v_t<double>, bm * nn, bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, lam64, V64, sx);
+    cd* CWb = p.CW64 + hn;
+    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64, n, nn, dzero, CWt, n, nn, s, midx));
+    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64 + hn, n, nn, dzero, CWb, n, nn, s, midx));
+    MX_EW(k_modes_v_t<double>, bm * nn, bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, nn, lam64, V64, sx);
     MX_EW(k_round, bm * nn, bm * nn, V64, V32);
     // FP32 inverses and V0 products
     MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     MX_TRY(launch_copy<float>(bm, n, n, V32, n, nn, p.lu32, n, nn, s));
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Vi, n, nn, p.piv, sx, s));
-    MX_EW(k_v0_right<float>, bm * nn, bm, nh, gx, gy, kpx, k0x, Vi, p.Q0[0]);
-    MX_EW(k_v0inv_left<float>, bm * nn, bm, nh, gx, gy, kpx, k0x, V32, p.Vt[0]);
+    MX_EW(k_v0_blocks, bm * nh, bm, nh, gx, gy, kpx, k0x, p.v0b, p.v0ib);
+    MX_EW(k_v0_right<float>, bm * nn, bm, nh, p.v0b, Vi, p.Q0[0]);
+    MX_EW(k_v0inv_left<float>, bm * nn, bm, nh, p.v0ib, V32, p.Vt[0]);
     MX_EW(k_or_status, batch, batch, S, sx, status);
+  } else {
+    MX_EW(k_v0_blocks, batch * nh, batch, nh, gx, gy, kp, k0, p.v0b, p.v0ib);
   }
   // ---- homogeneous blocks (FP64) ----
   MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
@@ -1072,7 +1106,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.F, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));  // rho
       MX_TRY(launch_copy<float>(batch, n, n, p.zr[l], n, nn, p.F, n, nn, s));
-      MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.lam32[m], depth_of(l), k0, p.F);
+      MX_EW(k_xvec<float>, batch * n, batch, n, p.lam32[m], depth_of(l), k0, p.xv);
+      MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.xv, p.F);
       MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.Gb, n, nn, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));
       MX_TRY(launch_copy<float>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));
@@ -1093,6 +1128,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   tb.trn = p.trn;
   tb.inv0 = p.inv0;
   tb.gam = p.gam;
+  tb.v0b = p.v0b;
+  tb.v0ib = p.v0ib;
   for (int l = 0; l < L; ++l) {
     Elem& E = tb.e[l];
     E.kind = kinds[l] == 1 ? 1 : 0;

@@ -140,6 +140,67 @@ __global__ void k_convmat_gather(int64_t nmaps, int px, int py, const cd* __rest
   }
 }
 
+// (exp(z) - 1) / z with the nested Taylor series below |z| = 1e-2 (fourier.py:7-20).
+__device__ cd fexpz(cd z) {
+  if (cabs(z) > 1e-2) return cdiv(cexp(z) - mk(1.0), z);
+  const cd one = mk(1.0);
+  cd r = one + z * (1.0 / 7.0);
+  r = one + z * (1.0 / 6.0) * r;
+  r = one + z * (1.0 / 5.0) * r;
+  r = one + z * (1.0 / 4.0) * r;
+  r = one + z * (1.0 / 3.0) * r;
+  return one + z * 0.5 * r;
+}
+
+// Fourier coefficients of analytical layers (layer.py:161-168, fourier.py:23-58, 145-159) in the
+// layout of k_convmat_dft: F[map][dxi][dyi] for |dx| < px, |dy| < py.  The reference evaluates the
+// island transforms on the expanded grid epw = (3 px, 3 py) (1 for a single harmonic), lays the
+// flat result (m fastest) out as an epw[0] x epw[1] array and reads entry (g0x + dx, g0y + dy);
+// the same flat-index arithmetic is used here.  islands: [nisl][8] = map, type (0 disc, 1
+// rectangle), eps re, eps im, params[4]; eps_host: complex [nmaps].
+__global__ void k_convmat_islands(int64_t nmaps, int px, int py, int nisl, const double* __restrict__ islands,
+                                  const cd* __restrict__ eps_host, double b1x, double b1y, double b2x, double b2y,
+                                  double sigma, cd* F) {
+  const int ndx = 2 * px - 1, ndy = 2 * py - 1;
+  const int ex = px > 1 ? 3 * px : 1, ey = py > 1 ? 3 * py : 1;
+  const int64_t total = nmaps * (int64_t)ndx * ndy;
+  const double pi = 3.14159265358979323846;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t map = e / ((int64_t)ndx * ndy);
+    const int k = (int)(e % ((int64_t)ndx * ndy));
+    const int dx = k / ndy - (px - 1), dy = k % ndy - (py - 1);
+    const int a = ex / 2 + dx, b = ey / 2 + dy;
+    const int flat = a * ey + b;
+    const int i = flat % ex, j = flat / ex;
+    const double m = i - (ex - 1) / 2, nn = j - (ey - 1) / 2;
+    const double gx = m * b1x + nn * b2x, gy = m * b1y + nn * b2y;
+    const cd host = eps_host[map];
+    cd acc = flat == (ex * ey - 1) / 2 ? host : mk(0.0);
+    for (int s = 0; s < nisl; ++s) {
+      const double* isl = islands + 8 * s;
+      if ((int64_t)isl[0] != map) continue;
+      const cd coef = mk(isl[2], isl[3]) - host;
+      cd tr;
+      if (isl[1] == 0.0) {  // disc (center0, center1, radius)
+        const double r = isl[6];
+        const double norm = sqrt(gx * gx + gy * gy) * r;
+        if (fabs(gx) <= 1e-8 && fabs(gy) <= 1e-8) {
+          tr = mk(pi * r * r / sigma);
+        } else {
+          const double ph = -(isl[4] * gx + isl[5] * gy);
+          tr = mk(cos(ph), sin(ph)) * (pi * r * r / sigma * 2.0 * j1(norm) / norm);
+        }
+      } else {  // rectangle (ll0, ll1, ur0, ur1)
+        const double w = isl[6] - isl[4], h = isl[7] - isl[5];
+        const double ph = -(isl[4] * gx + isl[5] * gy);
+        tr = fexpz(mk(0.0, -gx * w)) * fexpz(mk(0.0, -gy * h)) * mk(cos(ph), sin(ph)) * (w * h / sigma);
+      }
+      acc += coef * tr;
+    }
+    F[e] = acc;
+  }
+}
+
 // Adjoint of k_convmat_gather: dF[map][dx][dy] = sum of dC over the (r, c) with
 // p_r - p_c = dx, q_r - q_c = dy (fixed order).
 __global__ void k_convmat_bwd_gather(int64_t nmaps, int px, int py, const cd* __restrict__ dC, cd* dF) {
@@ -630,6 +691,32 @@ int khp_convmat(int64_t nmaps, int64_t nx, int64_t ny, const double* eps, int32_
       cudaFuncSetAttribute(k_convmat_dft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
   k_convmat_dft<<<dim3(2 * px - 1, (unsigned)nmaps), 256, smem, s>>>(nx, ny, (const cd*)eps, px, py, w.F);
+  count_launches(1);
+  const int64_t total = nmaps * (int64_t)px * py * px * py;
+  k_convmat_gather<<<ew_grid(total), 256, 0, s>>>(nmaps, px, py, w.F, (cd*)conv);
+  count_launches(1);
+  return cuda_status();
+}
+
+size_t khp_convmat_islands_workspace(int64_t nmaps, int32_t px, int32_t py) {
+  Arena a{nullptr, 0};
+  plan_conv(a, nmaps, px, py);
+  return a.off;
+}
+
+int khp_convmat_islands(int64_t nmaps, int32_t px, int32_t py, int32_t nislands, const double* islands,
+                        const double* eps_host, double b1x, double b1y, double b2x, double b2y, double cell_area,
+                        double* conv, void* workspace, size_t ws_bytes, void* stream) {
+  if (nmaps < 0 || px < 1 || py < 1 || (px % 2) == 0 || (py % 2) == 0 || nislands < 0 || !eps_host || !conv ||
+      (nislands > 0 && !islands) || !(cell_area > 0.0))
+    return KHP_ERR_INVALID_ARG;
+  if (nmaps == 0) return KHP_OK;
+  Arena a{static_cast<char*>(workspace), ws_bytes};
+  ConvWs w = plan_conv(a, nmaps, px, py);
+  if (!a.ok || !workspace) return KHP_ERR_WORKSPACE;
+  cudaStream_t s = as_stream(stream);
+  k_convmat_islands<<<ew_grid(nmaps * (int64_t)(2 * px - 1) * (2 * py - 1)), 256, 0, s>>>(
+      nmaps, px, py, nislands, islands, (const cd*)eps_host, b1x, b1y, b2x, b2y, cell_area, w.F);
   count_launches(1);
   const int64_t total = nmaps * (int64_t)px * py * px * py;
   k_convmat_gather<<<ew_grid(total), 256, 0, s>>>(nmaps, px, py, w.F, (cd*)conv);

@@ -134,7 +134,35 @@ def workspace(nbytes, device):
     return buf
 
 
+class AnalyticalMap:
+    """Permittivity of an analytical layer (Layer.analytical, khepri/layer.py:121-129): islands
+    as Drawing.islands() describes them (dicts with "type" "disc" | "rectangle", "params",
+    "epsilon") in a host medium.  Used in place of a pixmap; its convolution matrix comes from
+    the closed-form island transforms (khp_convmat_islands)."""
+
+    _TYPES = {"disc": 0, "rectangle": 1}
+
+    def __init__(self, islands, eps_host):
+        self.islands = [dict(type=i["type"], params=list(i["params"]), epsilon=i["epsilon"]) for i in islands]
+        self.eps_host = complex(eps_host)
+        for i in self.islands:
+            if i["type"] not in self._TYPES:
+                raise NotImplementedError(f"island type {i['type']!r}")
+        self.key = "islands:" + repr((self.islands, self.eps_host))
+
+    def rows(self, map_index=0):
+        """[n][8] rows of khp_convmat_islands."""
+        out = []
+        for i in self.islands:
+            p = list(i["params"]) + [0.0] * (4 - len(i["params"]))
+            e = complex(i["epsilon"])
+            out.append([map_index, self._TYPES[i["type"]], e.real, e.imag] + p)
+        return np.asarray(out, dtype=np.float64).reshape(-1, 8)
+
+
 def _digest(a):
+    if isinstance(a, AnalyticalMap):
+        return a.key
     a = np.ascontiguousarray(a)
     return hashlib.blake2b(a.tobytes(), digest_size=16).hexdigest() + str(a.shape) + str(a.dtype)
 
@@ -158,6 +186,7 @@ class StructureGPU:
         self.nh = self.pw[0] * self.pw[1]
         self.n = 2 * self.nh
         self.device = torch.device(device)
+        self.lattice = np.asarray(lattice, dtype=float)
         g = g_vectors(self.pw, lattice)
         self.gx = torch.tensor(g[0], dtype=F64, device=self.device)
         self.gy = torch.tensor(g[1], dtype=F64, device=self.device)
@@ -169,16 +198,26 @@ class StructureGPU:
         hit = self._maps.get(key)
         if hit is not None:
             return hit
-        eps = torch.as_tensor(np.asarray(eps_map), device=self.device).to(C128).contiguous()
-        nx, ny = eps.shape
         px, py = self.pw
         nh = self.nh
         conv = torch.empty((1, nh, nh), dtype=C128, device=self.device)
         lib = _capi.load()
         sp = _capi.stream_ptr()
-        ws = workspace(lib.khp_convmat_workspace(1, px, py), self.device)
-        _capi.check(lib.khp_convmat(1, nx, ny, _capi.ptr(eps), px, py, _capi.ptr(conv), _capi.ptr(ws), ws.numel(), sp),
-                    "khp_convmat")
+        if isinstance(eps_map, AnalyticalMap):
+            rows = torch.tensor(eps_map.rows(), dtype=F64, device=self.device)
+            host = torch.tensor([eps_map.eps_host], dtype=C128, device=self.device)
+            b = reciprocal_basis(self.lattice)
+            area = abs(self.lattice[0, 0] * self.lattice[1, 1] - self.lattice[0, 1] * self.lattice[1, 0])
+            ws = workspace(lib.khp_convmat_islands_workspace(1, px, py), self.device)
+            _capi.check(lib.khp_convmat_islands(1, px, py, rows.shape[0], _capi.ptr(rows), _capi.ptr(host),
+                                                float(b[0, 0]), float(b[0, 1]), float(b[1, 0]), float(b[1, 1]), area,
+                                                _capi.ptr(conv), _capi.ptr(ws), ws.numel(), sp), "khp_convmat_islands")
+        else:
+            eps = torch.as_tensor(np.asarray(eps_map), device=self.device).to(C128).contiguous()
+            nx, ny = eps.shape
+            ws = workspace(lib.khp_convmat_workspace(1, px, py), self.device)
+            _capi.check(lib.khp_convmat(1, nx, ny, _capi.ptr(eps), px, py, _capi.ptr(conv), _capi.ptr(ws), ws.numel(),
+                                        sp), "khp_convmat")
         ic = torch.empty_like(conv)
         hx = torch.empty_like(conv)
         hy = torch.empty_like(conv)

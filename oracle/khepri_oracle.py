@@ -387,6 +387,11 @@ class OracleCrystal:
     def add_layer_pixmap(self, name, epsilon, depth):
         self.layers[name] = SimpleNamespace(kind="pixmap", eps=epsilon, depth=depth, fields=False)
 
+    def add_layer_analytical(self, name, epsilon, epsilon_host, depth):
+        """crystal.py:119-123: islands description (Drawing.islands()) and host permittivity."""
+        self.layers[name] = SimpleNamespace(kind="analytical", eps=epsilon, eps_host=epsilon_host, depth=depth,
+                                            fields=False)
+
     def set_device(self, layers_stack, fields_mask=False):
         """crystal.py:131-164."""
         self.device_stack = list(layers_stack)
@@ -416,8 +421,9 @@ class OracleCrystal:
 
     def _solve_layer(self, layer, kx, ky, w0, v0, k0):
         """layer.py:145-194."""
-        if layer.kind == "pixmap":
-            conv = convolution_matrix(layer.eps, self.pw)
+        if layer.kind in ("pixmap", "analytical"):
+            conv = (convolution_matrix(layer.eps, self.pw) if layer.kind == "pixmap" else
+                    analytical_convolution_matrix(layer.eps, layer.eps_host, self.pw, self.lattice))
             layer.IC = np.linalg.inv(conv)
             layer.W, layer.V, layer.L = solve_structured_layer(kx, ky, conv)
             layer.S = build_scatmat(layer.W, layer.V, w0, v0, layer.L, layer.depth, k0)
@@ -531,3 +537,151 @@ def solve_rt(pw, layers, stack, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, 
     cl.set_source(wavelength, te, tm, theta, phi, kp)
     cl.solve()
     return cl.poynting_flux_end(only_total)
+
+
+# ---------------------------------------------------------------------------------------
+# Twisted bilayers: product expansions and extended layers (khepri/expansion.py:52-73,
+# khepri/extension.py:10-126)
+# ---------------------------------------------------------------------------------------
+def rotation_matrix(angle_rad):
+    """tools.py:23-24."""
+    c, s = math.cos(angle_rad), math.sin(angle_rad)
+    return np.array([[c, -s], [s, c]])
+
+
+def twisted_g_vectors(g1, g2):
+    """Minkowski sum of two expansions, expansion.py:60-74: index i = i1 * N2 + i2 with g = g1[i1] +
+    g2[i2] (the left operand's vectors vary slowest)."""
+    return (g1[:, :, None] + g2[:, None, :]).reshape(2, -1)
+
+
+def joint_subspace(mats, kind):
+    """Scatter N matrices of size 2N (one per shift m) into the 2N^2 space; extension.py:10-49.
+
+    Within each polarisation quadrant, kind 0 puts element (a, b) of matrix m at
+    (m N + a, m N + b) and kind 1 at (a N + m, b N + m)."""
+    n_base = mats[0].shape[0] // 2
+    N = n_base
+    out = np.zeros((2 * N * N, 2 * N * N), dtype=mats[0].dtype)
+    a = np.arange(N)
+    for m, mat in enumerate(mats):
+        idx = m * N + a if kind == 0 else a * N + m
+        for bi in range(2):
+            for bj in range(2):
+                out[np.ix_(bi * N * N + idx, bj * N * N + idx)] = mat[bi * N:(bi + 1) * N, bj * N:(bj + 1) * N]
+    return out
+
+
+def joint_subspace_s(smats, kind):
+    """The four blocks of extended S-matrices; extension.py:52-62."""
+    return np.array([[joint_subspace([s[i, j] for s in smats], kind) for j in range(2)] for i in range(2)])
+
+
+def _base_layer_s(layer, pw, gvec, kp, wavelength):
+    """S of one base-expansion layer at in-plane k (layer.py:145-194)."""
+    kx, ky, _ = k_vectors(gvec, kp, wavelength)
+    w0, v0 = free_space_eigenmodes(kx, ky)
+    k0 = TWOPI / wavelength
+    kind, eps, depth = layer
+    if kind == "pixmap":
+        w, v, lam = solve_structured_layer(kx, ky, convolution_matrix(eps, pw))
+        return build_scatmat(w, v, w0, v0, lam, depth, k0)
+    if kind == "uniform":
+        w, v, lam = solve_uniform_layer(kx, ky, eps)
+        return build_scatmat(w, v, w0, v0, lam, depth, k0)
+    if kind == "inc":
+        return scattering_reflection(kx, ky, w0, v0, eps)[0]
+    return scattering_transmission(kx, ky, w0, v0, eps)[0]
+
+
+def twisted_solve_rt(pw, lattice, angle_rad, lower, gap, upper, wavelength, te=1.0, tm=1.0, kp=(0.0, 0.0),
+                     epsi=1.0, epse=1.0):
+    """R, T of a twisted bilayer as the reference's extended crystal computes them
+    (examples/crystal_api/twisted_phc.py:35-57 with crystal.py:180-206, 363-396):
+    the incidence half-space and ``lower`` layers use the base expansion e1 (lattice), the
+    ``upper`` layers and the emergence half-space use e2 = e1 rotated by ``angle_rad``; every such
+    layer's extended S-matrix is the joint subspace of its base solves at kp + g for every g of
+    the other expansion (extension.py:82-111); ``gap`` layers are uniform layers of the product
+    expansion.  Layers: ("pixmap", eps_map, depth) | ("uniform", eps, depth)."""
+    lat = lattice_vectors(lattice) if isinstance(lattice, str) else np.asarray(lattice)
+    g1 = g_vectors(pw, lat)
+    g2 = rotation_matrix(angle_rad) @ g1
+    gsum = twisted_g_vectors(g1, g2)
+    N = pw[0] * pw[1]
+    kp = np.asarray(kp, dtype=complex)
+
+    def extended(layer, on_e1):
+        # base over e1: shifts from e2, kind 1; base over e2: shifts from e1, kind 0
+        gb, gs, kind = (g1, g2, 1) if on_e1 else (g2, g1, 0)
+        return joint_subspace_s([_base_layer_s(layer, pw, gb, kp + gs[:, m], wavelength) for m in range(N)], kind)
+
+    smats = [extended(("inc", epsi, 0.0), True)]
+    smats += [extended(l, True) for l in lower]
+    kx, ky, _ = k_vectors(gsum, kp, wavelength)
+    w0, v0 = free_space_eigenmodes(kx, ky)
+    k0 = TWOPI / wavelength
+    for kind, eps, depth in gap:
+        w, v, lam = solve_uniform_layer(kx, ky, eps)
+        smats.append(build_scatmat(w, v, w0, v0, lam, depth, k0))
+    smats += [extended(l, False) for l in upper]
+    smats.append(extended(("trn", epse, 0.0), False))
+    _, _, stot = stack_layers(smats, [False] * len(smats))
+    kzi = np.conj(cmath.sqrt(k0 ** 2 * epsi - kp[0] ** 2 - kp[1] ** 2))
+    inc = incident((N, N), te, tm, (kp[0], kp[1], kzi))
+    t = poynting_fluxes(gsum, stot[1, 0] @ inc, kp, wavelength, epsi, epse)
+    r = poynting_fluxes(gsum, stot[0, 0] @ inc, kp, wavelength, epsi, epsi)
+    return r[0].real, t[0].real, stot
+
+
+# ---------------------------------------------------------------------------------------
+# Analytical layers: closed-form Fourier coefficients of islands (khepri/layer.py:161-168,
+# khepri/fourier.py:7-68, 145-159)
+# ---------------------------------------------------------------------------------------
+def _fexpz(z):
+    """(exp(z) - 1) / z with the reference's series below |z| = 1e-2; fourier.py:7-20."""
+    z = np.asarray(z, dtype=complex)
+    out = np.empty_like(z)
+    big = np.abs(z) > 1e-2
+    out[big] = (np.exp(z[big]) - 1.0) / z[big]
+    s = z[~big]
+    out[~big] = 1 + s / 2.0 * (1 + s / 3.0 * (1 + s / 4.0 * (1 + s / 5.0 * (1 + s / 6.0 * (1 + s / 7)))))
+    return out
+
+
+def island_transform(island, gx, gy, sigma):
+    """2-D Fourier transform of one island at (gx, gy); fourier.py:23-58 (rectangle, disc)."""
+    kind, p = island["type"], island["params"]
+    if kind == "rectangle":
+        ll0, ll1, ur0, ur1 = p
+        a, b = ur0 - ll0, ur1 - ll1
+        return a * b / sigma * _fexpz(-1j * gx * a) * _fexpz(-1j * gy * b) * np.exp(-1j * (ll0 * gx + ll1 * gy))
+    if kind == "disc":
+        from scipy import special
+        c0, c1, r = p
+        norm = np.sqrt(gx * gx + gy * gy) * r
+        at0 = np.isclose(gx, 0.0) & np.isclose(gy, 0.0)
+        out = np.zeros_like(gx, dtype=complex)
+        nz = ~at0
+        out[nz] = np.pi * r ** 2 / sigma * 2 * np.exp(-1j * (c0 * gx[nz] + c1 * gy[nz])) * special.jv(1.0, norm[nz]) / norm[nz]
+        out[at0] = np.pi * r ** 2 / sigma
+        return out
+    raise NotImplementedError(kind)
+
+
+def analytical_convolution_matrix(islands, eps_host, pw, lattice="square"):
+    """C of an analytical layer: island transforms on the expanded grid (3 Px x 3 Py harmonics,
+    expansion.py:86-92), combined with the host (fourier.py:145-159), the flat array reshaped to
+    that grid as the reference does, then the Toeplitz rule (tools.py:38-56); layer.py:161-168."""
+    lat = lattice_vectors(lattice) if isinstance(lattice, str) else np.asarray(lattice, dtype=float)
+    recip = reciprocal_basis(lat)
+    sigma = abs(lat[0, 0] * lat[1, 1] - lat[0, 1] * lat[1, 0])
+    epw = tuple(e * 3 if e > 1 else 1 for e in pw)
+    idx = expansion_indices(epw)
+    g = np.sum(recip[:, :, None] * idx[:, None], axis=0)
+    gx, gy = g[0], g[1]
+    length = gx.shape[0]
+    eps_g = np.zeros(length, dtype=complex)
+    eps_g[(length - 1) // 2] = eps_host
+    for isl in islands:
+        eps_g += (isl["epsilon"] - eps_host) * island_transform(isl, gx, gy, sigma)
+    return convolution_matrix_fourier(eps_g.reshape(epw), pw)

@@ -188,5 +188,76 @@ def main(ref_root):
     print(f"golden vectors written in {time.time() - t0:.1f} s")
 
 
+def twisted(ref_root):
+    """Twisted bilayer (examples/crystal_api/twisted_phc.py:35-57 with pixmap gratings): extended
+    crystal over e1 + e2, e2 rotated; R, T and the global S at 3x3 base harmonics."""
+    sys.path.insert(0, ROOT)
+    Crystal, Drawing, tools = _import_reference(ref_root)
+    from khepri.expansion import Expansion
+    from khepri.layer import Layer
+    rng = np.random.default_rng(11)
+    x = np.linspace(-0.5, 0.5, 32)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    cases, out = [], []
+    for lattice in ("square", "hexagonal"):
+        for angle_deg, f, d_gap, r in ((7.0, 0.62, 0.25, 0.3), (23.0, 0.71, 0.4, 0.22)):
+            disc = np.where(X ** 2 + Y ** 2 < r ** 2, 4.0, 1.0)
+            lat = Crystal((1, 1), lattice=lattice).lattice
+            e1 = Expansion((3, 3), lattice=lat)
+            e2 = Expansion((3, 3), lattice=lat)
+            e2.rotate(np.deg2rad(angle_deg))
+            cl = Crystal.from_expansion(e1 + e2)
+            etw = cl.expansion
+            cl.add_layer("Sref", Layer.half_infinite(e1, "reflexion", 1), True)
+            cl.add_layer("G1", Layer.pixmap(e1, disc, 0.3), True)
+            cl.add_layer("Gap", Layer.uniform(etw, 1.0, d_gap), False)
+            cl.add_layer("G2", Layer.pixmap(e2, disc, 0.3), True)
+            cl.add_layer("Strans", Layer.half_infinite(e2, "transmission", 1), True)
+            cl.set_device(["G1", "Gap", "G2"], [False] * 3)
+            kp = (0.21 * 2 * np.pi * f, -0.08 * 2 * np.pi * f)
+            cl.set_source(1.0 / f, 1.0, 1.0, kp=kp)
+            cl.solve()
+            R, T = cl.poynting_flux_end()
+            cases.append((0 if lattice == "square" else 1, angle_deg, f, d_gap, r, kp[0], kp[1]))
+            out.append((R, T))
+            if len(out) == 1:
+                S0 = np.asarray(cl.Stot)
+    np.savez_compressed(os.path.join(HERE, "twisted_3x3.npz"), cases=np.array(cases), RT=np.array(out), S0=S0,
+                        n_pix=32)
+
+
+def analytical(ref_root):
+    """Analytical layers (closed-form island transforms, layer.py:161-168): C and R, T of a stack
+    [analytical, uniform, analytical] for square (3x5 harmonics) and hexagonal (5x5) lattices."""
+    sys.path.insert(0, ROOT)
+    Crystal, Drawing, tools = _import_reference(ref_root)
+    out = {}
+    for tag, lattice, pw in (("sq", "square", (3, 5)), ("hex", "hexagonal", (5, 5))):
+        dr = Drawing((64, 64), 1.5)
+        dr.disc((0.1, -0.05), 0.25, 8.0)
+        dr.rectangle((-0.2, 0.15), (0.2, 0.3), 3.0)
+        islands = dr.islands()
+        cl = Crystal(pw, lattice=lattice)
+        cl.add_layer_analytical("A", islands, 1.5, 0.4)
+        cl.add_layer_uniform("U", 2.0, 0.3)
+        cl.set_device(["A", "U", "A"], [False] * 3)
+        RT, C = [], None
+        for f, kx, ky in ((0.45, 0.1, 0.0), (0.62, 0.05, -0.12)):
+            cl.set_source(1.0 / f, 1.0, 1.0, kp=(kx * 2 * np.pi * f, ky * 2 * np.pi * f))
+            cl.solve()
+            RT.append(cl.poynting_flux_end())
+            C = np.asarray(cl.layers["A"].C)
+        out[tag + "_RT"] = np.array(RT)
+        out[tag + "_C"] = C
+        out[tag + "_islands"] = np.array([[0 if i["type"] == "disc" else 1, i["epsilon"]] + list(i["params"]) +
+                                          [0.0] * (4 - len(i["params"])) for i in islands])
+    np.savez_compressed(os.path.join(HERE, "analytical.npz"), **out)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 2 and sys.argv[2] == "analytical":
+        analytical(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "twisted":
+        twisted(sys.argv[1])
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -141,3 +141,47 @@ def test_batched_11x11_points(golden):
     for j, p in enumerate(g["problems"][:2]):
         r, t = _solve(st.pw, st.layers, st.stack, wl[p], 1.0, 0.0, kp=tuple(kp[p]))
         assert abs(r - g["R_te"][j]) < 1e-9 and abs(t - g["T_te"][j]) < 1e-9
+
+
+def test_oracle_twisted_bilayer(golden):
+    """Extended (twisted) crystal: e1 + rotated e2, pixmap gratings on each, uniform gap;
+    reference fixture from examples/crystal_api/twisted_phc.py's construction."""
+    g = golden("twisted_3x3")
+    n_pix = int(g["n_pix"])
+    x = np.linspace(-0.5, 0.5, n_pix)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    for k, (lat, ang, f, dg, r, kx, ky) in enumerate(g["cases"]):
+        disc = np.where(X ** 2 + Y ** 2 < r ** 2, 4.0, 1.0)
+        R, T, S = ko.twisted_solve_rt((3, 3), ["square", "hexagonal"][int(lat)], np.deg2rad(ang),
+                                      [("pixmap", disc, 0.3)], [("uniform", 1.0, dg)], [("pixmap", disc, 0.3)],
+                                      1.0 / f, 1.0, 1.0, kp=(kx, ky))
+        assert abs(R - g["RT"][k, 0]) < 1e-12 and abs(T - g["RT"][k, 1]) < 1e-12
+        if k == 0:
+            np.testing.assert_allclose(S, g["S0"], atol=1e-12)
+
+
+def _islands(rows):
+    out = []
+    for row in rows:
+        t = int(row[0])
+        out.append({"type": ["disc", "rectangle"][t], "params": list(row[2:6] if t == 1 else row[2:5]),
+                    "epsilon": float(row[1])})
+    return out
+
+
+def test_oracle_analytical_layers(golden):
+    """Analytical layers (closed-form disc / rectangle transforms, layer.py:161-168): C exactly and
+    R, T of [A, U, A] against the reference."""
+    g = golden("analytical")
+    for tag, lattice, pw in (("sq", "square", (3, 5)), ("hex", "hexagonal", (5, 5))):
+        isl = _islands(g[tag + "_islands"])
+        np.testing.assert_allclose(ko.analytical_convolution_matrix(isl, 1.5, pw, lattice), g[tag + "_C"], atol=1e-14)
+        cl = ko.OracleCrystal(pw, lattice=lattice)
+        cl.add_layer_analytical("A", isl, 1.5, 0.4)
+        cl.add_layer_uniform("U", 2.0, 0.3)
+        cl.set_device(["A", "U", "A"], False)
+        for k, (f, kx, ky) in enumerate(((0.45, 0.1, 0.0), (0.62, 0.05, -0.12))):
+            cl.set_source(1.0 / f, 1.0, 1.0, kp=(kx * 2 * np.pi * f, ky * 2 * np.pi * f))
+            cl.solve()
+            r, t = cl.poynting_flux_end()
+            assert abs(r - g[tag + "_RT"][k, 0]) < 1e-10 and abs(t - g[tag + "_RT"][k, 1]) < 1e-10
