@@ -406,10 +406,13 @@ __global__ void __launch_bounds__(256) k_stack_sweep_T(Table tb, const double* g
     team_mvT2(t, gam(l), n, T0, T1);  // T3-bar = 1/2 Gamma^T s-bar
     t.sync();
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
-      const int i = e / 2, c = e % 2;
-      const int g = i % nh, rb = i / nh;
       k1b[e] = k1b[e] + T0[e] - T1[e];
       k2b[e] = k2b[e] + T0[e] + T1[e];
+    }
+    t.sync();  // the V0^-T product below reads other threads' k2b entries
+    for (int e = t.tid(); e < 2 * n; e += t.size()) {
+      const int i = e / 2, c = e % 2;
+      const int g = i % nh, rb = i / nh;
       f1[e] += ld2(k1b, i, c);
       const M2 vi = tb.v0ib[b * nh + g];
       const cd z = m2T_apply(vi, rb, g, nh, c, k2b);
