@@ -314,6 +314,20 @@ int khp_fields_idft(int64_t rows, int32_t nh, const double* ff, const double* gx
 long long khp_launch_count(void);
 double khp_probe_fp64_tflops(double* scratch, int64_t scratch_doubles, void* stream);
 
+/*
+ * FP64-accurate batched complex product on the bf16 tensor cores (no counterpart in the
+ * reference; the mixed-precision solve forms its FP64 eigen-residuals and V = Q W this way).
+ * C[b] = A[b] B[b]; A: complex [batch] m x k (row stride lda, batch stride bsA, in complex
+ * elements), B: k x n, C: m x n.  Each operand is split exactly into seven 8-bit digits per row
+ * (A) or column (B) and the 28 leading digit products are summed exactly in FP32/int32; the
+ * error per element is ~2^-55 * 2k * max|A row| * max|B column|, an FP64 product's own bound.
+ * k <= 4096.  Scratch: khp_zgemm_fp64_tc_workspace(batch, m, n, k) bytes.
+ */
+size_t khp_zgemm_fp64_tc_workspace(int64_t batch, int32_t m, int32_t n, int32_t k);
+int khp_zgemm_fp64_tc(int64_t batch, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda, int64_t bsA,
+                      const double* B, int64_t ldb, int64_t bsB, double* C, int64_t ldc, int64_t bsC, void* workspace,
+                      size_t ws_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

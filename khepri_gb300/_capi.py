@@ -72,6 +72,9 @@ _SIGNATURES = {
                                       _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
+    "khp_zgemm_fp64_tc_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_i32]),
+    "khp_zgemm_fp64_tc": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_i64, _c_i64, _c_p, _c_i64, _c_i64,
+                                         _c_p, _c_i64, _c_i64, _c_p, _c_sz, _c_p]),
 }
 
 _lib = None

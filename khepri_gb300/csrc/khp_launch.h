@@ -58,6 +58,30 @@ template <typename T>
 int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
                            int64_t bsI, int* piv, int* info, cudaStream_t s);
 
+// FP64-accurate complex products on the bf16 tensor cores (error-free digit splitting; the
+// result matches an FP64 product to its own rounding bound).  Scratch for the digit arrays:
+// capacities in elements (bf16 digits) and entries (exponents); products over more problems
+// than the capacities hold run in chunks.
+struct OzakiWs {
+  void* ad = nullptr;  // A digits
+  size_t ad_elems = 0;
+  int* ea = nullptr;   // A row exponents
+  size_t ea_n = 0;
+  void* bd = nullptr;  // B digits
+  size_t bd_elems = 0;
+  int* eb = nullptr;   // B column exponents
+  size_t eb_n = 0;
+};
+constexpr int64_t kOzakiMaxChunk = 256;  // problems per chunk (digit arrays: ~5.5 MB per 242 x 242 problem)
+size_t ozaki_a_elems(int m, int k);  // per problem
+size_t ozaki_b_elems(int k, int n);  // per problem
+int ozaki_rows_padded(int m);
+int64_t ozaki_chunk(int64_t batch);  // problems per chunk for a batch (even split, <= kOzakiMaxChunk)
+// C[b] = A[aidx ? aidx[b] : b] B[b] (complex FP64; A m x k, B k x n; aidx optional, device).
+int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64_t lda, int64_t bsA, const int* aidx,
+                const cplx<double>* B, int64_t ldb, int64_t bsB, cplx<double>* C, int64_t ldc, int64_t bsC,
+                const OzakiWs& w, cudaStream_t s);
+
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 
 // Adds k to the process-wide launch counter reported by khp_launch_count().

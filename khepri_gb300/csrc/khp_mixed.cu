@@ -8,7 +8,8 @@
 //      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i); mutually nearest eigenvalues
 //      closer than 3e-3 max|mu| take the exact 2x2 update of their block of E instead (first
 //      order converges slowly there); other pairs closer than 1e-5 relative stay coupled
-//      (second-order error);  V = Q W / lam in FP64;
+//      (second-order error);  V = Q W / lam in FP64.  The FP64 products M W and C W run on the
+//      bf16 tensor cores with exact digit splitting (ozaki_zgemm), FP64-accurate;
 //   2. the reflection-matrix recursion of khp_solve_batched on the FP32-rounded refined modes,
 //      keeping every factor it makes (the explicit inverses, rho, Gamma at every gap, Gamma M^-1),
 //      with every O(n^3) step a blocked LU / inverse or a tiled product;
@@ -766,6 +767,7 @@ struct MixedPlan {
   cf* SW;
   double* corr;  // [2][batch]: correction sizes of the last two refinement rounds
   int* active;   // [batch]: refinement not yet converged
+  OzakiWs oz;    // digit arrays of the FP64-accurate tensor-core products (M W and C W)
 };
 
 MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, int nmaps_used) {
@@ -801,6 +803,18 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.pair = a.take<int>(bm * n);
   p.nearest = a.take<int>(bm * n);
   p.piv = a.take<int>(bm * n);
+  if (nmaps_used > 0) {
+    // sized for M W (n x n x n); the C W products (nh x n, inner nh) need less
+    const size_t ch = (size_t)ozaki_chunk((int64_t)bm);
+    p.oz.ad_elems = ch * ozaki_a_elems((int)n, (int)n);
+    p.oz.ad = a.take<uint16_t>(p.oz.ad_elems);
+    p.oz.ea_n = ch * ozaki_rows_padded((int)n);
+    p.oz.ea = a.take<int>(p.oz.ea_n);
+    p.oz.bd_elems = ch * ozaki_b_elems((int)n, (int)n);
+    p.oz.bd = a.take<uint16_t>(p.oz.bd_elems);
+    p.oz.eb_n = ch * n;
+    p.oz.eb = a.take<int>(p.oz.eb_n);
+  }
   p.kpx = a.take<double>(bm * 4);
   p.k0x = a.take<double>(bm);
   p.statx = a.take<int>(bm);
@@ -1029,7 +1043,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
-    // M W in FP64 for the first and the last step; in between, after W += dW = W32 F, it is
+    // M W in FP64 (tensor-core digit products) for the first and the last step; in between, after W += dW = W32 F, it is
     // updated as M W += round(M W) F in FP32.  That update is only FP32-accurate where F is large
     // (close eigenvalues), so the last step's residual is formed from scratch.  (The structured
     // product P (Q W) costs less but cancels terms of size k^4 / eps for the evanescent orders.)
@@ -1042,7 +1056,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
         MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
       }
       if (step == 0 || last)
-        MX_TRY(launch_gemm<double>(bm, n, n, n, done, p.M64, n, nn, W64, n, nn, dzero, p.MW64, n, nn, s));
+        MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
       MX_EW(k_eig_residual, bm * nn, bm, n, p.MW64, W64, mu_a, p.E32);
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
       k_find_pairs<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
@@ -1062,8 +1076,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
     cd* CWb = p.CW64 + hn;
-    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64, n, nn, dzero, CWt, n, nn, s, midx));
-    MX_TRY(launch_gemm<double>(bm, nh, n, nh, done, Cm, nh, hh, W64 + hn, n, nn, dzero, CWb, n, nn, s, midx));
+    MX_TRY(ozaki_zgemm(bm, nh, n, nh, Cm, nh, hh, midx, W64, n, nn, CWt, n, nn, p.oz, s));
+    MX_TRY(ozaki_zgemm(bm, nh, n, nh, Cm, nh, hh, midx, W64 + hn, n, nn, CWb, n, nn, p.oz, s));
     MX_EW(k_modes_v_t<double>, bm * nn, bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, nn, lam64, V64, sx);
     MX_EW(k_round, bm * nn, bm * nn, V64, V32);
     // FP32 inverses and V0 products
