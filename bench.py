@@ -10,9 +10,11 @@ polarisations from one S-matrix per problem.  A step solves one chunk of ``--bat
   timed with CUDA events over exactly K steps (barrier + synchronize on both sides).
 * e2e: the same metric through the public batched API (khepri_gb300.batch.solve_rt) from host
   numpy inputs to host R/T, host<->device copies inside the timed region.
-* roofline: the libkhp entry point with the largest share of the timed region, algorithmic
-  FP64 flops per launch / its mean launch duration (events on the launching stream), against
-  the FP64 FMA throughput measured in this run by khp_probe_fp64_tflops.
+* roofline: the dominant kernel, the FP32 eigensolver of the modes stage (k_geev_schur): its
+  algorithmic flops per launch (100 n^3 per matrix) / its mean launch duration, timed by CUDA
+  events that libkhp records on its stream around each stage (khp_stage_timing), against the
+  FP32 FMA throughput measured in this run (khp_probe_fp32_tflops).  The per-stage times and
+  the tensor-core products' fraction of the bf16 peak ride along.
 * cpu_baseline: the CPU oracle (numpy/LAPACK restatement of the reference) on a bounded sample.
 
 ``--impl reference`` times that CPU restatement alone (all host threads), same metric/config.
@@ -48,6 +50,20 @@ FLOPS_PER_CALL = {
 }
 
 
+def _up64(x):
+    return (x + 63) // 64 * 64
+
+
+# bf16 tensor flops issued per modes matrix by the FP64-accurate products of the mixed solve:
+# M W twice (m = k = n) and C W twice (m = k = n/2, 2n real columns), 28 digit pairs each
+TC_FLOPS_PER_MATRIX = 28 * 2 * (2 * _up64(N_MAT) * _up64(2 * N_MAT) * _up64(2 * N_MAT)
+                                + 2 * _up64(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
+BF16_PEAK = 1935.4  # TFLOP/s, MEASURED_PEAKS.json bf16_tflops (burst)
+# DRAM bytes per matrix of the FP32 eigensolver (read + write) at 456 matrices per launch, from
+# one ncu capture (profiles/geev_fp32_n242_batch456_traffic.md): 364.1 GB / 456
+GEEV_TRAFFIC_PER_MATRIX = (197903963392 + 166228993536) / 456
+
+
 def solve_mixed_flops(n, nmaps, npattern, nhomog):
     """Algorithmic flops per problem of khp_solve_batched_mixed (FP32 and FP64 together): the
     recursion as in solve_batched_flops, plus per map the eigen-refinement (FP64 residual GEMM
@@ -67,7 +83,8 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=304)
+    ap.add_argument("--batch", type=int, default=456,
+                    help="problems per call (456 = 3 x 152 SMs: three eigensolver CTAs per SM)")
     ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -78,6 +95,9 @@ def parse():
     ap.add_argument("--uneven", type=int, default=0, help="uneven structures for the many-structure measurement")
     ap.add_argument("--twisted", type=int, default=16,
                     help="twisted-bilayer problems (5x5 base harmonics, n = 1250) for the extended-crystal measurement")
+    ap.add_argument("--tc-product", type=int, default=0,
+                    help="only time khp_zgemm_fp64_tc (FP64-accurate tensor-core product) on this many random "
+                         "242 x 242 complex problems (kernel profiling)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -241,8 +261,10 @@ def bench_grad(args, struct11, st11, wl_all, kp_all):
     g11()
     _, tg = _timed(g11)
     s11()
+    rep0 = dict(batch.STATS)
     _, ts = _timed(s11)
     out["sweep_11x11"] = {"solve_grad_per_s": B / tg, "solve_per_s_same_call_path": B / ts,
+                          "repairs_in_timed_solve": {k: batch.STATS[k] - rep0[k] for k in batch.STATS},
                           "problems": B, "loss": "sum of T (te) over the chunk",
                           "wrt": "the 256x256 pixmap shared by the 3 patterned layers"}
     if args.grad_designs > 0:
@@ -370,25 +392,26 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
-    timer = engine.StageTimer()
     results = []
+    _capi.check(lib.khp_stage_timing(1), "khp_stage_timing")
     launches0 = lib.khp_launch_count()
-    repairs0 = batch.STATS["fp64_repairs"]
+    repairs0 = dict(batch.STATS)
     with ClockSampler(local) as clocks:
         barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        with timer:
-            for k in range(args.warmup, nsteps):
-                flush.zero_()
-                results.append(step(k))
+        for k in range(args.warmup, nsteps):
+            flush.zero_()
+            results.append(step(k))
         e1.record()
         torch.cuda.synchronize()
         barrier()
     launches = lib.khp_launch_count() - launches0
-    repairs = batch.STATS["fp64_repairs"] - repairs0
+    stage_ms = _capi.stage_times()
+    lib.khp_stage_timing(0)
+    repairs = {k: batch.STATS[k] - repairs0[k] for k in batch.STATS}
     ms = e0.elapsed_time(e1)
     ms = replicas.max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms * 1e-3)
@@ -400,24 +423,41 @@ def run_gpu(args):
                               "config": {"batch": B, "problems_with_status": bad}}), flush=True)
         return
 
-    # roofline of the entry point with the largest share of the timed region
-    totals = timer.totals_ms()
-    dom = max(totals, key=lambda k: totals[k][0])
-    dom_ms, dom_calls = totals[dom]
-    share = {k: round(v[0] / ms, 4) for k, v in totals.items()}
-    scratch = torch.empty(1024 * 1024, dtype=torch.float64, device=dev)
+    # roofline of the dominant kernel: the FP32 eigensolver of the modes stage (k_geev_schur,
+    # ~40 % of the step in the launch list), timed live by the library's stage events
+    scratch = torch.empty(2048 * 1024, dtype=torch.float64, device=dev)
     fp64_peak = lib.khp_probe_fp64_tflops(_capi.ptr(scratch), scratch.numel(), _capi.stream_ptr())
+    fp32_peak = lib.khp_probe_fp32_tflops(_capi.ptr(scratch), 2 * scratch.numel(), _capi.stream_ptr())
     roof = None
-    if dom in FLOPS_PER_CALL:
-        achieved = FLOPS_PER_CALL[dom] * B / (dom_ms / dom_calls * 1e-3) / 1e12
-        roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
-                "peak_source": "FP64 FMA pipe measured in this run (khp_probe_fp64_tflops); MEASURED_PEAKS.json "
+    eig_ms, eig_calls = stage_ms["eigensolve"]
+    if prec == "mixed" and eig_calls > 0:
+        mats = B * plan.nmaps  # modes matrices per call (one per problem and distinct map)
+        eig_flops = 100.0 * N_MAT ** 3 * mats  # convention: complex eig with vectors = 100 n^3
+        achieved = eig_flops / (eig_ms / eig_calls * 1e-3) / 1e12
+        stages = {k: {"ms_per_call": v[0] / args.steps, "share": round(v[0] / ms, 4)}
+                  for k, v in stage_ms.items() if v[1] > 0}
+        roof = {"bound": "fp32", "kernel": "k_geev_schur<float> (eigensolve stage of khp_solve_batched_mixed)",
+                "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak if fp32_peak > 0 else None,
+                "traffic": GEEV_TRAFFIC_PER_MATRIX * mats if GEEV_TRAFFIC_PER_MATRIX else None,
+                "traffic_source": "DRAM read + write per matrix from one ncu capture at 456 matrices per launch, "
+                                  "scaled by the matrices of this launch",
+                "peak_source": "FP32 FMA pipe measured in this run (khp_probe_fp32_tflops); MEASURED_PEAKS.json "
                                "lists only HBM and bf16",
-                "note": "the mixed path runs its O(n^3) work on the FP32 pipe (70 TFLOP/s measured), so its "
-                        "fraction of the FP64 pipe can exceed 1" if prec == "mixed" else None,
-                "flops_per_launch": FLOPS_PER_CALL[dom] * B, "launch_ms": dom_ms / dom_calls,
-                "share_of_step": share}
+                "note": "latency-bound (one CTA per matrix; barriers and dependent loads inside each QR "
+                        "window), not pipe-bound",
+                "flops_per_launch": eig_flops, "launch_ms": eig_ms / eig_calls, "stages": stages,
+                "fp64_peak_tflops": fp64_peak}
+        tc_ms, tc_calls = stage_ms["tc_product"]
+        if tc_calls > 0:
+            tc_flops = mats * TC_FLOPS_PER_MATRIX
+            tc_rate = tc_flops / (tc_ms / args.steps * 1e-3) / 1e12
+            roof["tensor_stage"] = {
+                "bound": "tensor", "kernel": "k_ozaki_gemm (FP64-accurate products M W, C W on bf16 mma.sync)",
+                "achieved": tc_rate, "peak": BF16_PEAK, "unit": "TFLOP/s", "frac": tc_rate / BF16_PEAK,
+                "flops": "bf16 flops issued: 28 digit pairs x 2 Mp N2p K2p per product (padded to 64)",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+                "fp64_equivalent_tflops": mats * 20.0 * N_MAT ** 3 / (tc_ms / args.steps * 1e-3) / 1e12}
 
     # error of the timed path against the FP64 recursion on the first timed chunk (untimed)
     err = None
@@ -510,7 +550,7 @@ def run_gpu(args):
                                  % ("_mixed" if prec == "mixed" else ""),
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
-                       "fp64_repairs": repairs,
+                       "repairs": repairs,
                        "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": world * B * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -523,10 +563,50 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_tc_product(args):
+    """Times the FP64-accurate tensor-core product alone: C = A B for args.tc_product random
+    complex 242 x 242 pairs, against torch's FP64 matmul for the error."""
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from khepri_gb300 import _capi
+    lib = _capi.load()
+    b, n = args.tc_product, N_MAT
+    g = torch.Generator(device="cpu").manual_seed(3)
+    A = torch.randn(b, n, n, generator=g, dtype=torch.complex128).cuda()
+    Bm = torch.randn(b, n, n, generator=g, dtype=torch.complex128).cuda()
+    C = torch.empty_like(A)
+    ws = torch.empty(lib.khp_zgemm_fp64_tc_workspace(b, n, n, n), dtype=torch.uint8, device="cuda")
+
+    def call():
+        _capi.check(lib.khp_zgemm_fp64_tc(b, n, n, n, _capi.ptr(A), n, n * n, _capi.ptr(Bm), n, n * n, _capi.ptr(C), n,
+                                          n * n, _capi.ptr(ws), ws.numel(), _capi.stream_ptr()), "khp_zgemm_fp64_tc")
+
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ref = A @ Bm
+    rel = ((C - ref).abs().max() / ref.abs().max()).item()
+    print(json.dumps({"metric": "FP64-accurate complex products (242^3) per second", "value": b / (ms * 1e-3),
+                      "unit": "products/s", "ms_per_call": ms, "problems": b, "steps": args.steps,
+                      "warmup": args.warmup, "fp64_equivalent_tflops": 8.0 * n ** 3 * b / (ms * 1e-3) / 1e12,
+                      "max_rel_err_vs_torch_fp64": rel}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.tc_product > 0:
+        run_tc_product(args)
     else:
         run_gpu(args)
 

@@ -315,6 +315,25 @@ long long khp_launch_count(void);
 double khp_probe_fp64_tflops(double* scratch, int64_t scratch_doubles, void* stream);
 
 /*
+ * khp_probe_fp32_tflops: the same probe for the FP32 FMA pipe (scratch: floats, at least
+ * 2048 * number of SMs).
+ * khp_stage_timing(enable): with enable = 1, the mixed solve records CUDA events on its stream
+ * around its stages (below) and sums their device time; 0 stops.  Either call discards what was
+ * recorded.  khp_stage_timing_read(stage, ms, marks): total milliseconds and number of timed
+ * intervals of a stage since the last khp_stage_timing call (synchronises the recorded events).
+ * Off by default; meant for benchmarks, not for stream capture.
+ */
+#define KHP_STAGE_MODES 0       /* modes of the patterned layers: eigensolve, refinement, V, inverses */
+#define KHP_STAGE_EIGENSOLVE 1  /* the FP32 eigensolver inside the modes stage */
+#define KHP_STAGE_TC_PRODUCT 2  /* FP64-accurate tensor-core products (khp_zgemm_fp64_tc and internal uses) */
+#define KHP_STAGE_RECURSION 3   /* FP32 reflection-matrix recursion with its kept factors */
+#define KHP_STAGE_REFINE 4      /* FP64 iterative refinement of the stack equations and fluxes */
+#define KHP_NUM_STAGES 5
+double khp_probe_fp32_tflops(float* scratch, int64_t scratch_floats, void* stream);
+int khp_stage_timing(int32_t enable);
+int khp_stage_timing_read(int32_t stage, double* ms, int64_t* marks);
+
+/*
  * FP64-accurate batched complex product on the bf16 tensor cores (no counterpart in the
  * reference; the mixed-precision solve forms its FP64 eigen-residuals and V = Q W this way).
  * C[b] = A[b] B[b]; A: complex [batch] m x k (row stride lda, batch stride bsA, in complex

@@ -72,6 +72,9 @@ _SIGNATURES = {
                                       _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
+    "khp_probe_fp32_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
+    "khp_stage_timing": (ctypes.c_int, [_c_i32]),
+    "khp_stage_timing_read": (ctypes.c_int, [_c_i32, _c_p, _c_p]),
     "khp_zgemm_fp64_tc_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_i32]),
     "khp_zgemm_fp64_tc": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_i64, _c_i64, _c_p, _c_i64, _c_i64,
                                          _c_p, _c_i64, _c_i64, _c_p, _c_sz, _c_p]),
@@ -137,3 +140,18 @@ STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-fini
 
 def decode_status(word: int) -> str:
     return ", ".join(v for k, v in STATUS_BITS.items() if word & k) or "ok"
+
+
+STAGES = {"modes": 0, "eigensolve": 1, "tc_product": 2, "recursion": 3, "refine": 4}
+
+
+def stage_times():
+    """{stage name: (total ms, intervals)} recorded since the last khp_stage_timing call."""
+    lib = load()
+    out = {}
+    for name, sid in STAGES.items():
+        ms = ctypes.c_double(0.0)
+        marks = ctypes.c_int64(0)
+        check(lib.khp_stage_timing_read(sid, ctypes.byref(ms), ctypes.byref(marks)), "khp_stage_timing_read")
+        out[name] = (ms.value, marks.value)
+    return out

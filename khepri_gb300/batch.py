@@ -110,13 +110,14 @@ def _host(a):
 
 
 def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None, precision="fp64",
-                      refine=2, pmap=None, pdepth=None):
+                      refine=2, pmap=None, pdepth=None, repair=True):
     """R, T of one chunk by the reflection-matrix recursion (khp_solve_batched).
 
     te, tm: optional [B, npol] complex device tensors (default: prob.te, prob.tm as one
     polarisation); the recursion runs once and every polarisation is read from it.
     pmap, pdepth: optional device tensors [L, B] (int32 map index into plan's maps, float64
     depth) giving every problem its own maps and depths.
+    repair: re-solve problems whose mixed refinement did not converge (status bit 8).
     Returns R, T of shape [B] (one polarisation) or [B, npol].
     """
     B = prob.batch
@@ -150,7 +151,8 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
             code = lib.khp_solve_batched_mixed(*common, int(refine), _capi.ptr(R), _capi.ptr(T), _capi.ptr(status),
                                                _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
         _capi.check(code, "khp_solve_batched_mixed")
-        _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap, pdepth)
+        if repair:
+            _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap, pdepth)
     else:
         ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)),
                               dev)
@@ -164,23 +166,39 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
 
 
 REFINE_BIT = 8
-STATS = {"fp64_repairs": 0}  # problems re-solved in FP64 after a non-converged mixed refinement
+# problems re-solved after a non-converged mixed refinement: with longer refinement (mixed) and,
+# if that still does not converge, in FP64
+STATS = {"refine_repairs": 0, "fp64_repairs": 0}
+REPAIR_REFINE = 8  # refinement rounds of the repair solve (plus the adaptive extra rounds)
 
 
 def _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap=None, pdepth=None):
-    """Re-solve in FP64 (khp_solve_batched) the problems whose mixed-precision refinement did
-    not converge (status bit 8: an ill-conditioned stack, e.g. next to a Wood anomaly), and
-    write their R, T and status in place."""
+    """Re-solve the problems whose mixed-precision refinement did not converge (status bit 8: an
+    ill-conditioned stack, e.g. next to a Wood anomaly, where the FP32 factors make the
+    refinement converge at ~0.3 per round): first by the mixed path with REPAIR_REFINE rounds,
+    then in FP64 (khp_solve_batched) for any still unconverged; R, T and status in place."""
     flagged = (status & REFINE_BIT) != 0
     if not bool(flagged.any()):
         return
     idx = torch.nonzero(flagged).flatten()
-    STATS["fp64_repairs"] += int(idx.numel())
+    STATS["refine_repairs"] += int(idx.numel())
     sub = prob.subset(idx)
     st = torch.zeros(idx.numel(), dtype=torch.int32, device=status.device)
+    pm = None if pmap is None else pmap[:, idx]
+    pd = None if pdepth is None else pdepth[:, idx]
     r, t = solve_chunk_gamma(struct, plan, sub, st, epsi, epse, te[idx].contiguous(), tm[idx].contiguous(),
-                             precision="fp64", pmap=None if pmap is None else pmap[:, idx],
-                             pdepth=None if pdepth is None else pdepth[:, idx])
+                             precision="mixed", refine=REPAIR_REFINE, pmap=pm, pdepth=pd, repair=False)
+    still = (st & REFINE_BIT) != 0
+    if bool(still.any()):
+        j = torch.nonzero(still).flatten()
+        STATS["fp64_repairs"] += int(j.numel())
+        st64 = torch.zeros(j.numel(), dtype=torch.int32, device=status.device)
+        r64, t64 = solve_chunk_gamma(struct, plan, sub.subset(j), st64, epsi, epse, te[idx][j].contiguous(),
+                                     tm[idx][j].contiguous(), precision="fp64",
+                                     pmap=None if pm is None else pm[:, j], pdepth=None if pd is None else pd[:, j])
+        r[j] = r64
+        t[j] = t64
+        st[j] = st64
     R[idx] = r
     T[idx] = t
     status[idx] = (status[idx] & ~REFINE_BIT) | st

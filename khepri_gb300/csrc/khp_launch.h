@@ -87,4 +87,9 @@ inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : K
 // Adds k to the process-wide launch counter reported by khp_launch_count().
 void count_launches(int k);
 
+// Stage timing (khp_stage_timing): when enabled, a CUDA event is recorded on the stream at the
+// begin and end marks of a stage (KHP_STAGE_* of the public header); no-ops otherwise.
+void stage_begin(int stage, cudaStream_t s);
+void stage_end(int stage, cudaStream_t s);
+
 }  // namespace khp

@@ -1011,6 +1011,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   // ---- 1. modes: FP32 eigensolve + FP64 refinement, every map slot in one batch ----
   const int S = (int)used.size();
   if (S > 0) {
+    stage_begin(KHP_STAGE_MODES, s);
     const int64_t bm = (int64_t)S * batch;
     const cd* Cm = reinterpret_cast<const cd*>(conv);
     const cd* HX = reinterpret_cast<const cd*>(hx);
@@ -1033,7 +1034,9 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps,
             midx + (int64_t)m * batch, sx + (int64_t)m * batch);
     MX_EW(k_assemble_pq_t<float>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32);
+    stage_begin(KHP_STAGE_EIGENSOLVE, s);
     MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s));
+    stage_end(KHP_STAGE_EIGENSOLVE, s);
     // Refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 inverse of the current W, held
     // in Wi until the final inverse), mu += diag(E), W += W F.
     MX_EW(k_assemble_pq_t<double>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M64);
@@ -1089,10 +1092,12 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_EW(k_v0_right<float>, bm * nn, bm, nh, p.v0b, Vi, p.Q0[0]);
     MX_EW(k_v0inv_left<float>, bm * nn, bm, nh, p.v0ib, V32, p.Vt[0]);
     MX_EW(k_or_status, batch, batch, S, sx, status);
+    stage_end(KHP_STAGE_MODES, s);
   } else {
     MX_EW(k_v0_blocks, batch * nh, batch, nh, gx, gy, kp, k0, p.v0b, p.v0ib);
   }
   // ---- homogeneous blocks (FP64) ----
+  stage_begin(KHP_STAGE_RECURSION, s);
   MX_EW(k_homog_blocks, batch * nh, batch, nh, 1, epsi, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.inc, status);
   MX_EW(k_homog_blocks, batch * nh, batch, nh, 2, epse, DepthSel{nullptr, 0.0}, gx, gy, kp, k0, p.trn, status);
   for (int l = 0; l < L; ++l)
@@ -1133,7 +1138,9 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   }
   MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.inc, gam(0), p.lu32);
   MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv0, n, nn, p.piv, status, s));
+  stage_end(KHP_STAGE_RECURSION, s);
   // ---- 3. iterative refinement of the stack equations ----
+  stage_begin(KHP_STAGE_REFINE, s);
   Table tb;
   tb.L = L;
   tb.nh = nh;
@@ -1195,8 +1202,10 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
                                                          reinterpret_cast<const cd*>(te),
                                                          reinterpret_cast<const cd*>(tm), epsi, epse, R, Tt);
     count_launches(1);
+    stage_end(KHP_STAGE_REFINE, s);
     return cuda_status();
   }
+  stage_end(KHP_STAGE_REFINE, s);
   return grad_mixed(tb, p, gp, *grad, batch, nh, L, kinds, slot, used, depth_of, nmaps, conv, gx, gy, kp, k0, npol,
                     te, tm, epsi, epse, refine, R, Tt, s);
 }

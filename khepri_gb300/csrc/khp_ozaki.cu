@@ -415,6 +415,7 @@ int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64
                                std::min<int64_t>((int64_t)(w.bd_elems / ozaki_b_elems(k, n)), (int64_t)(w.eb_n / n)));
   const int64_t chunk = std::min(cap, ozaki_chunk(batch));
   if (chunk <= 0) return KHP_ERR_WORKSPACE;
+  stage_begin(KHP_STAGE_TC_PRODUCT, s);
   for (int64_t off = 0; off < batch; off += chunk) {
     const int64_t nb = std::min<int64_t>(chunk, batch - off);
     int st = aidx ? split_a(nb, m, k, A, lda, bsA, aidx + off, w.ad, w.ea, s)
@@ -423,6 +424,7 @@ int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64
     if (!st) st = product(nb, m, n, k, w.ad, w.ea, w.bd, w.eb, C + off * bsC, ldc, bsC, s);
     if (st) return st;
   }
+  stage_end(KHP_STAGE_TC_PRODUCT, s);
   return KHP_OK;
 }
 

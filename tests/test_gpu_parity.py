@@ -304,15 +304,16 @@ def test_mixed_precision_small_cases(khp, golden):
 def test_mixed_precision_repairs_ill_conditioned_problem(khp):
     """A sweep problem next to a Wood anomaly (f index 49, k index 341 of the 11x11 sweep) whose
     FP32-preconditioned refinement converges too slowly: the mixed path must flag it (status
-    bit 8) and re-solve it in FP64, so that it still meets |dR|, |dT| <= 1e-6."""
+    bit 8) and re-solve it (longer mixed refinement, then FP64 if needed), so that it still
+    meets |dR|, |dT| <= 1e-6."""
     from khepri_gb300 import batch, workloads
     st = workloads.batched_structure(0)
     wl, kp = workloads.batched_problems()
     inside = np.flatnonzero(np.hypot(kp[:, 0], kp[:, 1]) < 2 * np.pi / wl)
     idx = np.concatenate([[50517, 38308, 47259], inside[inside > 20000][:3]])
-    before = batch.STATS["fp64_repairs"]
+    before = batch.STATS["refine_repairs"]
     Rm, Tm, sm = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="mixed")
-    assert batch.STATS["fp64_repairs"] > before
+    assert batch.STATS["refine_repairs"] > before
     assert not sm.any()
     Rg, Tg, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="gamma")
     assert np.isfinite(Rg).all() and np.isfinite(Tg).all()
