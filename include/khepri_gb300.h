@@ -305,6 +305,66 @@ int khp_fields_idft(int64_t rows, int32_t nh, const double* ff, const double* gx
                     int64_t npts, const double* x, const double* y, double* out, void* stream);
 
 /*
+ * Band structure from a scattering matrix: the eigenpairs of the pencil (Sl, Sr) of
+ * khepri/eigentricks.py:5-43 (scattering_splitlr, scattering_eigenvalues, scattering_det).
+ *   S: complex [batch][4 ng][4 ng] dense, row-major, blocks [[S11, S12], [S21, S22]] of 2 ng
+ *      (the reference's p = 0:2ng, m = 2ng:4ng); s_stride: batch stride in complex elements.
+ *   w: complex [batch][4 ng] eigenvalues;  v: complex [batch][4 ng][4 ng] unit right
+ *      eigenvectors (columns) or NULL;  det: complex [batch] = det(S11 - S12 S22^-1 S21) det(S22)
+ *      or NULL.  Computed as the eigenpairs of Sr^-1 Sl (S22 is inverted once).
+ *   status: int32 [batch], OR-ed: SINGULAR (S22 singular: an infinite pencil eigenvalue),
+ *      NONFINITE (NaN / inf in S: the reference returns None), NOT_CONVERGED.
+ */
+size_t khp_scattering_eig_workspace(int64_t batch, int32_t ng);
+int khp_scattering_eig(int64_t batch, int32_t ng, const double* S, int64_t s_stride, double* w, double* v,
+                       double* det, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
+ * Plane-wave amplitudes of a sampled beam over a Brillouin-zone-integration supercell
+ * (khepri/beams.py:164-190, amplitudes_from_fields, with fourier.slow_dft, fourier.py:94-104).
+ *   fields: complex [X][Y][2][3] (E, H; x, y, z) with X = bzs1 * ns, Y = bzs0 * ns;
+ *   x, y: real [X][Y] sample coordinates; kp: complex [2] incident planar wavevector;
+ *   gx, gy: real [ng] the expansion's g vectors;  out: complex [4][ng] for (Ex, Ey, Hx, Hy):
+ *   sum over the bzs0 * bzs1 cells of the direct DFT of the fields divided by exp(i kp.r), over
+ *   (cells * ns) — the reference's cell pairing of samples and coordinates included.
+ *   Scratch: khp_bzi_amplitudes_workspace(bzs0, bzs1, ns) bytes.
+ */
+size_t khp_bzi_amplitudes_workspace(int32_t bzs0, int32_t bzs1, int32_t ns);
+int khp_bzi_amplitudes(int32_t bzs0, int32_t bzs1, int32_t ns, const double* fields, const double* x, const double* y,
+                       const double* kp, int32_t ng, const double* gx, const double* gy, double* out, void* workspace,
+                       size_t ws_bytes, void* stream);
+
+/*
+ * tmat formulation of a patterned layer (khepri/tmat/scattering.py:25-51, matrices.py:126-212),
+ * SI units, batched over (wavelength, kp) problems that share the Fourier coefficients.
+ * khp_tmat_layer_smatrix:
+ *   eps_g, epsinv_g: complex [nq0][nq1] coefficients of eps and 1/eps (tools.epsilon_g);
+ *   gx, gy: real [px * py] g vectors of the harmonics in the reference's order (lattice.gx.T
+ *   flattened: harmonic g = i1 + px * i2);  kp: real [batch][2];  wavelength: real [batch];
+ *   u_blocks, v_blocks: complex [batch][16][px * py], the 4 x 4 blocks of diagonals of U and Vi
+ *   (matrix_u, matrix_v; block (a, c) at a * 4 + c);  depth, slicing_pow as scattering_matrix.
+ *   S: complex [batch][4 ng][4 ng] = multS^p(matrix_s(U expm(-A depth / 2^p) Vi)).
+ *   A_out, E_out, T_out (each complex [batch][4 ng][4 ng] or NULL): A, the slice's expm, U E Vi.
+ *   The exponential is one scaling and squaring for the batch (its largest 1-norm): the call
+ *   synchronises the stream once to read that norm.
+ * khp_tmat_multS: S = multS(S1, S2) (matrices.py:194-212), dense [4 ng][4 ng] each.
+ * khp_tmat_matrix_s: S = matrix_s(T) (matrices.py:171-180), T and S [batch][4 ng][4 ng]
+ *   contiguous; scratch: khp_tmat_multS_workspace(batch, ng) bytes.
+ * status: int32 [batch], OR-ed (SINGULAR for a singular block inverse or solve).
+ */
+size_t khp_tmat_layer_workspace(int64_t batch, int32_t ng);
+int khp_tmat_layer_smatrix(int64_t batch, int32_t px, int32_t py, int32_t nq0, int32_t nq1, const double* eps_g,
+                           const double* epsinv_g, const double* gx, const double* gy, const double* kp,
+                           const double* wavelength, const double* u_blocks, const double* v_blocks, double depth,
+                           int32_t slicing_pow, double* S, double* A_out, double* E_out, double* T_out,
+                           int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+size_t khp_tmat_multS_workspace(int64_t batch, int32_t ng);
+int khp_tmat_matrix_s(int64_t batch, int32_t ng, const double* T, double* S, int32_t* status, void* workspace,
+                      size_t ws_bytes, void* stream);
+int khp_tmat_multS(int64_t batch, int32_t ng, const double* S1, int64_t s1_stride, const double* S2, int64_t s2_stride,
+                   double* S, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
+
+/*
  * Diagnostics (no counterpart in the reference).
  * khp_launch_count: number of kernels libkhp has launched in this process (all entry points).
  * khp_probe_fp64_tflops: measured FP64 FMA throughput of the current device in TFLOP/s, the

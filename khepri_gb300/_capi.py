@@ -75,6 +75,18 @@ _SIGNATURES = {
     "khp_probe_fp32_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
     "khp_stage_timing": (ctypes.c_int, [_c_i32]),
     "khp_stage_timing_read": (ctypes.c_int, [_c_i32, _c_p, _c_p]),
+    "khp_scattering_eig_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_scattering_eig": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_bzi_amplitudes_workspace": (_c_sz, [_c_i32, _c_i32, _c_i32]),
+    "khp_bzi_amplitudes": (ctypes.c_int, [_c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_p,
+                                          _c_p, _c_sz, _c_p]),
+    "khp_tmat_layer_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_tmat_layer_smatrix": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                              _c_p, _c_p, _c_p, _c_d, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                              _c_sz, _c_p]),
+    "khp_tmat_multS_workspace": (_c_sz, [_c_i64, _c_i32]),
+    "khp_tmat_matrix_s": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_tmat_multS": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_zgemm_fp64_tc_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_i32]),
     "khp_zgemm_fp64_tc": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_i64, _c_i64, _c_p, _c_i64, _c_i64,
                                          _c_p, _c_i64, _c_i64, _c_p, _c_sz, _c_p]),

@@ -25,6 +25,7 @@ import numpy as np
 import torch
 
 from . import _capi, engine
+from .expansion import Expansion
 from .engine import LayerSpec
 
 
@@ -78,6 +79,7 @@ class Crystal:
         self.epse = epse
         self.source = None
         self.lattice = engine.lattice_vectors(lattice, lattice_pitch)
+        self.expansion = Expansion(self.pw, self.lattice)
         self._struct = engine.StructureGPU(self.pw, self.lattice, device)
         self.device = self._struct.device
         self.layers = dict()

@@ -685,3 +685,295 @@ def analytical_convolution_matrix(islands, eps_host, pw, lattice="square"):
     for isl in islands:
         eps_g += (isl["epsilon"] - eps_host) * island_transform(isl, gx, gy, sigma)
     return convolution_matrix_fourier(eps_g.reshape(epw), pw)
+
+
+# ------------------------------------------------------------------------------------------
+# Band structure from S (khepri/eigentricks.py:5-55)
+# ------------------------------------------------------------------------------------------
+def scattering_splitlr(S):
+    """eigentricks.py:5-23: the pencil (Sl, Sr) of a dense [4 ng, 4 ng] S."""
+    ng = S.shape[0] // 4
+    p = np.s_[0:2 * ng]
+    m = np.s_[2 * ng:4 * ng]
+    Sl = np.zeros_like(S)
+    Sl[p, p] = S[p, p]
+    Sl[m, p] = S[m, p]
+    Sl[m, m] = -np.eye(2 * ng, dtype=S.dtype)
+    Sr = np.zeros_like(S)
+    Sr[p, p] = np.eye(2 * ng, dtype=S.dtype)
+    Sr[p, m] = -S[p, m]
+    Sr[m, m] = -S[m, m]
+    return Sl, Sr
+
+
+def scattering_det(S):
+    """eigentricks.py:25-29."""
+    ng = S.shape[0] // 4
+    p = np.s_[0:2 * ng]
+    m = np.s_[2 * ng:4 * ng]
+    return np.linalg.det(S[p, p] - S[p, m] @ np.linalg.inv(S[m, m]) @ S[m, p]) * np.linalg.det(S[m, m])
+
+
+def scattering_eigenvalues(S, dos=False):
+    """eigentricks.py:30-39: generalized eigenpairs of (Sl, Sr) by QZ (scipy.linalg.eig)."""
+    from scipy.linalg import eig
+    Sl, Sr = scattering_splitlr(S)
+    if np.any(np.isnan(Sr)) or np.any(np.isnan(Sl)):
+        return None
+    w, v = eig(Sl, Sr)
+    return (w, v, scattering_det(S)) if dos else (w, v)
+
+
+def band_structure(S):
+    """eigentricks.py:46-55."""
+    res = scattering_eigenvalues(S)
+    if res is None:
+        return None
+    w = res[0].real
+    w = w[w > 0]
+    w = w[w < 1]
+    return w[np.isclose(np.abs(w), 1.0, rtol=0.0, atol=1e-10)]
+
+
+def match_eigenvalues(a, b):
+    """Largest relative distance from each finite value of b to its nearest value in a (a test
+    helper for eigenvalue sets whose order is arbitrary)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    b = b[np.isfinite(b)]
+    if b.size == 0:
+        return 0.0
+    d = np.abs(b[:, None] - a[None, :]).min(axis=1)
+    return float((d / np.maximum(1.0, np.abs(b))).max())
+
+
+# ------------------------------------------------------------------------------------------
+# Brillouin-zone-integrated beams (khepri/beams.py:164-207)
+# ------------------------------------------------------------------------------------------
+def amplitudes_from_fields(fields, g, kp, x, y, bzs):
+    """beams.py:164-190 with fourier.slow_dft (fourier.py:94-104): fields [X, Y, 2, 3] divided by
+    exp(i kp.r), cut into bzs[0] x bzs[1] cells of ns x ns samples, the cells' direct DFTs at the
+    g vectors [2, ng] summed, over (cells * ns).  The reference's cut pairs the samples of cell i
+    ((c1 ns + ix, c0 ns + iy), c0 = i // bzs[1], c1 = i % bzs[1]) with the coordinates of
+    ((d1 ns + ix, d0 ns + iy), d1 = i // bzs[0], d0 = i % bzs[0]); restated by these index maps."""
+    b0, b1 = bzs
+    X, Y = x.shape
+    ns = X // b1
+    F = fields / np.exp(1j * (kp[0] * x + kp[1] * y))[..., None, None]
+    F = F[..., :2].reshape(X, Y, 4)  # (Ex, Ey, Hx, Hy)
+    cells = b0 * b1
+    i = np.arange(cells)[:, None, None]
+    ix = np.arange(ns)[None, :, None]
+    iy = np.arange(ns)[None, None, :]
+    fr, fc = (i % b1) * ns + ix, (i // b1) * ns + iy
+    cr, cc = (i // b0) * ns + ix, (i % b0) * ns + iy
+    vals = F[fr, fc].reshape(-1, 4)
+    xs = x[cr, cc].reshape(-1)
+    ys = y[cr, cc].reshape(-1)
+    ph = np.exp(-1j * (np.outer(xs, g[0]) + np.outer(ys, g[1])))  # [points, ng]
+    return (vals.T @ ph) / (cells * ns)
+
+
+def gen_bzi_grid(shape, a=1, reciproc=None):
+    """beams.py:193-207."""
+    if reciproc is None:
+        b1, b2 = [2 * np.pi / a, 0], [0, 2 * np.pi / a]
+    else:
+        b1, b2 = reciproc
+    si, sj = 1 / shape[0], 1 / shape[1]
+    i, j = np.meshgrid(np.arange(-0.5 + si / 2, 0.5, si), np.arange(-0.5 + sj / 2, 0.5, sj), indexing="ij")
+    return np.stack([b1[0] * i + b2[0] * j, b1[1] * i + b2[1] * j])
+
+
+# ------------------------------------------------------------------------------------------
+# tmat formulation (khepri/tmat/lattice.py, tools.py, matrices.py, scattering.py): SI units,
+# the layer's transfer matrix from expm of the 4 ng x 4 ng field matrix, sliced and squared by
+# star products in the dense [p; m] layout.
+# ------------------------------------------------------------------------------------------
+MU0C = 4 * math.pi * 1e-7 * 299792458.0  # constants.py:3-5
+
+
+def tmat_grid_size(pw):
+    """tools.py:27-37: (nx, ny) and the q grid of the Fourier coefficients."""
+    if pw[0] % 2 == 0:
+        nx, ny = pw[0] // 2, pw[1] // 2
+        return (nx, ny), (4 * nx, 4 * ny)
+    nx, ny = (pw[0] - 1) // 2, (pw[1] - 1) // 2
+    return (nx, ny), (4 * nx + 1, 4 * ny + 1)
+
+
+def tmat_lattice(pw, a1, a2):
+    """lattice.py:32-87: reciprocal basis, the q-grid G vectors and the pw sub-grid g vectors
+    (cut with q[0] on both axes, as lattice.py:77-84)."""
+    coef = TWOPI / (a1[0] * a2[1] - a1[1] * a2[0])
+    b1 = (a2[1] * coef, -a2[0] * coef)
+    b2 = (-a1[1] * coef, a1[0] * coef)
+    _, q = tmat_grid_size(pw)
+    cx = q[0] // 2 if q[0] % 2 == 0 else (q[0] - 1) // 2
+    cy = q[1] // 2 if q[1] % 2 == 0 else (q[1] - 1) // 2
+    m1 = np.arange(q[0]) - cx
+    m2 = np.arange(q[1]) - cy
+    Gx = np.add.outer(b1[0] * m1, b2[0] * m2)
+    Gy = np.add.outer(b1[1] * m1, b2[1] * m2)
+    nx = q[0] // 4 if q[0] % 2 == 0 else (q[0] - 1) // 4
+    ny = q[1] // 4 if q[1] % 2 == 0 else (q[1] - 1) // 4
+    cut = np.s_[nx:q[0] - nx, ny:q[0] - ny]
+    return SimpleNamespace(pw=tuple(pw), b1=b1, b2=b2, q=q, Gx=Gx, Gy=Gy, gx=Gx[cut], gy=Gy[cut],
+                           area=abs(a1[0] * a2[1] - a1[1] * a2[0]))
+
+
+def tmat_kz(gx, gy, eps, wavelength, kp):
+    """tools.py:39-47: kz with Im >= 0 (and Re >= 0 when Im == 0)."""
+    u2 = np.abs(kp[0] + gx) ** 2 + np.abs(kp[1] + gy) ** 2
+    kz = np.emath.sqrt(eps * (TWOPI / wavelength) ** 2 - u2).astype(complex)
+    flip = (kz.imag < 0.0) | (np.isclose(kz.imag, 0.0) & (kz.real < 0.0))
+    return np.where(flip, -kz, kz)
+
+
+def _unit_planar(gx, gy, kp):
+    ux = (kp[0] + gx).astype(complex)
+    uy = (kp[1] + gy).astype(complex)
+    nrm = np.sqrt(np.abs(ux) ** 2 + np.abs(uy) ** 2)
+    small = nrm ** 2 < np.finfo(float).eps
+    safe = np.where(small, 1.0, nrm)
+    return np.where(small, 1.0, ux / safe), np.where(small, 0.0, uy / safe)
+
+
+def tmat_eta(gx, gy, kp):
+    """tools.py:49-59: eta = (u_y, -u_x) of the unit planar wavevector ((0, -1) at u = 0)."""
+    ux, uy = _unit_planar(gx, gy, kp)
+    return uy, -ux
+
+
+def tmat_mu(gx, gy, kz, eps, wavelength, kp):
+    """tools.py:62-71: mu = kz / (sqrt(eps) k0) u."""
+    ux, uy = _unit_planar(gx, gy, kp)
+    f = kz / (cmath.sqrt(eps) * TWOPI / wavelength)
+    return f * ux, f * uy
+
+
+def _blocks_to_dense(blocks, ng):
+    M = np.zeros((4 * ng, 4 * ng), dtype=complex)
+    for (i, j), d in blocks.items():
+        M[i * ng:(i + 1) * ng, j * ng:(j + 1) * ng] += np.diag(d)
+    return M
+
+
+def tmat_u_blocks(kz, eta, mu, eps, wavelength):
+    """matrices.py:9-42 (matrix_u) as its 4 x 4 blocks of diagonals, harmonics in .T order."""
+    hU = MU0C / cmath.sqrt(eps)
+    mgx, mgy = mu[0].T.ravel(), mu[1].T.ravel()
+    egx, egy = eta[0].T.ravel(), eta[1].T.ravel()
+    dg = cmath.sqrt(eps) * math.pi / wavelength / kz.T.ravel()
+    return {(0, 0): dg * mgy, (2, 0): dg * mgy, (0, 1): -dg * mgx, (2, 1): -dg * mgx,
+            (1, 0): dg * egy, (3, 0): -dg * egy, (1, 1): -dg * egx, (3, 1): dg * egx,
+            (0, 2): -hU * dg * egy, (2, 2): hU * dg * egy, (1, 2): hU * dg * mgy, (3, 2): hU * dg * mgy,
+            (1, 3): -hU * dg * mgx, (3, 3): -hU * dg * mgx, (2, 3): -hU * dg * egx, (0, 3): hU * dg * egx}
+
+
+def tmat_v_blocks(eta, mu, eps):
+    """matrices.py:44-74 (matrix_v) as its 4 x 4 blocks of diagonals."""
+    hV = np.sqrt(eps) / MU0C
+    mgx, mgy = mu[0].T.ravel(), mu[1].T.ravel()
+    egx, egy = eta[0].T.ravel(), eta[1].T.ravel()
+    return {(0, 0): egx, (1, 0): egy, (2, 0): hV * mgx, (3, 0): hV * mgy,
+            (0, 1): -mgx, (1, 1): -mgy, (2, 1): hV * egx, (3, 1): hV * egy,
+            (0, 2): egx, (1, 2): egy, (2, 2): -hV * mgx, (3, 2): -hV * mgy,
+            (0, 3): mgx, (1, 3): mgy, (2, 3): hV * egx, (3, 3): hV * egy}
+
+
+def tmat_uv(lat, wavelength, kp, eps_incid, eps_emerg):
+    """lattice.py:138-171: U (incidence), Vi (incidence), Ve (emergence), dense."""
+    ng = lat.gx.size
+    kzi = tmat_kz(lat.gx, lat.gy, eps_incid, wavelength, kp)
+    kze = tmat_kz(lat.gx, lat.gy, eps_emerg, wavelength, kp)
+    eta = tmat_eta(lat.gx, lat.gy, kp)
+    mui = tmat_mu(lat.gx, lat.gy, kzi, eps_incid, wavelength, kp)
+    mue = tmat_mu(lat.gx, lat.gy, kze, eps_emerg, wavelength, kp)
+    return (_blocks_to_dense(tmat_u_blocks(kzi, eta, mui, eps_incid, wavelength), ng),
+            _blocks_to_dense(tmat_v_blocks(eta, mui, eps_incid), ng),
+            _blocks_to_dense(tmat_v_blocks(eta, mue, eps_emerg), ng))
+
+
+def tmat_epsilon_g(q, islands_data, eps_host, inverse=False):
+    """tools.py:76-86."""
+    f = (lambda v: 1 / v) if inverse else (lambda v: v)
+    out = np.zeros(q, dtype=complex)
+    out[q[0] // 2, q[1] // 2] = f(eps_host)
+    for bf, e in islands_data:
+        out += (f(e) - f(eps_host)) * bf
+    return out
+
+
+def tmat_indices(pw, nxy):
+    """tools.py:73-75 (coords_from_index, Fortran order) for every harmonic."""
+    g = np.arange(pw[0] * pw[1])
+    return np.stack([g % pw[0] - nxy[0], g // pw[0] - nxy[1]], axis=1)
+
+
+def tmat_matrix_a(pw, gx, gy, eps_g, epsinv_g, wavelength, kp):
+    """matrices.py:126-169 (matrix_a): 4 x 4 blocks of ng x ng, vectorised."""
+    nx, ny = gx.shape[0] // 2, gx.shape[1] // 2
+    ind = tmat_indices(pw, (nx, ny))
+    c1 = TWOPI / wavelength
+    ieo, iseo, imo, ismo = 1j / MU0C * c1, 1j * MU0C / c1, 1j * MU0C * c1, 1j / MU0C / c1
+    ng = gx.size
+    ux = kp[0] + gx.T.ravel()
+    uy = kp[1] + gy.T.ravel()
+    d1 = ind[:, 0][:, None] - ind[:, 0][None, :] + 2 * nx
+    d2 = ind[:, 1][:, None] - ind[:, 1][None, :] + 2 * ny
+    E = eps_g[d1, d2]
+    Ei = epsinv_g[d1, d2]
+    I = np.eye(ng)
+    A = np.zeros((4 * ng, 4 * ng), dtype=complex)
+
+    def put(i, j, M):
+        A[i * ng:(i + 1) * ng, j * ng:(j + 1) * ng] = M
+
+    put(2, 0, -ismo * np.diag(ux * uy))
+    put(3, 0, -ismo * np.diag(uy ** 2) + ieo * E)
+    put(2, 1, ismo * np.diag(ux ** 2) - ieo * E)
+    put(3, 1, ismo * np.diag(ux * uy))
+    put(1, 2, -imo * I + iseo * uy[:, None] * Ei * uy[None, :])
+    put(0, 3, imo * I - iseo * ux[:, None] * Ei * ux[None, :])
+    put(0, 2, iseo * ux[:, None] * Ei * uy[None, :])
+    put(1, 3, -iseo * uy[:, None] * Ei * ux[None, :])
+    return A
+
+
+def tmat_matrix_s(T):
+    """matrices.py:171-180."""
+    h = T.shape[0] // 2
+    p, m = np.s_[0:h], np.s_[h:2 * h]
+    S = np.zeros_like(T)
+    S[p, p] = np.linalg.inv(T[p, p])
+    S[p, m] = -S[p, p] @ T[p, m]
+    S[m, p] = T[m, p] @ S[p, p]
+    S[m, m] = T[m, m] + T[m, p] @ S[p, m]
+    return S
+
+
+def tmat_multS(S1, S2):
+    """matrices.py:194-212: star product in the dense [p; m] layout."""
+    h = S1.shape[0] // 2
+    p, m = np.s_[0:h], np.s_[h:2 * h]
+    I0 = np.eye(h, dtype=S1.dtype)
+    I = I0 - S1[p, m] @ S2[m, p]
+    G1 = np.linalg.solve(I, S1[p, p])
+    G2 = np.linalg.solve(I, S1[p, m])
+    S = np.empty_like(S1)
+    S[p, p] = S2[p, p] @ G1
+    S[m, p] = S1[m, p] + S1[m, m] @ S2[m, p] @ G1
+    S[p, m] = S2[p, m] + S2[p, p] @ G2 @ S2[m, m]
+    S[m, m] = S1[m, m] @ (I0 + S2[m, p] @ G2) @ S2[m, m]
+    return S
+
+
+def tmat_layer_smatrix(A, U, Vi, depth, slicing_pow):
+    """scattering.py:25-51: T = U expm(-A d / 2^p) Vi, S = matrix_s(T), squared p times."""
+    from scipy.linalg import expm
+    E = expm(-A * (depth / 2 ** slicing_pow))
+    S = tmat_matrix_s(U @ E @ Vi)
+    for _ in range(slicing_pow):
+        S = tmat_multS(S, S)
+    return S, E

@@ -254,8 +254,136 @@ def analytical(ref_root):
     np.savez_compressed(os.path.join(HERE, "analytical.npz"), **out)
 
 
+def bands(ref_root):
+    """Band structure from S (khepri/eigentricks.py:5-55): pencil eigenvalues, determinant and
+    band_structure of the dense global S of a patterned slab (3x3 harmonics, disc eps 8 in air,
+    d = 0.4) at four (f, kx) points, from the reference's Crystal solve."""
+    sys.path.insert(0, ROOT)
+    Crystal, Drawing, tools = _import_reference(ref_root)
+    from khepri import eigentricks as et
+    x = np.linspace(-0.5, 0.5, 64)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    emap = np.where(X ** 2 + Y ** 2 < 0.3 ** 2, 8.0, 1.0)
+    cl = _crystal(Crystal, (3, 3), {"P": ("pixmap", emap, 0.4)}, ["P"])
+    points = [(0.3, 0.0), (0.45, 0.3), (0.6, 0.8), (0.7, 1.5)]
+    Ss, ws, dets, bs, counts = [], [], [], [], []
+    for f, kx in points:
+        cl.set_source(1.0 / f, 1.0, 0.0, kp=(kx, 0.0))
+        cl.solve()
+        S = np.asarray(cl.Stot)
+        n = S.shape[2]
+        Sd = S.transpose(0, 2, 1, 3).reshape(2 * n, 2 * n)
+        w, _, d = et.scattering_eigenvalues(Sd, dos=True)
+        b = et.band_structure(Sd)
+        Ss.append(Sd)
+        ws.append(w)
+        dets.append(d)
+        bs.extend(list(b))
+        counts.append(len(b))
+    np.savez_compressed(os.path.join(HERE, "bands_3x3.npz"), S=np.array(Ss), w=np.array(ws), det=np.array(dets),
+                        bands=np.array(bs, dtype=float), band_counts=np.array(counts), points=np.array(points))
+    print("bands_3x3: eigenvalues of", len(points), "S-matrices of size", Ss[0].shape)
+
+
+def beams(ref_root):
+    """Brillouin-zone-integrated beams (khepri/beams.py:164-207): amplitudes_from_fields on seeded
+    random fields over 3x3 and 2x3 supercells (3x3 harmonics), and gen_bzi_grid."""
+    sys.path.insert(0, ROOT)
+    _import_reference(ref_root)
+    from khepri.beams import amplitudes_from_fields, gen_bzi_grid
+    from khepri.expansion import Expansion
+    rng = np.random.default_rng(21)
+    out = {}
+    for name, bzs, ns, kp in [("sq", (3, 3), 4, (0.4, -0.25)), ("rect", (2, 3), 4, (-0.1, 0.3))]:
+        X, Y = bzs[1] * ns, bzs[0] * ns
+        fields = rng.standard_normal((X, Y, 2, 3)) + 1j * rng.standard_normal((X, Y, 2, 3))
+        x, y = np.meshgrid((np.arange(X) + 0.5) / ns, (np.arange(Y) + 0.5) / ns * 1.1, indexing="ij")
+        e = Expansion((3, 3))
+        F = amplitudes_from_fields(fields, e, 1.0, kp, x, y, bzs)
+        out.update({f"{name}_fields": fields, f"{name}_x": x, f"{name}_y": y, f"{name}_kp": np.array(kp),
+                    f"{name}_bzs": np.array(bzs), f"{name}_g": e.g_vectors, f"{name}_F": F})
+    out["grid_a"] = gen_bzi_grid((4, 3))
+    out["grid_b"] = gen_bzi_grid((3, 3), a=2)
+    out["grid_c"] = gen_bzi_grid((2, 5), reciproc=((1.0, 0.5), (-0.3, 2.0)))
+    np.savez_compressed(os.path.join(HERE, "beams.npz"), **out)
+    print("beams: amplitudes of", out["sq_F"].shape, out["rect_F"].shape)
+
+
+def _pin(out, name, M, rng_seed=0):
+    """A large matrix pinned by seeded sampled entries and two seeded matrix-vector checksums."""
+    rng = np.random.default_rng(rng_seed)
+    M = np.asarray(M)
+    idx = rng.choice(M.size, size=min(M.size, 6000), replace=False)
+    r = rng.standard_normal(M.shape[1]) + 1j * rng.standard_normal(M.shape[1])
+    l = rng.standard_normal(M.shape[0]) + 1j * rng.standard_normal(M.shape[0])
+    out[f"{name}_idx"] = idx
+    out[f"{name}_val"] = M.flat[idx]
+    out[f"{name}_Mr"] = M @ r
+    out[f"{name}_lM"] = l @ M
+
+
+def tmat(ref_root):
+    """tmat expm formulation (khepri/tmat/*.py): the MATLAB fixtures of the reference's own test
+    (test/integration/test_pair_pw.py, fixtures/pair_pw: pw 8x8, a = 100 nm, lambda = 200 nm,
+    disc r = 0.2 a, eps 8.9, depth 100 nm / 2^3 slices) and the reference run on a second case
+    (pw 5x5, oblique kp, two islands).  Large matrices are stored as seeded samples plus
+    matrix-vector checksums (_pin)."""
+    sys.path.insert(0, ROOT)
+    _import_reference(ref_root)
+    from scipy.io import loadmat
+    from scipy.linalg import expm
+    from khepri.tmat.lattice import CartesianLattice
+    from khepri.tmat.tools import epsilon_g, grid_size, coords_from_index
+    from khepri.tmat.matrices import matrix_a, matrix_s, multS
+    from khepri.fourier import transform
+    fx = os.path.join(ref_root, "test", "integration", "fixtures", "pair_pw")
+    out = {}
+    # (1) the MATLAB values
+    d = {}
+    for f in ("S", "T", "UV", "epsg", "eta", "gvectors", "kz", "mu", "reciproc", "interface", "fourier"):
+        d.update({k: v for k, v in loadmat(os.path.join(fx, f + ".mat")).items() if not k.startswith("__")})
+    for k in ("A", "Tslice", "Sslice", "T_xyz", "U_in", "V_in", "V_em", "S_interface"):
+        _pin(out, "mat_" + k, d[k], rng_seed=1)
+    for k in ("eps_g", "epsinv_g", "etagx", "etagy", "gx", "gy", "Gx", "Gy", "kgz_in", "kgz_em", "mugx_in",
+              "mugy_in", "b1", "b2"):
+        out["mat_" + k] = np.asarray(d[k])
+    out["mat_Omega_g"] = np.vectorize(lambda c: complex(np.asarray(c).item()), otypes=[complex])(d["Omega_g"])
+    # (2) the reference on pw 5x5, oblique incidence, a disc and a rectangle
+    pw, a, wl, kp, depth, sp = (5, 5), 100e-9, 310e-9, (2.1e6, -1.3e6), 80e-9, 2
+    lat = CartesianLattice(pw, a1=(a, 0.0), a2=(0.0, a), eps_emerg=2.25, eps_incid=1.0, dtype=np.float64)
+    isl = [(transform("disc", [0.3 * a, 0.45 * a, 0.22 * a], lat.Gx, lat.Gy, lat.area), 6.0),
+           (transform("rectangle", [0.6 * a, 0.1 * a, 0.9 * a, 0.35 * a], lat.Gx, lat.Gy, lat.area), 3.0 + 0.1j)]
+    _, q = grid_size(pw)
+    epsg = epsilon_g(q, isl, 1.5)
+    iepsg = epsilon_g(q, isl, 1.5, inverse=True)
+    nx, ny = lat.gx.shape[0] // 2, lat.gx.shape[1] // 2
+    ind = np.array([coords_from_index(pw, (nx, ny), i) for i in range(pw[0] * pw[1])])
+    A = matrix_a(ind, lat.gx, lat.gy, epsg, iepsg, wl, kx=kp[0], ky=kp[1])
+    E = expm(-A * (depth / 2 ** sp))
+    U, Vi, Ve = lat.U(wl, kp), lat.Vi(wl, kp), lat.Ve(wl, kp)
+    T = U @ E @ Vi
+    S = matrix_s(T)
+    for _ in range(sp):
+        S = multS(S, S)
+    Si = matrix_s(U @ Ve)
+    out.update({"ref_pw": np.array(pw), "ref_a": a, "ref_wl": wl, "ref_kp": np.array(kp), "ref_depth": depth,
+                "ref_slicing": sp, "ref_eps_incid": 1.0, "ref_eps_emerg": 2.25, "ref_eps_host": 1.5,
+                "ref_epsg": epsg, "ref_iepsg": iepsg, "ref_gx": lat.gx, "ref_gy": lat.gy, "ref_Gx": lat.Gx,
+                "ref_Gy": lat.Gy})
+    for k, M in (("A", A), ("E", E), ("U", U), ("Vi", Vi), ("Ve", Ve), ("T", T), ("S", S), ("Sint", Si)):
+        _pin(out, "ref_" + k, M, rng_seed=2)
+    np.savez_compressed(os.path.join(HERE, "tmat.npz"), **out)
+    print("tmat: MATLAB pair_pw pins and a 5x5 reference case;", A.shape)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "analytical":
+    if len(sys.argv) > 2 and sys.argv[2] == "tmat":
+        tmat(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "beams":
+        beams(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "bands":
+        bands(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "analytical":
         analytical(sys.argv[1])
     elif len(sys.argv) > 2 and sys.argv[2] == "twisted":
         twisted(sys.argv[1])

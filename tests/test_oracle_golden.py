@@ -185,3 +185,79 @@ def test_oracle_analytical_layers(golden):
             cl.solve()
             r, t = cl.poynting_flux_end()
             assert abs(r - g[tag + "_RT"][k, 0]) < 1e-10 and abs(t - g[tag + "_RT"][k, 1]) < 1e-10
+
+
+def test_oracle_band_structure_matches_reference(golden):
+    """eigentricks.py: pencil eigenvalues, determinant and band_structure of dense global
+    S-matrices from the reference's Crystal solve (tests/golden/bands_3x3.npz)."""
+    g = golden("bands_3x3")
+    for i in range(len(g["S"])):
+        w, v, d = ko.scattering_eigenvalues(g["S"][i], dos=True)
+        assert ko.match_eigenvalues(w, g["w"][i]) < 1e-9
+        assert abs(d - g["det"][i]) <= 1e-9 * abs(g["det"][i])
+        Sl, Sr = ko.scattering_splitlr(g["S"][i])
+        assert np.abs(Sl @ v - (Sr @ v) * w).max() < 1e-9
+        assert ko.band_structure(g["S"][i]).size == g["band_counts"][i]
+
+
+def test_oracle_beams_match_reference(golden):
+    """beams.py: amplitudes_from_fields (square and rectangular supercells, with the reference's
+    cell pairing) and gen_bzi_grid (tests/golden/beams.npz)."""
+    g = golden("beams")
+    for name in ("sq", "rect"):
+        F = ko.amplitudes_from_fields(g[f"{name}_fields"], g[f"{name}_g"], g[f"{name}_kp"], g[f"{name}_x"],
+                                      g[f"{name}_y"], tuple(g[f"{name}_bzs"]))
+        assert np.abs(F - g[f"{name}_F"]).max() < 1e-12 * np.abs(g[f"{name}_F"]).max()
+    assert np.allclose(ko.gen_bzi_grid((4, 3)), g["grid_a"], rtol=0, atol=1e-15)
+    assert np.allclose(ko.gen_bzi_grid((3, 3), a=2), g["grid_b"], rtol=0, atol=1e-15)
+    assert np.allclose(ko.gen_bzi_grid((2, 5), reciproc=((1.0, 0.5), (-0.3, 2.0))), g["grid_c"], rtol=0, atol=1e-15)
+
+
+
+def test_oracle_tmat_matches_matlab_and_reference(golden):
+    """tmat formulation: the oracle against the reference's MATLAB fixtures (fixtures/pair_pw,
+    with the reference test's tolerances, test_pair_pw.py:40-131) and against the reference run
+    on a 5x5 oblique two-island case (tests/golden/tmat.npz)."""
+    from pins import check_pinned
+    g = golden("tmat")
+    pw, a, wl, kp, depth, sp = (8, 8), 100e-9, 200e-9, (0.0, 0.0), 1e-7, 3
+    lat = ko.tmat_lattice(pw, (a, 0.0), (0.0, a))
+    assert np.allclose(lat.b1, g["mat_b1"]) and np.allclose(lat.b2, g["mat_b2"])
+    assert np.allclose(lat.gx, g["mat_gx"]) and np.allclose(lat.gy, g["mat_gy"])
+    assert np.allclose(lat.Gx, g["mat_Gx"]) and np.allclose(lat.Gy, g["mat_Gy"])
+    disc = {"type": "disc", "params": (0.5 * a, 0.5 * a, 0.2 * a)}
+    bf = ko.island_transform(disc, lat.Gx, lat.Gy, lat.area)
+    assert np.allclose(bf, g["mat_Omega_g"], rtol=1e-7)
+    _, q = ko.tmat_grid_size(pw)
+    epsg = ko.tmat_epsilon_g(q, [(bf, 8.9)], 1.0)
+    iepsg = ko.tmat_epsilon_g(q, [(bf, 8.9)], 1.0, inverse=True)
+    assert np.allclose(epsg, g["mat_eps_g"], rtol=1e-7) and np.allclose(iepsg, g["mat_epsinv_g"], rtol=1e-7)
+    kz = ko.tmat_kz(lat.gx, lat.gy, 1.0, wl, kp)
+    assert np.allclose(kz, g["mat_kgz_in"], rtol=1e-7)
+    eta = ko.tmat_eta(lat.gx, lat.gy, kp)
+    assert np.allclose(eta[0], g["mat_etagx"], rtol=1e-7) and np.allclose(eta[1], g["mat_etagy"], rtol=1e-7)
+    U, Vi, Ve = ko.tmat_uv(lat, wl, kp, 1.0, 1.0)
+    check_pinned(g, "mat_U_in", U, 1, rtol=1e-7)
+    check_pinned(g, "mat_V_in", Vi, 1, rtol=1e-7)
+    A = ko.tmat_matrix_a(pw, lat.gx, lat.gy, epsg, iepsg, wl, kp)
+    check_pinned(g, "mat_A", A, 1, rtol=1e-7)
+    S, E = ko.tmat_layer_smatrix(A, U, Vi, depth, sp)
+    # numpy's assert_allclose defaults (rtol 1e-7) with the test's atol values
+    check_pinned(g, "mat_T_xyz", E, 1, rtol=1e-7, atol=1e-10)
+    check_pinned(g, "mat_Tslice", U @ E @ Vi, 1, rtol=1e-7, atol=4e-10)
+    check_pinned(g, "mat_Sslice", S, 1, rtol=1e-7, atol=1e-11)
+    check_pinned(g, "mat_S_interface", ko.tmat_matrix_s(U @ Ve), 1, rtol=1e-7, atol=1e-12)
+    # the reference itself on pw 5x5, oblique kp, a disc and a lossy rectangle
+    pw = tuple(g["ref_pw"])
+    a, wl, kp, depth, sp = float(g["ref_a"]), float(g["ref_wl"]), tuple(g["ref_kp"]), float(g["ref_depth"]), \
+        int(g["ref_slicing"])
+    lat = ko.tmat_lattice(pw, (a, 0.0), (0.0, a))
+    assert np.allclose(lat.gx, g["ref_gx"]) and np.allclose(lat.Gy, g["ref_Gy"])
+    A = ko.tmat_matrix_a(pw, lat.gx, lat.gy, g["ref_epsg"], g["ref_iepsg"], wl, kp)
+    check_pinned(g, "ref_A", A, 2, rtol=1e-12)
+    U, Vi, Ve = ko.tmat_uv(lat, wl, kp, float(g["ref_eps_incid"]), float(g["ref_eps_emerg"]))
+    for name, M in (("ref_U", U), ("ref_Vi", Vi), ("ref_Ve", Ve)):
+        check_pinned(g, name, M, 2, rtol=1e-12)
+    S, E = ko.tmat_layer_smatrix(A, U, Vi, depth, sp)
+    check_pinned(g, "ref_E", E, 2, rtol=1e-10, atol=1e-12)
+    check_pinned(g, "ref_S", S, 2, rtol=1e-9, atol=1e-11)
