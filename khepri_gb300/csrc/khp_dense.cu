@@ -31,8 +31,23 @@ __global__ void __launch_bounds__(kTeamThreads) k_getrs(int n, const cplx<T>* A,
   team_getrs(t, A + b * bsA, lda, n, piv + b * n, B + b * bsB, ldb, m);
 }
 
-// Schur form and eigenvectors of the triangular factor (X left in A, Q in Z); the back-transform
-// W = Z X runs afterwards as a batched tiled product.
+// Hessenberg reduction, Q in Z: blocked (panels of KHP_GEHRD_NB reflectors, scratch in W) when
+// the matrix is large enough for it, else one reflector at a time.
+template <typename T>
+__global__ void __launch_bounds__(kTeamThreads, 3) k_gehrd(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
+                                                         cplx<T>* W, int64_t ldw, int64_t bsW, int blocked) {
+  __shared__ TeamShared sh;
+  extern __shared__ unsigned char dyn[];
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  if (blocked)
+    team_gehrd_blocked(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, W + b * bsW, ldw, &sh);
+  else
+    team_gehrd(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, reinterpret_cast<cplx<T>*>(dyn), &sh);
+}
+
+// Schur form of the Hessenberg matrix and eigenvectors of the triangular factor (X left in A,
+// Q in Z); the back-transform W = Z X runs afterwards as a batched tiled product.
 template <typename T>
 __global__ void __launch_bounds__(kTeamThreads) k_geev_schur(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
                                                               cplx<T>* lam, int64_t bsLam, int* info) {
@@ -40,13 +55,10 @@ __global__ void __launch_bounds__(kTeamThreads) k_geev_schur(int n, cplx<T>* A, 
   __shared__ cplx<T> win[(KHP_HQR_WIN + 2) * (KHP_HQR_WIN + 2)];
   __shared__ cplx<T> rs[KHP_HQR_WIN];
   __shared__ T rc[KHP_HQR_WIN];
-  extern __shared__ unsigned char dyn[];
-  cplx<T>* vbuf = reinterpret_cast<cplx<T>*>(dyn);
   TeamCta t;
   const int64_t b = blockIdx.x;
   cplx<T>* Ab = A + b * bsA;
   cplx<T>* Zb = Z + b * (int64_t)n * n;
-  team_gehrd(t, Ab, lda, n, Zb, n, vbuf, &sh);
   const int st = team_hqr_win(t, Ab, lda, n, Zb, n, win, rc, rs, &sh);
   team_trevc(t, Ab, lda, n, lam + b * bsLam);
   if (threadIdx.x == 0 && st) info[b] |= st;
@@ -335,12 +347,15 @@ template <typename T>
 int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
                 int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
-  const size_t smem = sizeof(cplx<T>) * (size_t)n;  // Householder vector
+  // blocked reduction when W can hold its scratch (ldw >= 3 NB + 2 columns) and panels pay off
+  const int blocked = (n >= 64 && ldw >= 3 * KHP_GEHRD_NB + 2) ? 1 : 0;
+  const size_t smem = blocked ? 0 : sizeof(cplx<T>) * (size_t)n;  // unblocked: Householder vector
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_geev_schur<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      cudaFuncSetAttribute(k_gehrd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
-  k_geev_schur<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
-  count_launches(1);
+  k_gehrd<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, W, ldw, bsW, blocked);
+  k_geev_schur<T><<<(unsigned)batch, kTeamThreads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
+  count_launches(2);
   int st = cuda_status();
   if (st) return st;
   // W = Z X (X unit upper triangular, stored in A) and unit columns

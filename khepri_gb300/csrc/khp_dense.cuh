@@ -216,6 +216,201 @@ KHP_HD void team_gemm(const Team& t, int n, int m, int k, cplx<T> alpha, const c
 }
 
 // ------------------------------------------------------------------------------------------
+// Blocked Hessenberg reduction (same reflectors as team_gehrd, applied in panels of KHP_GEHRD_NB
+// columns).  With Q_b = H_0 ... H_{nb-1} = I - V T V^H for the panel's reflectors (V unit lower
+// trapezoidal, T upper triangular), the panel is reduced column by column against
+// Y = A V T (A: the matrix before the panel):
+//   column c_j of A Q_j = A[:, c_j] - Y_j conj(V[c_j, 0:j]),   then Q_j^H from the left;
+//   Y[:, j] = tau_j (A v_j - Y_j (V_j^H v_j)),   T[0:j, j] = -tau_j T_j (V_j^H v_j);
+// and only then is the rest of the matrix updated, once per panel:
+//   A[:, J] -= Y V[J, :]^H (right), A[c0+1:, J] -= V T^H (V^H A[c0+1:, J]) (left),
+//   Z[:, c0+1:] -= (Z V T) V^H.
+// Each column costs one pass over the matrix (A v_j) instead of three read-write passes over
+// the matrix and Z.  The reflectors are stored below the subdiagonal (cleared at the end).
+// Scratch (ldw-strided, n rows): Y in columns [0, NB), T in rows [0, NB) of columns [2 NB, 3 NB),
+// vectors w, u in columns 3 NB and 3 NB + 1: needs ldw >= 3 NB + 2 and n >= NB.
+// ------------------------------------------------------------------------------------------
+#ifndef KHP_GEHRD_NB
+#define KHP_GEHRD_NB 8
+#endif
+
+template <class Team, typename T>
+KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* W,
+                               int64_t ldw, TeamShared* sh) {
+  // panel width (the per-thread accumulators of the panel updates stay in registers)
+  constexpr int NB = KHP_GEHRD_NB;
+  const int lanes = t.size() < 32 ? t.size() : 32;
+  const int lane = t.tid() % lanes, warp = t.tid() / lanes, nwarps = t.size() / lanes;
+  cplx<T>* Y = W;                   // Y[i][l] = W[i * ldw + l]
+  cplx<T>* Tm = W + 2 * NB;         // Tm[m][l] = W[m * ldw + 2 NB + l]
+  cplx<T>* wv = W + 3 * NB;         // wv[l] = W[l * ldw + 3 NB]
+  cplx<T>* uv = W + 3 * NB + 1;     // uv[l] = W[l * ldw + 3 NB + 1]
+  team_set_identity(t, Z, ldz, n, n);
+  for (int c0 = 0; c0 + 2 < n; c0 += NB) {
+    const int nb = (n - 2 - c0) < NB ? (n - 2 - c0) : NB;
+    // V(i, l) of reflector l (column c0 + l): 0 above row c0 + l + 1, 1 there, stored below
+    auto V = [&](int i, int l) -> cplx<T> {
+      const int cl = c0 + l;
+      return i <= cl ? mk(T(0)) : (i == cl + 1 ? mk(T(1)) : H[(int64_t)i * ld + cl]);
+    };
+    for (int j = 0; j < nb; ++j) {
+      const int c = c0 + j;
+      if (j > 0) {
+        // column c of A Q_j: b = A[:, c] - Y_j conj(V[c, 0:j]) (every row)
+        for (int i = t.tid(); i < n; i += t.size()) {
+          cplx<T> acc = H[(int64_t)i * ld + c];
+          for (int l = 0; l < j; ++l) acc -= mul_conj(Y[(int64_t)i * ldw + l], V(c, l));
+          H[(int64_t)i * ld + c] = acc;
+        }
+        t.sync();
+        // w = V_j^H b (rows c0+1..), then w = T_j^H w, then b -= V_j w
+        for (int l = warp; l < j; l += nwarps) {
+          cplx<T> acc = mk(T(0));
+          for (int i = c0 + 1 + lane; i < n; i += lanes) acc += conj_mul(V(i, l), H[(int64_t)i * ld + c]);
+          acc = warp_sum(t, acc);
+          if (lane == 0) wv[(int64_t)l * ldw] = acc;
+        }
+        t.sync();
+        if (t.tid() == 0) {
+          for (int l = j - 1; l >= 0; --l) {  // in place, highest first: (T^H w)_l = sum_{m<=l} conj(T_ml) w_m
+            cplx<T> acc = mk(T(0));
+            for (int m = 0; m <= l; ++m) acc += conj_mul(Tm[(int64_t)m * ldw + l], wv[(int64_t)m * ldw]);
+            wv[(int64_t)l * ldw] = acc;
+          }
+        }
+        t.sync();
+        for (int i = c0 + 1 + t.tid(); i < n; i += t.size()) {
+          cplx<T> acc = H[(int64_t)i * ld + c];
+          for (int l = 0; l < j; ++l) acc -= V(i, l) * wv[(int64_t)l * ldw];
+          H[(int64_t)i * ld + c] = acc;
+        }
+        t.sync();
+      }
+      // reflector of column c (rows c+1..)
+      T s = T(0);
+      for (int i = c + 2 + t.tid(); i < n; i += t.size()) s += norm2(H[(int64_t)i * ld + c]);
+      s = team_sum(t, s, sh);
+      const cplx<T> alpha = H[(int64_t)(c + 1) * ld + c];
+      cplx<T> tau = mk(T(0));
+      if (!(s == T(0) && alpha.im == T(0))) {
+        const T beta = -copysign(sqrt(norm2(alpha) + s), alpha.re);
+        tau = mk((beta - alpha.re) / beta, -alpha.im / beta);
+        const cplx<T> scal = cdiv(mk(T(1)), alpha - mk(beta));
+        t.sync();  // every thread has read alpha
+        for (int i = c + 2 + t.tid(); i < n; i += t.size()) H[(int64_t)i * ld + c] = H[(int64_t)i * ld + c] * scal;
+        if (t.tid() == 0) H[(int64_t)(c + 1) * ld + c] = mk(beta);
+      }
+      t.sync();
+      // Y[:, j] = tau (A v - Y_j u), u = V_j^H v;  v = V(., j), A = columns c+1.. of H
+      for (int i = t.tid(); i < n; i += t.size()) {
+        const cplx<T>* row = H + (int64_t)i * ld;
+        cplx<T> acc = row[c + 1];
+        for (int col = c + 2; col < n; ++col) fma_acc(acc, row[col], H[(int64_t)col * ld + c]);
+        Y[(int64_t)i * ldw + j] = acc;
+      }
+      for (int l = warp; l < j; l += nwarps) {
+        cplx<T> acc = mk(T(0));
+        for (int i = c + 1 + lane; i < n; i += lanes) acc += conj_mul(V(i, l), V(i, j));
+        acc = warp_sum(t, acc);
+        if (lane == 0) uv[(int64_t)l * ldw] = acc;
+      }
+      t.sync();
+      for (int i = t.tid(); i < n; i += t.size()) {
+        cplx<T> acc = Y[(int64_t)i * ldw + j];
+        for (int l = 0; l < j; ++l) acc -= Y[(int64_t)i * ldw + l] * uv[(int64_t)l * ldw];
+        Y[(int64_t)i * ldw + j] = tau * acc;
+      }
+      if (t.tid() == 0) {  // T[0:j, j] = -tau T_j u ; T[j][j] = tau
+        for (int m = 0; m < j; ++m) {
+          cplx<T> acc = mk(T(0));
+          for (int l = m; l < j; ++l) fma_acc(acc, Tm[(int64_t)m * ldw + l], uv[(int64_t)l * ldw]);
+          Tm[(int64_t)m * ldw + j] = -(tau * acc);
+        }
+        Tm[(int64_t)j * ldw + j] = tau;
+        for (int m = j + 1; m < NB; ++m) Tm[(int64_t)m * ldw + j] = mk(T(0));
+      }
+      t.sync();
+    }
+    const int J0 = c0 + nb;
+    // right: A[:, J] -= Y V[J, :]^H for the columns after the panel
+    if (J0 < n) {
+      const int m = n - J0;
+      for (int e = t.tid(); e < n * m; e += t.size()) {
+        const int i = e / m, J = J0 + e % m;
+        cplx<T> acc = H[(int64_t)i * ld + J];
+        for (int l = 0; l < nb; ++l) acc -= mul_conj(Y[(int64_t)i * ldw + l], V(J, l));
+        H[(int64_t)i * ld + J] = acc;
+      }
+      t.sync();
+      // left: A[c0+1:, J] -= V T^H (V^H A[c0+1:, J]), thread per column
+      for (int J = J0 + t.tid(); J < n; J += t.size()) {
+        cplx<T> x[NB];
+#pragma unroll
+        for (int l = 0; l < NB; ++l) x[l] = mk(T(0));
+        for (int i = c0 + 1; i < n; ++i) {
+          const cplx<T> a = H[(int64_t)i * ld + J];
+#pragma unroll
+          for (int l = 0; l < NB; ++l)
+            if (l < nb) x[l] += conj_mul(V(i, l), a);
+        }
+#pragma unroll
+        for (int l = NB - 1; l >= 0; --l) {
+          if (l >= nb) continue;
+          cplx<T> acc = mk(T(0));
+#pragma unroll
+          for (int q = 0; q < NB; ++q)
+            if (q <= l) acc += conj_mul(Tm[(int64_t)q * ldw + l], x[q]);
+          x[l] = acc;
+        }
+        for (int i = c0 + 1; i < n; ++i) {
+          cplx<T> acc = H[(int64_t)i * ld + J];
+#pragma unroll
+          for (int l = 0; l < NB; ++l)
+            if (l < nb) acc -= V(i, l) * x[l];
+          H[(int64_t)i * ld + J] = acc;
+        }
+      }
+    }
+    // Z[:, c0+1:] -= (Z V T) V^H, thread per row of Z
+    for (int i = t.tid(); i < n; i += t.size()) {
+      cplx<T>* zr = Z + (int64_t)i * ldz;
+      cplx<T> x[NB];
+#pragma unroll
+      for (int l = 0; l < NB; ++l) x[l] = mk(T(0));
+      for (int col = c0 + 1; col < n; ++col) {
+        const cplx<T> z = zr[col];
+#pragma unroll
+        for (int l = 0; l < NB; ++l)
+          if (l < nb) fma_acc(x[l], z, V(col, l));
+      }
+#pragma unroll
+      for (int l = NB - 1; l >= 0; --l) {  // x <- x T (upper triangular), highest first
+        if (l >= nb) continue;
+        cplx<T> acc = mk(T(0));
+#pragma unroll
+        for (int q = 0; q < NB; ++q)
+          if (q <= l) fma_acc(acc, x[q], Tm[(int64_t)q * ldw + l]);
+        x[l] = acc;
+      }
+      for (int col = c0 + 1; col < n; ++col) {
+        cplx<T> acc = zr[col];
+#pragma unroll
+        for (int l = 0; l < NB; ++l)
+          if (l < nb) acc -= mul_conj(x[l], V(col, l));
+        zr[col] = acc;
+      }
+    }
+    t.sync();
+  }
+  // clear the reflector storage below the subdiagonal
+  for (int e = t.tid(); e < n * n; e += t.size()) {
+    const int i = e / n, j = e % n;
+    if (i > j + 1) H[(int64_t)i * ld + j] = mk(T(0));
+  }
+  t.sync();
+}
+
+// ------------------------------------------------------------------------------------------
 // Hessenberg reduction by Householder reflectors, H = Q^H A Q, Q accumulated into Z.
 // Reflector convention: P = I - tau u u^H with u = [1, v], beta real, P^H [alpha; x] = [beta; 0].
 // vbuf: n complex of scratch.
