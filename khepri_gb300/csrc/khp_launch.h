@@ -71,6 +71,7 @@ struct OzakiWs {
   size_t bd_elems = 0;
   int* eb = nullptr;   // B column exponents
   size_t eb_n = 0;
+  int* err = nullptr;  // one int: set when a tensor-core tile timed out (the tcgen05 path)
 };
 constexpr int64_t kOzakiMaxChunk = 256;  // problems per chunk (digit arrays: ~5.5 MB per 242 x 242 problem)
 size_t ozaki_a_elems(int m, int k);  // per problem
@@ -81,6 +82,19 @@ int64_t ozaki_chunk(int64_t batch);  // problems per chunk for a batch (even spl
 int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64_t lda, int64_t bsA, const int* aidx,
                 const cplx<double>* B, int64_t ldb, int64_t bsB, cplx<double>* C, int64_t ldc, int64_t bsC,
                 const OzakiWs& w, cudaStream_t s);
+
+// The same exact digit products on tcgen05 with TMEM accumulators (7-bit digits, ND = 8 for an
+// FP64 result, 4 for FP32): C = alpha A B + beta C, A[aidx[b]] and B[bidx[b]] optional gathers.
+// Valid while 2k rounded up to 64 is at most tc_max_k2p(ND); digit arrays in OzakiWs sized by
+// tc_a_elems / tc_b_elems (per problem), exponents by tc_rows_padded(m) and n.
+int tc_max_k2p(int nd);
+size_t tc_a_elems(int nd, int m, int k);
+size_t tc_b_elems(int nd, int k, int n);
+int tc_rows_padded(int m);
+template <int ND, typename TI, typename TO>
+int tc_product(int64_t batch, int m, int n, int k, const cplx<TI>* A, int64_t lda, int64_t bsA, const int* aidx,
+               const cplx<TI>* B, int64_t ldb, int64_t bsB, const int* bidx, cplx<TO> alpha, cplx<TO> beta,
+               cplx<TO>* C, int64_t ldc, int64_t bsC, const OzakiWs& w, cudaStream_t s);
 
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 

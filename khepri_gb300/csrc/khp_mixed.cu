@@ -814,6 +814,7 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
     p.oz.bd = a.take<uint16_t>(p.oz.bd_elems);
     p.oz.eb_n = ch * n;
     p.oz.eb = a.take<int>(p.oz.eb_n);
+    p.oz.err = a.take<int>(1);
   }
   p.kpx = a.take<double>(bm * 4);
   p.k0x = a.take<double>(bm);

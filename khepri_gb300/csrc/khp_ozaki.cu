@@ -396,9 +396,9 @@ int product(int64_t batch, int m, int n, int k, const void* Ad, const int* ea, c
 
 }  // namespace
 
-size_t ozaki_a_elems(int m, int k) { return (size_t)kDig * up64(m) * up64(2 * k); }
-size_t ozaki_b_elems(int k, int n) { return (size_t)kDig * up64(2 * n) * up64(2 * k); }
-int ozaki_rows_padded(int m) { return up64(m); }
+size_t ozaki_a_elems(int m, int k) { return std::max((size_t)kDig * up64(m) * up64(2 * k), tc_a_elems(8, m, k)); }
+size_t ozaki_b_elems(int k, int n) { return std::max((size_t)kDig * up64(2 * n) * up64(2 * k), tc_b_elems(8, k, n)); }
+int ozaki_rows_padded(int m) { return std::max(up64(m), tc_rows_padded(m)); }
 
 int64_t ozaki_chunk(int64_t batch) {
   const int64_t parts = (batch + kOzakiMaxChunk - 1) / kOzakiMaxChunk;
@@ -411,8 +411,14 @@ int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64
   if (batch <= 0 || m <= 0 || n <= 0) return KHP_OK;
   // the int32 level sums stay below 2.25 * 2^16 * K2p, under 2^31 for k <= 4096
   if (k <= 0 || k > 4096) return KHP_ERR_INVALID_ARG;
-  const int64_t cap = std::min(std::min<int64_t>((int64_t)(w.ad_elems / ozaki_a_elems(m, k)), (int64_t)(w.ea_n / up64(m))),
-                               std::min<int64_t>((int64_t)(w.bd_elems / ozaki_b_elems(k, n)), (int64_t)(w.eb_n / n)));
+  // tcgen05 with TMEM level accumulators where its exactness bound and the scratch allow
+  if (w.err && up64(2 * k) <= tc_max_k2p(8) && w.ad_elems >= tc_a_elems(8, m, k) &&
+      w.bd_elems >= tc_b_elems(8, k, n) && w.ea_n >= (size_t)tc_rows_padded(m) && w.eb_n >= (size_t)n)
+    return tc_product<8, double, double>(batch, m, n, k, A, lda, bsA, aidx, B, ldb, bsB, nullptr, mk(1.0), mk(0.0), C,
+                                         ldc, bsC, w, s);
+  const int64_t per_a = (int64_t)kDig * up64(m) * up64(2 * k), per_b = (int64_t)kDig * up64(2 * n) * up64(2 * k);
+  const int64_t cap = std::min(std::min<int64_t>((int64_t)(w.ad_elems / per_a), (int64_t)(w.ea_n / up64(m))),
+                               std::min<int64_t>((int64_t)(w.bd_elems / per_b), (int64_t)(w.eb_n / n)));
   const int64_t chunk = std::min(cap, ozaki_chunk(batch));
   if (chunk <= 0) return KHP_ERR_WORKSPACE;
   stage_begin(KHP_STAGE_TC_PRODUCT, s);
@@ -435,7 +441,7 @@ using namespace khp;
 namespace {
 
 struct WsLayout {
-  size_t ad, ea, bd, eb, total;
+  size_t ad, ea, bd, eb, err, total;
 };
 
 WsLayout abi_layout(int64_t chunk, int m, int n, int k) {
@@ -445,7 +451,8 @@ WsLayout abi_layout(int64_t chunk, int m, int n, int k) {
   l.ea = l.ad + al((size_t)chunk * ozaki_a_elems(m, k) * 2);
   l.bd = l.ea + al((size_t)chunk * ozaki_rows_padded(m) * sizeof(int));
   l.eb = l.bd + al((size_t)chunk * ozaki_b_elems(k, n) * 2);
-  l.total = l.eb + al((size_t)chunk * n * sizeof(int));
+  l.err = l.eb + al((size_t)chunk * n * sizeof(int));
+  l.total = l.err + al(sizeof(int));
   return l;
 }
 
@@ -477,6 +484,7 @@ int khp_zgemm_fp64_tc(int64_t batch, int32_t m, int32_t n, int32_t k, const doub
   w.bd_elems = (size_t)chunk * ozaki_b_elems(k, n);
   w.eb = reinterpret_cast<int*>(base + l.eb);
   w.eb_n = (size_t)chunk * n;
+  w.err = reinterpret_cast<int*>(base + l.err);
   return ozaki_zgemm(batch, m, n, k, reinterpret_cast<const cd*>(A), lda, bsA, nullptr,
                      reinterpret_cast<const cd*>(B), ldb, bsB, reinterpret_cast<cd*>(C), ldc, bsC, w,
                      reinterpret_cast<cudaStream_t>(stream));
