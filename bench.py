@@ -10,8 +10,8 @@ polarisations from one S-matrix per problem.  A step solves one chunk of ``--bat
   timed with CUDA events over exactly K steps (barrier + synchronize on both sides).
 * e2e: the same metric through the public batched API (khepri_gb300.batch.solve_rt) from host
   numpy inputs to host R/T, host<->device copies inside the timed region.
-* roofline: the dominant kernel, the FP32 eigensolver of the modes stage (k_geev_schur): its
-  algorithmic flops per launch (100 n^3 per matrix) / its mean launch duration, timed by CUDA
+* roofline: the dominant kernels, the FP32 eigensolver of the modes stage (k_gehrd +
+  k_geev_schur): its algorithmic flops per call (100 n^3 per matrix) / its mean launch duration, timed by CUDA
   events that libkhp records on its stream around each stage (khp_stage_timing), against the
   FP32 FMA throughput measured in this run (khp_probe_fp32_tflops).  The per-stage times and
   the tensor-core products' fraction of the bf16 peak ride along.
@@ -54,10 +54,16 @@ def _up64(x):
     return (x + 63) // 64 * 64
 
 
-# bf16 tensor flops issued per modes matrix by the FP64-accurate products of the mixed solve:
-# M W twice (m = k = n) and C W twice (m = k = n/2, 2n real columns), 28 digit pairs each
-TC_FLOPS_PER_MATRIX = 28 * 2 * (2 * _up64(N_MAT) * _up64(2 * N_MAT) * _up64(2 * N_MAT)
-                                + 2 * _up64(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
+def _up128(x):
+    return (x + 127) // 128 * 128
+
+
+# bf16 tensor flops issued per modes matrix by the FP64-accurate products of the mixed solve
+# (k_tc_digits: 8 digits, the 36 pairs i + j < 8, rows padded to 128, real columns and inner
+# index to 64): M W twice (m = k = n) and C W twice (m = k = n/2, n complex columns)
+TC_PAIRS = 36
+TC_FLOPS_PER_MATRIX = TC_PAIRS * 2 * (2 * _up128(N_MAT) * _up64(2 * N_MAT) * _up64(2 * N_MAT)
+                                      + 2 * _up128(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
 BF16_PEAK = 1935.4  # TFLOP/s, MEASURED_PEAKS.json bf16_tflops (burst)
 # DRAM bytes per matrix of the FP32 eigensolver (read + write) at 456 matrices per launch, from
 # one ncu capture (profiles/geev_fp32_n242_batch456_traffic.md): 364.1 GB / 456
@@ -423,8 +429,8 @@ def run_gpu(args):
                               "config": {"batch": B, "problems_with_status": bad}}), flush=True)
         return
 
-    # roofline of the dominant kernel: the FP32 eigensolver of the modes stage (k_geev_schur,
-    # ~40 % of the step in the launch list), timed live by the library's stage events
+    # roofline of the dominant kernels: the FP32 eigensolver of the modes stage (k_gehrd +
+    # k_geev_schur, ~32 % of the step in the launch list), timed live by the library's stage events
     scratch = torch.empty(2048 * 1024, dtype=torch.float64, device=dev)
     fp64_peak = lib.khp_probe_fp64_tflops(_capi.ptr(scratch), scratch.numel(), _capi.stream_ptr())
     fp32_peak = lib.khp_probe_fp32_tflops(_capi.ptr(scratch), 2 * scratch.numel(), _capi.stream_ptr())
@@ -436,7 +442,7 @@ def run_gpu(args):
         achieved = eig_flops / (eig_ms / eig_calls * 1e-3) / 1e12
         stages = {k: {"ms_per_call": v[0] / args.steps, "share": round(v[0] / ms, 4)}
                   for k, v in stage_ms.items() if v[1] > 0}
-        roof = {"bound": "fp32", "kernel": "k_geev_schur<float> (eigensolve stage of khp_solve_batched_mixed)",
+        roof = {"bound": "fp32", "kernel": "k_gehrd<float> + k_geev_schur<float> (eigensolve stage of khp_solve_batched_mixed)",
                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak > 0 else None,
                 "traffic": GEEV_TRAFFIC_PER_MATRIX * mats if GEEV_TRAFFIC_PER_MATRIX else None,
@@ -453,9 +459,9 @@ def run_gpu(args):
             tc_flops = mats * TC_FLOPS_PER_MATRIX
             tc_rate = tc_flops / (tc_ms / args.steps * 1e-3) / 1e12
             roof["tensor_stage"] = {
-                "bound": "tensor", "kernel": "k_ozaki_gemm (FP64-accurate products M W, C W on bf16 mma.sync)",
+                "bound": "tensor", "kernel": "k_tc_digits (FP64-accurate products M W, C W: tcgen05 bf16 digit products in TMEM)",
                 "achieved": tc_rate, "peak": BF16_PEAK, "unit": "TFLOP/s", "frac": tc_rate / BF16_PEAK,
-                "flops": "bf16 flops issued: 28 digit pairs x 2 Mp N2p K2p per product (padded to 64)",
+                "flops": "bf16 flops issued: 36 digit pairs x 2 Mp N2p K2p per product (rows padded to 128, columns and inner index to 64)",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
                 "fp64_equivalent_tflops": mats * 20.0 * N_MAT ** 3 / (tc_ms / args.steps * 1e-3) / 1e12}
 
