@@ -231,6 +231,120 @@ __global__ void __launch_bounds__(256) k_panel_lu(int n, int kb, int w, cplx<T>*
   if (threadIdx.x == 0 && st) info[b] |= st;
 }
 
+// The same panel factorisation with the panel in registers: thread i holds row kb + i (needs
+// n - kb <= 256 and w <= KHP_NB).  Per column: a team argmax (ties to the lower row), the pivot
+// row and row jj exchanged through shared memory, then each thread scales and updates its own
+// row from the pivot row (a shared-memory broadcast).  Two barriers per column and no shared-memory
+// traffic for the elimination itself.  Same pivots, same order of operations per element as
+// k_panel_lu.
+template <typename T>
+__global__ void __launch_bounds__(256, 3) k_panel_lu_reg(int n, int kb, int w, cplx<T>* A, int64_t lda, int64_t bsA,
+                                                         int* piv, int* info) {
+  __shared__ cplx<T> prow[KHP_NB], srow[KHP_NB];
+  __shared__ T wv[8];
+  __shared__ int wi[8];
+  const int64_t b = blockIdx.x;
+  cplx<T>* Ab = A + b * bsA;
+  const int rows = n - kb;
+  const int i = threadIdx.x, lane = i & 31, warp = i >> 5;
+  cplx<T> a[KHP_NB];
+#pragma unroll
+  for (int c = 0; c < KHP_NB; ++c) a[c] = (i < rows && c < w) ? Ab[(int64_t)(kb + i) * lda + kb + c] : mk(T(0));
+  int st = 0;
+  // a[] is only indexed by compile-time c (selects against jj), so it stays in registers
+#pragma unroll 1
+  for (int jj = 0; jj < KHP_NB; ++jj) {
+    if (jj < w) {
+      cplx<T> ajj = a[0];
+#pragma unroll
+      for (int c = 1; c < KHP_NB; ++c)
+        if (c == jj) ajj = a[c];
+      T v = T(-1);
+      int bi = jj;
+      if (i >= jj && i < rows) {
+        const T x = abs1(ajj);
+        if (x > v) { v = x; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > v || (ov == v && oi < bi)) { v = ov; bi = oi; }
+      }
+      if (lane == 0) { wv[warp] = v; wi[warp] = bi; }
+      __syncthreads();
+      T best = wv[0];
+      int bsel = wi[0];
+#pragma unroll
+      for (int q = 1; q < 8; ++q)
+        if (wv[q] > best || (wv[q] == best && wi[q] < bsel)) { best = wv[q]; bsel = wi[q]; }
+      if (i == 0) piv[b * n + kb + jj] = kb + bsel;
+      if (!(best > T(0))) {
+        st |= (best == T(0)) ? KHP_BIT_SINGULAR : KHP_BIT_NONFINITE;
+        __syncthreads();  // wv / wi are read before the next column writes them
+      } else {
+        if (i == bsel) {
+#pragma unroll
+          for (int c = 0; c < KHP_NB; ++c) prow[c] = a[c];
+        } else if (i == jj) {
+#pragma unroll
+          for (int c = 0; c < KHP_NB; ++c) srow[c] = a[c];
+        }
+        __syncthreads();
+        if (bsel != jj) {
+          if (i == jj) {
+#pragma unroll
+            for (int c = 0; c < KHP_NB; ++c) a[c] = prow[c];
+          } else if (i == bsel) {
+#pragma unroll
+            for (int c = 0; c < KHP_NB; ++c) a[c] = srow[c];
+            ajj = srow[jj];  // this thread now holds the old row jj
+          }
+        }
+        if (i > jj && i < rows) {
+          const cplx<T> l = cdiv(ajj, prow[jj]);
+#pragma unroll
+          for (int c = 0; c < KHP_NB; ++c) {
+            if (c == jj) a[c] = l;
+            else if (c > jj && c < w) fms_acc(a[c], l, prow[c]);
+            // keeps the compiler from hoisting all of prow into registers at once
+            if ((c & 7) == 7) asm volatile("" ::: "memory");
+          }
+        }
+      }
+    }
+  }
+  if (i < rows)
+#pragma unroll
+    for (int c = 0; c < KHP_NB; ++c)
+      if (c < w) Ab[(int64_t)(kb + i) * lda + kb + c] = a[c];
+  if (threadIdx.x == 0 && st) info[b] |= st;
+}
+
+// B = P: the permutation matrix of the row interchanges piv[0:n) applied to the identity (one CTA
+// per matrix; the permutation is resolved in shared memory by one thread, then written row-wise).
+template <typename T>
+__global__ void k_perm_matrix(int n, const int* __restrict__ piv, cplx<T>* B, int64_t ldb, int64_t bsB) {
+  extern __shared__ int perm[];
+  const int64_t b = blockIdx.x;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) perm[r] = r;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < n; ++k) {
+      const int p = piv[b * n + k];
+      if (p != k) {
+        const int t = perm[k];
+        perm[k] = perm[p];
+        perm[p] = t;
+      }
+    }
+  __syncthreads();
+  cplx<T>* Bb = B + b * bsB;
+  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
+    const int r = (int)(e / n), c = (int)(e % n);
+    Bb[(int64_t)r * ldb + c] = (c == perm[r]) ? mk(T(1)) : mk(T(0));
+  }
+}
+
 // Apply the row interchanges piv[k0:k1] to columns [c0, c1) of A (thread per column, in order).
 template <typename T>
 __global__ void k_laswp(int64_t batch, int n, int k0, int k1, int c0, int c1, cplx<T>* A, int64_t lda, int64_t bsA,
@@ -257,9 +371,12 @@ template <typename T>
 __global__ void k_trsm_block(int w, int d0, const cplx<T>* __restrict__ A, int64_t lda, int64_t bsA, int r0, int m,
                              cplx<T>* B, int64_t ldb, int64_t bsB, int lower, int64_t batch) {
   __shared__ cplx<T> Tb[KHP_NB * KHP_NB];
+  __shared__ cplx<T> dinv[KHP_NB];  // reciprocals of the diagonal (upper)
   const int64_t b = blockIdx.y;
   const cplx<T>* Ab = A + b * bsA;
   for (int e = threadIdx.x; e < w * w; e += blockDim.x) Tb[e] = Ab[(int64_t)(d0 + e / w) * lda + d0 + e % w];
+  __syncthreads();
+  if (!lower && threadIdx.x < w) dinv[threadIdx.x] = cdiv(mk(T(1)), Tb[threadIdx.x * w + threadIdx.x]);
   __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
@@ -286,7 +403,7 @@ __global__ void k_trsm_block(int w, int d0, const cplx<T>* __restrict__ A, int64
 #pragma unroll
       for (int k = 0; k < KHP_NB; ++k)
         if (k > ii && k < w) fms_acc(acc, Tb[ii * w + k], x[k]);
-      x[ii] = cdiv(acc, Tb[ii * w + ii]);
+      x[ii] = acc * dinv[ii];
     }
   }
 #pragma unroll
@@ -326,13 +443,19 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
                 cudaStream_t s, const int* aidx, const int* bidx) {
   if (batch <= 0 || n <= 0 || m <= 0) return KHP_OK;
-  // 64 x 64 tiles (4 x 4 outputs per thread) once both output dimensions reach 64, else 32 x 32
+  // 64 x 64 tiles (4 x 4 outputs per thread) once both output dimensions reach 64; 32 x 128
+  // (2 x 8) for outputs of at most 32 rows and at least 128 columns (the block rows of the
+  // substitutions); else 32 x 32
   const bool big = n >= 64 && m >= 64;
-  const int BM = big ? 64 : 32, BN = big ? 64 : 32;
+  const bool wide = !big && n <= 32 && m >= 128;
+  const int BM = big ? 64 : 32, BN = big ? 64 : wide ? 128 : 32;
   for (int64_t off = 0; off < batch; off += kMaxGridY) {
     const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
     dim3 grid((m + BN - 1) / BN, (n + BM - 1) / BM, nb);
-    if (big)
+    if (wide)
+      k_gemm<T, 32, 128, 16><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
+                                                  aidx, bidx);
+    else if (big)
       k_gemm<T, 64, 64, 8><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
                                                 aidx, bidx);
     else
@@ -418,11 +541,21 @@ int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t 
     // panel width: KHP_NB columns, fewer when the (n - kb) x w panel would not fit in shared memory
     w = (int)std::min<size_t>({(size_t)KHP_NB, (size_t)(n - kb), kPanelSmem / (sizeof(cplx<T>) * (size_t)(n - kb))});
     if (w < 1) return KHP_ERR_TOO_LARGE;
-    const size_t smem = sizeof(cplx<T>) * (size_t)(n - kb) * w;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return KHP_ERR_CUDA;
-    k_panel_lu<T><<<(unsigned)batch, 256, smem, s>>>(n, kb, w, A, lda, bsA, piv, info);
+    bool reg_panel = false;
+    if constexpr (sizeof(T) == 4) {
+      if (n - kb <= 256) {
+        // FP32 panels of up to 256 rows: one row per thread, in registers
+        k_panel_lu_reg<T><<<(unsigned)batch, 256, 0, s>>>(n, kb, w, A, lda, bsA, piv, info);
+        reg_panel = true;
+      }
+    }
+    if (!reg_panel) {
+      const size_t smem = sizeof(cplx<T>) * (size_t)(n - kb) * w;
+      if (smem > 48 * 1024 &&
+          cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return KHP_ERR_CUDA;
+      k_panel_lu<T><<<(unsigned)batch, 256, smem, s>>>(n, kb, w, A, lda, bsA, piv, info);
+    }
     count_launches(1);
     // row swaps of this panel to the columns left and right of it
     const int other = n - w;
@@ -455,15 +588,11 @@ int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t 
   return cuda_status();
 }
 
-// Solve A X = B (n x m) with launch_getrf_blocked's factors: pivots, then block forward and
-// backward substitution with products for the off-diagonal blocks.
+// Block forward and backward substitution with launch_getrf_blocked's L and U (B already
+// permuted), products for the off-diagonal blocks.
 template <typename T>
-int launch_getrs_blocked(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv, cplx<T>* B,
-                         int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
-  if (batch <= 0) return KHP_OK;
-  k_laswp<T><<<swp_blocks(batch * m), 256, 0, s>>>(batch, n, 0, n, 0, m, B, ldb,
-                                                                                      bsB, piv);
-  count_launches(1);
+int getrs_blocked_tri(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb,
+                      int64_t bsB, int m, cudaStream_t s) {
   auto trsm = [&](int kb, int w, int lower) {
     for (int64_t off = 0; off < batch; off += kMaxGridY) {
       const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
@@ -495,14 +624,34 @@ int launch_getrs_blocked(int64_t batch, int n, const cplx<T>* A, int64_t lda, in
   return cuda_status();
 }
 
+// Solve A X = B (n x m) with launch_getrf_blocked's factors: pivots, then the block substitutions.
+template <typename T>
+int launch_getrs_blocked(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, const int* piv, cplx<T>* B,
+                         int64_t ldb, int64_t bsB, int m, cudaStream_t s) {
+  if (batch <= 0) return KHP_OK;
+  k_laswp<T><<<swp_blocks(batch * m), 256, 0, s>>>(batch, n, 0, n, 0, m, B, ldb, bsB, piv);
+  count_launches(1);
+  return getrs_blocked_tri<T>(batch, n, A, lda, bsA, B, ldb, bsB, m, s);
+}
+
+// A^-1 = U^-1 L^-1 P: the factors, the permutation matrix P written directly, the substitutions.
 template <typename T>
 int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Ainv, int64_t ldi,
                            int64_t bsI, int* piv, int* info, cudaStream_t s) {
-  int st = launch_identity<T>(batch, n, n, Ainv, ldi, bsI, mk(T(1)), s);
+  if (batch <= 0) return KHP_OK;
+  int st = launch_getrf_blocked<T>(batch, n, A, lda, bsA, piv, info, s);
   if (st) return st;
-  st = launch_getrf_blocked<T>(batch, n, A, lda, bsA, piv, info, s);
+  const size_t psmem = sizeof(int) * (size_t)n;
+  if (psmem > 48 * 1024) {
+    st = launch_identity<T>(batch, n, n, Ainv, ldi, bsI, mk(T(1)), s);
+    if (st) return st;
+    return launch_getrs_blocked<T>(batch, n, A, lda, bsA, piv, Ainv, ldi, bsI, n, s);
+  }
+  k_perm_matrix<T><<<(unsigned)batch, 256, psmem, s>>>(n, piv, Ainv, ldi, bsI);
+  count_launches(1);
+  st = cuda_status();
   if (st) return st;
-  return launch_getrs_blocked<T>(batch, n, A, lda, bsA, piv, Ainv, ldi, bsI, n, s);
+  return getrs_blocked_tri<T>(batch, n, A, lda, bsA, Ainv, ldi, bsI, n, s);
 }
 
 #define KHP_INSTANTIATE(T)                                                                                       \
