@@ -35,13 +35,13 @@ __global__ void __launch_bounds__(kTeamThreads) k_getrs(int n, const cplx<T>* A,
 // the matrix is large enough for it, else one reflector at a time.
 template <typename T>
 __global__ void __launch_bounds__(kTeamThreads, 3) k_gehrd(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
-                                                         cplx<T>* W, int64_t ldw, int64_t bsW, int blocked) {
+                                                         int blocked) {
   __shared__ TeamShared sh;
   extern __shared__ unsigned char dyn[];
   TeamCta t;
   const int64_t b = blockIdx.x;
   if (blocked)
-    team_gehrd_blocked(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, W + b * bsW, ldw, &sh);
+    team_gehrd_blocked(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, reinterpret_cast<cplx<T>*>(dyn), &sh);
   else
     team_gehrd(t, A + b * bsA, lda, n, Z + b * (int64_t)n * n, n, reinterpret_cast<cplx<T>*>(dyn), &sh);
 }
@@ -470,13 +470,15 @@ template <typename T>
 int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
                 int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s) {
   if (batch <= 0) return KHP_OK;
-  // blocked reduction when W can hold its scratch (ldw >= 3 NB + 2 columns) and panels pay off
-  const int blocked = (n >= 64 && ldw >= 3 * KHP_GEHRD_NB + 2) ? 1 : 0;
-  const size_t smem = blocked ? 0 : sizeof(cplx<T>) * (size_t)n;  // unblocked: Householder vector
+  // blocked reduction when panels pay off and their scratch fits in shared memory
+  const size_t scratch = sizeof(cplx<T>) * (size_t)gehrd_blocked_scratch(n);
+  const int blocked = (n >= 64 && scratch <= 200 * 1024) ? 1 : 0;
+  // blocked: the panel's reflectors, Y, T; unblocked: one Householder vector
+  const size_t smem = blocked ? scratch : sizeof(cplx<T>) * (size_t)n;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_gehrd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
-  k_gehrd<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, W, ldw, bsW, blocked);
+  k_gehrd<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, blocked);
   k_geev_schur<T><<<(unsigned)batch, kTeamThreads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
   count_launches(2);
   int st = cuda_status();

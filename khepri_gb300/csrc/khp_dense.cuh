@@ -227,39 +227,43 @@ KHP_HD void team_gemm(const Team& t, int n, int m, int k, cplx<T> alpha, const c
 //   Z[:, c0+1:] -= (Z V T) V^H.
 // Each column costs one pass over the matrix (A v_j) instead of three read-write passes over
 // the matrix and Z.  The reflectors are stored below the subdiagonal (cleared at the end).
-// Scratch (ldw-strided, n rows): Y in columns [0, NB), T in rows [0, NB) of columns [2 NB, 3 NB),
-// vectors w, u in columns 3 NB and 3 NB + 1: needs ldw >= 3 NB + 2 and n >= NB.
+// Scratch S (shared memory, gehrd_blocked_scratch(n) entries): the panel's reflectors V and Y
+// (reflector-major, n each), T (NB x NB) and the vectors w, u (NB each); needs n >= NB.
 // ------------------------------------------------------------------------------------------
 #ifndef KHP_GEHRD_NB
 #define KHP_GEHRD_NB 8
 #endif
+// Complex entries of team_gehrd_blocked's scratch for an n x n matrix.
+KHP_HD int64_t gehrd_blocked_scratch(int n) {
+  return 2 * (int64_t)KHP_GEHRD_NB * n + (int64_t)KHP_GEHRD_NB * KHP_GEHRD_NB + 2 * KHP_GEHRD_NB;
+}
+
 
 template <class Team, typename T>
-KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* W,
-                               int64_t ldw, TeamShared* sh) {
+KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* S,
+                               TeamShared* sh) {
   // panel width (the per-thread accumulators of the panel updates stay in registers)
   constexpr int NB = KHP_GEHRD_NB;
   const int lanes = t.size() < 32 ? t.size() : 32;
   const int lane = t.tid() % lanes, warp = t.tid() / lanes, nwarps = t.size() / lanes;
-  cplx<T>* Y = W;                   // Y[i][l] = W[i * ldw + l]
-  cplx<T>* Tm = W + 2 * NB;         // Tm[m][l] = W[m * ldw + 2 NB + l]
-  cplx<T>* wv = W + 3 * NB;         // wv[l] = W[l * ldw + 3 NB]
-  cplx<T>* uv = W + 3 * NB + 1;     // uv[l] = W[l * ldw + 3 NB + 1]
+  cplx<T>* Vs = S;                  // Vs[l n + i] = V(i, l)
+  cplx<T>* Ys = S + NB * n;         // Ys[l n + i] = Y[i][l]
+  cplx<T>* Tm = S + 2 * NB * n;     // Tm[m NB + l] = T[m][l]
+  cplx<T>* wv = Tm + NB * NB;       // w[l]
+  cplx<T>* uv = wv + NB;            // u[l]
   team_set_identity(t, Z, ldz, n, n);
   for (int c0 = 0; c0 + 2 < n; c0 += NB) {
     const int nb = (n - 2 - c0) < NB ? (n - 2 - c0) : NB;
-    // V(i, l) of reflector l (column c0 + l): 0 above row c0 + l + 1, 1 there, stored below
-    auto V = [&](int i, int l) -> cplx<T> {
-      const int cl = c0 + l;
-      return i <= cl ? mk(T(0)) : (i == cl + 1 ? mk(T(1)) : H[(int64_t)i * ld + cl]);
-    };
+    // V(i, l) of reflector l (column c0 + l): 0 above row c0 + l + 1, 1 there, the stored
+    // reflector below; copied to Vs[l n + i] (shared memory, reflector-major) once it is final
+    auto V = [&](int i, int l) -> cplx<T> { return Vs[(int64_t)l * n + i]; };
     for (int j = 0; j < nb; ++j) {
       const int c = c0 + j;
       if (j > 0) {
         // column c of A Q_j: b = A[:, c] - Y_j conj(V[c, 0:j]) (every row)
         for (int i = t.tid(); i < n; i += t.size()) {
           cplx<T> acc = H[(int64_t)i * ld + c];
-          for (int l = 0; l < j; ++l) acc -= mul_conj(Y[(int64_t)i * ldw + l], V(c, l));
+          for (int l = 0; l < j; ++l) acc -= mul_conj(Ys[(int64_t)l * n + i], V(c, l));
           H[(int64_t)i * ld + c] = acc;
         }
         t.sync();
@@ -268,20 +272,20 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
           cplx<T> acc = mk(T(0));
           for (int i = c0 + 1 + lane; i < n; i += lanes) acc += conj_mul(V(i, l), H[(int64_t)i * ld + c]);
           acc = warp_sum(t, acc);
-          if (lane == 0) wv[(int64_t)l * ldw] = acc;
+          if (lane == 0) wv[l] = acc;
         }
         t.sync();
         if (t.tid() == 0) {
           for (int l = j - 1; l >= 0; --l) {  // in place, highest first: (T^H w)_l = sum_{m<=l} conj(T_ml) w_m
             cplx<T> acc = mk(T(0));
-            for (int m = 0; m <= l; ++m) acc += conj_mul(Tm[(int64_t)m * ldw + l], wv[(int64_t)m * ldw]);
-            wv[(int64_t)l * ldw] = acc;
+            for (int m = 0; m <= l; ++m) acc += conj_mul(Tm[m * NB + l], wv[m]);
+            wv[l] = acc;
           }
         }
         t.sync();
         for (int i = c0 + 1 + t.tid(); i < n; i += t.size()) {
           cplx<T> acc = H[(int64_t)i * ld + c];
-          for (int l = 0; l < j; ++l) acc -= V(i, l) * wv[(int64_t)l * ldw];
+          for (int l = 0; l < j; ++l) acc -= V(i, l) * wv[l];
           H[(int64_t)i * ld + c] = acc;
         }
         t.sync();
@@ -301,33 +305,36 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
         if (t.tid() == 0) H[(int64_t)(c + 1) * ld + c] = mk(beta);
       }
       t.sync();
+      for (int i = t.tid(); i < n; i += t.size())
+        Vs[(int64_t)j * n + i] = i <= c ? mk(T(0)) : (i == c + 1 ? mk(T(1)) : H[(int64_t)i * ld + c]);
+      t.sync();
       // Y[:, j] = tau (A v - Y_j u), u = V_j^H v;  v = V(., j), A = columns c+1.. of H
       for (int i = t.tid(); i < n; i += t.size()) {
         const cplx<T>* row = H + (int64_t)i * ld;
         cplx<T> acc = row[c + 1];
-        for (int col = c + 2; col < n; ++col) fma_acc(acc, row[col], H[(int64_t)col * ld + c]);
-        Y[(int64_t)i * ldw + j] = acc;
+        for (int col = c + 2; col < n; ++col) fma_acc(acc, row[col], Vs[(int64_t)j * n + col]);
+        Ys[(int64_t)j * n + i] = acc;
       }
       for (int l = warp; l < j; l += nwarps) {
         cplx<T> acc = mk(T(0));
         for (int i = c + 1 + lane; i < n; i += lanes) acc += conj_mul(V(i, l), V(i, j));
         acc = warp_sum(t, acc);
-        if (lane == 0) uv[(int64_t)l * ldw] = acc;
+        if (lane == 0) uv[l] = acc;
       }
       t.sync();
       for (int i = t.tid(); i < n; i += t.size()) {
-        cplx<T> acc = Y[(int64_t)i * ldw + j];
-        for (int l = 0; l < j; ++l) acc -= Y[(int64_t)i * ldw + l] * uv[(int64_t)l * ldw];
-        Y[(int64_t)i * ldw + j] = tau * acc;
+        cplx<T> acc = Ys[(int64_t)j * n + i];
+        for (int l = 0; l < j; ++l) acc -= Ys[(int64_t)l * n + i] * uv[l];
+        Ys[(int64_t)j * n + i] = tau * acc;
       }
       if (t.tid() == 0) {  // T[0:j, j] = -tau T_j u ; T[j][j] = tau
         for (int m = 0; m < j; ++m) {
           cplx<T> acc = mk(T(0));
-          for (int l = m; l < j; ++l) fma_acc(acc, Tm[(int64_t)m * ldw + l], uv[(int64_t)l * ldw]);
-          Tm[(int64_t)m * ldw + j] = -(tau * acc);
+          for (int l = m; l < j; ++l) fma_acc(acc, Tm[m * NB + l], uv[l]);
+          Tm[m * NB + j] = -(tau * acc);
         }
-        Tm[(int64_t)j * ldw + j] = tau;
-        for (int m = j + 1; m < NB; ++m) Tm[(int64_t)m * ldw + j] = mk(T(0));
+        Tm[j * NB + j] = tau;
+        for (int m = j + 1; m < NB; ++m) Tm[m * NB + j] = mk(T(0));
       }
       t.sync();
     }
@@ -338,7 +345,7 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
       for (int e = t.tid(); e < n * m; e += t.size()) {
         const int i = e / m, J = J0 + e % m;
         cplx<T> acc = H[(int64_t)i * ld + J];
-        for (int l = 0; l < nb; ++l) acc -= mul_conj(Y[(int64_t)i * ldw + l], V(J, l));
+        for (int l = 0; l < nb; ++l) acc -= mul_conj(Ys[(int64_t)l * n + i], V(J, l));
         H[(int64_t)i * ld + J] = acc;
       }
       t.sync();
@@ -359,7 +366,7 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
           cplx<T> acc = mk(T(0));
 #pragma unroll
           for (int q = 0; q < NB; ++q)
-            if (q <= l) acc += conj_mul(Tm[(int64_t)q * ldw + l], x[q]);
+            if (q <= l) acc += conj_mul(Tm[q * NB + l], x[q]);
           x[l] = acc;
         }
         for (int i = c0 + 1; i < n; ++i) {
@@ -389,7 +396,7 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
         cplx<T> acc = mk(T(0));
 #pragma unroll
         for (int q = 0; q < NB; ++q)
-          if (q <= l) fma_acc(acc, x[q], Tm[(int64_t)q * ldw + l]);
+          if (q <= l) fma_acc(acc, x[q], Tm[q * NB + l]);
         x[l] = acc;
       }
       for (int col = c0 + 1; col < n; ++col) {
