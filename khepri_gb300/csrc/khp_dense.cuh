@@ -341,12 +341,30 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
     const int J0 = c0 + nb;
     // right: A[:, J] -= Y V[J, :]^H for the columns after the panel
     if (J0 < n) {
-      const int m = n - J0;
-      for (int e = t.tid(); e < n * m; e += t.size()) {
-        const int i = e / m, J = J0 + e % m;
-        cplx<T> acc = H[(int64_t)i * ld + J];
-        for (int l = 0; l < nb; ++l) acc -= mul_conj(Ys[(int64_t)l * n + i], V(J, l));
-        H[(int64_t)i * ld + J] = acc;
+      // a warp per row (Y's row broadcast), lanes along the row; the loads of PF elements are
+      // issued before their stores (the stores would otherwise order every later load)
+      constexpr int PF = 4;
+      for (int i = warp; i < n; i += nwarps) {
+        cplx<T> y[NB];
+#pragma unroll
+        for (int l = 0; l < NB; ++l) y[l] = l < nb ? Ys[(int64_t)l * n + i] : mk(T(0));
+        cplx<T>* hr = H + (int64_t)i * ld;
+        for (int J = J0 + lane; J < n; J += PF * lanes) {
+          cplx<T> a[PF];
+#pragma unroll
+          for (int u = 0; u < PF; ++u) a[u] = J + u * lanes < n ? hr[J + u * lanes] : mk(T(0));
+#pragma unroll
+          for (int u = 0; u < PF; ++u) {
+            const int Ju = J + u * lanes;
+            if (Ju < n) {
+              cplx<T> acc = a[u];
+#pragma unroll
+              for (int l = 0; l < NB; ++l)
+                if (l < nb) acc -= mul_conj(y[l], V(Ju, l));
+              hr[Ju] = acc;
+            }
+          }
+        }
       }
       t.sync();
       // left: A[c0+1:, J] -= V T^H (V^H A[c0+1:, J]), thread per column
@@ -369,12 +387,20 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
             if (q <= l) acc += conj_mul(Tm[q * NB + l], x[q]);
           x[l] = acc;
         }
-        for (int i = c0 + 1; i < n; ++i) {
-          cplx<T> acc = H[(int64_t)i * ld + J];
+        for (int i0 = c0 + 1; i0 < n; i0 += PF) {
+          cplx<T> a[PF];
 #pragma unroll
-          for (int l = 0; l < NB; ++l)
-            if (l < nb) acc -= V(i, l) * x[l];
-          H[(int64_t)i * ld + J] = acc;
+          for (int u = 0; u < PF; ++u) a[u] = i0 + u < n ? H[(int64_t)(i0 + u) * ld + J] : mk(T(0));
+#pragma unroll
+          for (int u = 0; u < PF; ++u) {
+            if (i0 + u < n) {
+              cplx<T> acc = a[u];
+#pragma unroll
+              for (int l = 0; l < NB; ++l)
+                if (l < nb) acc -= V(i0 + u, l) * x[l];
+              H[(int64_t)(i0 + u) * ld + J] = acc;
+            }
+          }
         }
       }
     }
@@ -399,12 +425,20 @@ KHP_HD void team_gehrd_blocked(const Team& t, cplx<T>* H, int64_t ld, int n, cpl
           if (q <= l) fma_acc(acc, x[q], Tm[q * NB + l]);
         x[l] = acc;
       }
-      for (int col = c0 + 1; col < n; ++col) {
-        cplx<T> acc = zr[col];
+      for (int col0 = c0 + 1; col0 < n; col0 += 4) {
+        cplx<T> a[4];
 #pragma unroll
-        for (int l = 0; l < NB; ++l)
-          if (l < nb) acc -= mul_conj(x[l], V(col, l));
-        zr[col] = acc;
+        for (int u = 0; u < 4; ++u) a[u] = col0 + u < n ? zr[col0 + u] : mk(T(0));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (col0 + u < n) {
+            cplx<T> acc = a[u];
+#pragma unroll
+            for (int l = 0; l < NB; ++l)
+              if (l < nb) acc -= mul_conj(x[l], V(col0 + u, l));
+            zr[col0 + u] = acc;
+          }
+        }
       }
     }
     t.sync();
