@@ -87,6 +87,8 @@ __global__ void __launch_bounds__(256) k_gemm(int n, int m, int k, cplx<T> alpha
                                               int64_t boff, const int* __restrict__ aidx,
                                               const int* __restrict__ bidx) {
   constexpr int TM = BM / 16, TN = BN / 16;
+  constexpr int LA = BM * BK / 256, LB = BK * BN / 256;  // tile elements loaded per thread
+  static_assert(LA * 256 == BM * BK && LB * 256 == BK * BN, "tile loads must split evenly over 256 threads");
   __shared__ cplx<T> As[BK][BM];
   __shared__ cplx<T> Bs[BK][BN];
   const int64_t b = blockIdx.z + boff;
@@ -100,18 +102,43 @@ __global__ void __launch_bounds__(256) k_gemm(int n, int m, int k, cplx<T> alpha
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = mk(T(0));
-  for (int k0 = 0; k0 < k; k0 += BK) {
-    for (int e = threadIdx.x; e < BM * BK; e += 256) {
-      const int r = e / BK, c = e % BK;
+  // the next K-slice is loaded into registers while the current one is multiplied
+  cplx<T> ra[LA], rb[LB];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + 256 * q, r = e / BK, c = e % BK;
       const int gr = row0 + r, gc = k0 + c;
-      As[c][r] = (gr < n && gc < k) ? A[(int64_t)gr * lda + gc] : mk(T(0));
+      ra[q] = (gr < n && gc < k) ? A[(int64_t)gr * lda + gc] : mk(T(0));
     }
-    for (int e = threadIdx.x; e < BK * BN; e += 256) {
-      const int r = e / BN, c = e % BN;
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + 256 * q, r = e / BN, c = e % BN;
       const int gr = k0 + r, gc = col0 + c;
-      Bs[r][c] = (gr < k && gc < m) ? B[(int64_t)gr * ldb + gc] : mk(T(0));
+      rb[q] = (gr < k && gc < m) ? B[(int64_t)gr * ldb + gc] : mk(T(0));
     }
+  };
+  auto stage = [&]() {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      As[e % BK][e / BK] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      Bs[e / BN][e % BN] = rb[q];
+    }
+  };
+  // FP32: prefetch (the products are latency-bound); FP64: load and stage in turn (the FP64 pipe
+  // bounds them, and the prefetch registers would cost occupancy)
+  constexpr bool kPrefetch = sizeof(T) == 4;
+  if (kPrefetch && k > 0) load(0);
+  for (int k0 = 0; k0 < k; k0 += BK) {
+    if (!kPrefetch) load(k0);
+    stage();
     __syncthreads();
+    if (kPrefetch && k0 + BK < k) load(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       cplx<T> a[TM], bb[TN];
@@ -411,6 +438,127 @@ __global__ void k_trsm_block(int w, int d0, const cplx<T>* __restrict__ A, int64
     if (i < w) Bb[(int64_t)i * ldb] = x[i];
 }
 
+// One block row of the substitutions, product and triangular solve fused:
+//   B[r0:r0+w, tile] <- Tkk^-1 (B[r0:r0+w, tile] - A[r0:r0+w, k0:k0+K] B[k0:k0+K, tile])
+// with Tkk = A[r0:r0+w, r0:r0+w] unit lower (lower) or upper with its diagonal.  A CTA per 128
+// columns of one problem: the 32 x 128 product tile in registers (2 x 8 per thread), then staged in
+// shared memory and solved a thread per column.  Dynamic shared memory: kBlockSolveSmem bytes.
+constexpr int kBsBM = 32, kBsBN = 128, kBsBK = 16;
+template <typename T>
+constexpr size_t block_solve_smem() {
+  return sizeof(cplx<T>) * ((size_t)kBsBK * kBsBM + (size_t)kBsBK * kBsBN + (size_t)kBsBM * kBsBN +
+                            (size_t)KHP_NB * KHP_NB + KHP_NB);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_solve(int w, int r0, int k0, int K, int m, const cplx<T>* __restrict__ A,
+                                                     int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb, int64_t bsB,
+                                                     int lower) {
+  constexpr int TM = kBsBM / 16, TN = kBsBN / 16;
+  extern __shared__ unsigned char dyn_bs[];
+  cplx<T>* As = reinterpret_cast<cplx<T>*>(dyn_bs);  // [BK][BM]
+  cplx<T>* Bs = As + kBsBK * kBsBM;                    // [BK][BN]
+  cplx<T>* Cs = Bs + kBsBK * kBsBN;                    // [BM][BN]
+  cplx<T>* Tb = Cs + kBsBM * kBsBN;                    // [w][w]
+  cplx<T>* dinv = Tb + KHP_NB * KHP_NB;                // [w]
+  const int64_t b = blockIdx.y;
+  const cplx<T>* Ab = A + b * bsA;
+  cplx<T>* Bb = B + b * bsB;
+  const int col0 = blockIdx.x * kBsBN;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  cplx<T> acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = mk(T(0));
+  constexpr int LA = kBsBM * kBsBK / 256, LB = kBsBK * kBsBN / 256;
+  cplx<T> ra[LA], rb[LB];  // the next K-slice, loaded while the current one is multiplied
+  auto load = [&](int kk0) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + 256 * q, r = e / kBsBK, c = e % kBsBK;
+      ra[q] = (r < w && kk0 + c < K) ? Ab[(int64_t)(r0 + r) * lda + k0 + kk0 + c] : mk(T(0));
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + 256 * q, r = e / kBsBN, c = e % kBsBN;
+      rb[q] = (kk0 + r < K && col0 + c < m) ? Bb[(int64_t)(k0 + kk0 + r) * ldb + col0 + c] : mk(T(0));
+    }
+  };
+  constexpr bool kPrefetch = sizeof(T) == 4;  // as in k_gemm
+  if (kPrefetch && K > 0) load(0);
+  for (int kk0 = 0; kk0 < K; kk0 += kBsBK) {
+    if (!kPrefetch) load(kk0);
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      As[(e % kBsBK) * kBsBM + e / kBsBK] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      Bs[(e / kBsBN) * kBsBN + e % kBsBN] = rb[q];
+    }
+    __syncthreads();
+    if (kPrefetch && kk0 + kBsBK < K) load(kk0 + kBsBK);
+#pragma unroll
+    for (int kk = 0; kk < kBsBK; ++kk) {
+      cplx<T> a[TM], bb[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk * kBsBM + ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) bb[j] = Bs[kk * kBsBN + tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) fma_acc(acc[i][j], a[i], bb[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int r = ty + 16 * i;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int c = tx + 16 * j;
+      Cs[r * kBsBN + c] = (r < w && col0 + c < m) ? Bb[(int64_t)(r0 + r) * ldb + col0 + c] - acc[i][j] : mk(T(0));
+    }
+  }
+  for (int e = threadIdx.x; e < w * w; e += 256) Tb[e] = Ab[(int64_t)(r0 + e / w) * lda + r0 + e % w];
+  __syncthreads();
+  if (!lower && threadIdx.x < w) dinv[threadIdx.x] = cdiv(mk(T(1)), Tb[threadIdx.x * w + threadIdx.x]);
+  __syncthreads();
+  const int j = threadIdx.x;
+  if (j >= kBsBN || col0 + j >= m) return;
+  cplx<T> x[KHP_NB];
+#pragma unroll
+  for (int i = 0; i < KHP_NB; ++i) x[i] = i < w ? Cs[i * kBsBN + j] : mk(T(0));
+  if (lower) {
+#pragma unroll
+    for (int i = 1; i < KHP_NB; ++i) {
+      if (i >= w) break;
+      cplx<T> a = x[i];
+#pragma unroll
+      for (int k = 0; k < KHP_NB; ++k)
+        if (k < i) fms_acc(a, Tb[i * w + k], x[k]);
+      x[i] = a;
+    }
+  } else {
+#pragma unroll
+    for (int ii = KHP_NB - 1; ii >= 0; --ii) {
+      if (ii >= w) continue;
+      cplx<T> a = x[ii];
+#pragma unroll
+      for (int k = 0; k < KHP_NB; ++k)
+        if (k > ii && k < w) fms_acc(a, Tb[ii * w + k], x[k]);
+      x[ii] = a * dinv[ii];
+    }
+  }
+  cplx<T>* out = Bb + (int64_t)r0 * ldb + col0 + j;
+#pragma unroll
+  for (int i = 0; i < KHP_NB; ++i)
+    if (i < w) out[(int64_t)i * ldb] = x[i];
+}
+
 // Grid for a thread-per-column row interchange: one thread per column up to 8 CTAs per SM.
 inline unsigned swp_blocks(int64_t columns) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((columns + 255) / 256, 152 * 8)); }
 
@@ -591,37 +739,60 @@ int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t 
 }
 
 // Block forward and backward substitution with launch_getrf_blocked's L and U (B already
-// permuted), products for the off-diagonal blocks.
+// permuted): for 128 or more right-hand sides each block row is one fused product + solve
+// (k_block_solve), for fewer a tiled product sized to m followed by the block solve.
 template <typename T>
 int getrs_blocked_tri(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb,
                       int64_t bsB, int m, cudaStream_t s) {
-  auto trsm = [&](int kb, int w, int lower) {
+  if (m < kBsBN) {
+    // few right-hand sides: tiled product sized to m, then the block solve
+    auto trsm = [&](int kb, int w, int lower) {
+      for (int64_t off = 0; off < batch; off += kMaxGridY) {
+        const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
+        k_trsm_block<T><<<dim3((m + 127) / 128, nb), 128, 0, s>>>(w, kb, A + off * bsA, lda, bsA, kb, m,
+                                                                 B + off * bsB, ldb, bsB, lower, nb);
+        count_launches(1);
+      }
+    };
+    for (int kb = 0; kb < n; kb += KHP_NB) {
+      const int w = std::min(KHP_NB, n - kb);
+      if (kb > 0) {
+        const int st = launch_gemm<T>(batch, w, m, kb, mk(T(-1)), A + (int64_t)kb * lda, lda, bsA, B, ldb, bsB,
+                                      mk(T(1)), B + (int64_t)kb * ldb, ldb, bsB, s);
+        if (st) return st;
+      }
+      trsm(kb, w, 1);
+    }
+    const int last = ((n - 1) / KHP_NB) * KHP_NB;
+    for (int kb = last; kb >= 0; kb -= KHP_NB) {
+      const int w = std::min(KHP_NB, n - kb);
+      const int rest = n - kb - w;
+      if (rest > 0) {
+        const int st = launch_gemm<T>(batch, w, m, rest, mk(T(-1)), A + (int64_t)kb * lda + kb + w, lda, bsA,
+                                      B + (int64_t)(kb + w) * ldb, ldb, bsB, mk(T(1)), B + (int64_t)kb * ldb, ldb,
+                                      bsB, s);
+        if (st) return st;
+      }
+      trsm(kb, w, 0);
+    }
+    return cuda_status();
+  }
+  constexpr size_t smem = block_solve_smem<T>();
+  if (cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return KHP_ERR_CUDA;
+  auto block = [&](int kb, int w, int k0, int K, int lower) {
     for (int64_t off = 0; off < batch; off += kMaxGridY) {
       const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
-      k_trsm_block<T><<<dim3((m + 127) / 128, nb), 128, 0, s>>>(w, kb, A + off * bsA, lda, bsA, kb, m,
-                                                               B + off * bsB, ldb, bsB, lower, nb);
+      k_block_solve<T><<<dim3((m + kBsBN - 1) / kBsBN, nb), 256, smem, s>>>(w, kb, k0, K, m, A + off * bsA, lda, bsA,
+                                                                           B + off * bsB, ldb, bsB, lower);
       count_launches(1);
     }
   };
-  for (int kb = 0; kb < n; kb += KHP_NB) {
-    const int w = std::min(KHP_NB, n - kb);
-    if (kb > 0) {
-      const int st = launch_gemm<T>(batch, w, m, kb, mk(T(-1)), A + (int64_t)kb * lda, lda, bsA, B, ldb, bsB, mk(T(1)),
-                                    B + (int64_t)kb * ldb, ldb, bsB, s);
-      if (st) return st;
-    }
-    trsm(kb, w, 1);
-  }
+  for (int kb = 0; kb < n; kb += KHP_NB) block(kb, std::min(KHP_NB, n - kb), 0, kb, 1);  // L Y = B
   const int last = ((n - 1) / KHP_NB) * KHP_NB;
-  for (int kb = last; kb >= 0; kb -= KHP_NB) {
+  for (int kb = last; kb >= 0; kb -= KHP_NB) {  // U X = Y
     const int w = std::min(KHP_NB, n - kb);
-    const int rest = n - kb - w;
-    if (rest > 0) {
-      const int st = launch_gemm<T>(batch, w, m, rest, mk(T(-1)), A + (int64_t)kb * lda + kb + w, lda, bsA,
-                                    B + (int64_t)(kb + w) * ldb, ldb, bsB, mk(T(1)), B + (int64_t)kb * ldb, ldb, bsB, s);
-      if (st) return st;
-    }
-    trsm(kb, w, 0);
+    block(kb, w, kb + w, n - kb - w, 0);
   }
   return cuda_status();
 }
