@@ -287,10 +287,22 @@ __device__ __forceinline__ cd xprop(const cd* lam64, int i, double dk) { return 
 __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* gx, const double* gy,
                                                         const double* kp, const double* k0v, const cd* __restrict__ X,
                                                         const cd* __restrict__ XA, const cd* __restrict__ RT,
-                                                        cd* RES, cd* scratch, const int* active) {
+                                                        cd* RES, cd* scratch, const int* active, int x_zero) {
   TeamCta t;
   const int64_t b = blockIdx.x;
   if (active && !active[b]) return;
+  if (x_zero) {
+    // every unknown is zero (the first round): only the incidence source terms remain, and the
+    // FP64 products of the layers would multiply zeros
+    const int nh = tb.nh, n = 2 * nh, L = tb.L;
+    const M2* S = tb.inc + b * nh * 4;
+    cd* res = RES + b * (int64_t)(L + 2) * 4 * 2 * n;
+    for (int64_t e = t.tid(); e < (int64_t)(L + 2) * 4 * 2 * n; e += t.size()) {
+      const int i = (int)(e % (2 * n)) / 2, c = (int)(e % 2);
+      res[e] = e < 2 * n ? src_col(S, 0, nh, i, c) : e < 4 * n ? src_col(S, 2, nh, i, c) : mk(0.0);
+    }
+    return;
+  }
   const int nh = tb.nh, n = 2 * nh, L = tb.L;
   const int64_t nn = (int64_t)n * n;
   const int64_t xs = (int64_t)(2 * (L + 1)) * 2 * n, xas = (int64_t)2 * L * 2 * n;
@@ -1184,7 +1196,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   const int total = refine >= 1 ? refine + kExtraRounds : 0;
   for (int it = 0; it <= total; ++it) {
     const int* act = it > refine ? p.active : nullptr;
-    k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr, act);
+    k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr, act,
+                                                      it == 0 ? 1 : 0);
     count_launches(1);
     MX_TRY(cuda_status());
     k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW,
