@@ -65,9 +65,9 @@ TC_PAIRS = 36
 TC_FLOPS_PER_MATRIX = TC_PAIRS * 2 * (2 * _up128(N_MAT) * _up64(2 * N_MAT) * _up64(2 * N_MAT)
                                       + 2 * _up128(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
 BF16_PEAK = 1935.4  # TFLOP/s, MEASURED_PEAKS.json bf16_tflops (burst)
-# DRAM bytes per matrix of the FP32 eigensolver (read + write) at 456 matrices per launch, from
-# one ncu capture (profiles/geev_fp32_n242_batch456_traffic.md): 364.1 GB / 456
-GEEV_TRAFFIC_PER_MATRIX = (197903963392 + 166228993536) / 456
+# DRAM bytes per matrix of the FP32 eigensolver (read + write of k_gehrd and k_geev_schur) at
+# 456 matrices per launch, from one ncu capture (profiles/geev_fp32_n242_batch456_traffic.md)
+GEEV_TRAFFIC_PER_MATRIX = (23328427776 + 9063487744 + 90695730432 + 99780031744) / 456
 
 
 def solve_mixed_flops(n, nmaps, npattern, nhomog):
