@@ -442,7 +442,8 @@ __global__ void k_trsm_block(int w, int d0, const cplx<T>* __restrict__ A, int64
 //   B[r0:r0+w, tile] <- Tkk^-1 (B[r0:r0+w, tile] - A[r0:r0+w, k0:k0+K] B[k0:k0+K, tile])
 // with Tkk = A[r0:r0+w, r0:r0+w] unit lower (lower) or upper with its diagonal.  A CTA per 128
 // columns of one problem: the 32 x 128 product tile in registers (2 x 8 per thread), then staged in
-// shared memory and solved a thread per column.  Dynamic shared memory: kBlockSolveSmem bytes.
+// shared memory and solved a thread per column in place.  Dynamic shared memory:
+// block_solve_smem<T>() bytes.
 constexpr int kBsBM = 32, kBsBN = 128, kBsBK = 16;
 template <typename T>
 constexpr size_t block_solve_smem() {
@@ -450,7 +451,7 @@ constexpr size_t block_solve_smem() {
                             (size_t)KHP_NB * KHP_NB + KHP_NB);
 }
 template <typename T>
-__global__ void __launch_bounds__(256) k_block_solve(int w, int r0, int k0, int K, int m, const cplx<T>* __restrict__ A,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_block_solve(int w, int r0, int k0, int K, int m, const cplx<T>* __restrict__ A,
                                                      int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb, int64_t bsB,
                                                      int lower) {
   constexpr int TM = kBsBM / 16, TN = kBsBN / 16;
@@ -527,36 +528,25 @@ __global__ void __launch_bounds__(256) k_block_solve(int w, int r0, int k0, int 
   __syncthreads();
   if (!lower && threadIdx.x < w) dinv[threadIdx.x] = cdiv(mk(T(1)), Tb[threadIdx.x * w + threadIdx.x]);
   __syncthreads();
+  // a thread per column solves in place in the shared tile (its own column only, no barriers)
   const int j = threadIdx.x;
   if (j >= kBsBN || col0 + j >= m) return;
-  cplx<T> x[KHP_NB];
-#pragma unroll
-  for (int i = 0; i < KHP_NB; ++i) x[i] = i < w ? Cs[i * kBsBN + j] : mk(T(0));
+  cplx<T>* xc = Cs + j;  // xc[i * kBsBN] = row i of this column
   if (lower) {
-#pragma unroll
-    for (int i = 1; i < KHP_NB; ++i) {
-      if (i >= w) break;
-      cplx<T> a = x[i];
-#pragma unroll
-      for (int k = 0; k < KHP_NB; ++k)
-        if (k < i) fms_acc(a, Tb[i * w + k], x[k]);
-      x[i] = a;
+    for (int i = 1; i < w; ++i) {
+      cplx<T> a = xc[i * kBsBN];
+      for (int k = 0; k < i; ++k) fms_acc(a, Tb[i * w + k], xc[k * kBsBN]);
+      xc[i * kBsBN] = a;
     }
   } else {
-#pragma unroll
-    for (int ii = KHP_NB - 1; ii >= 0; --ii) {
-      if (ii >= w) continue;
-      cplx<T> a = x[ii];
-#pragma unroll
-      for (int k = 0; k < KHP_NB; ++k)
-        if (k > ii && k < w) fms_acc(a, Tb[ii * w + k], x[k]);
-      x[ii] = a * dinv[ii];
+    for (int ii = w - 1; ii >= 0; --ii) {
+      cplx<T> a = xc[ii * kBsBN];
+      for (int k = ii + 1; k < w; ++k) fms_acc(a, Tb[ii * w + k], xc[k * kBsBN]);
+      xc[ii * kBsBN] = a * dinv[ii];
     }
   }
   cplx<T>* out = Bb + (int64_t)r0 * ldb + col0 + j;
-#pragma unroll
-  for (int i = 0; i < KHP_NB; ++i)
-    if (i < w) out[(int64_t)i * ldb] = x[i];
+  for (int i = 0; i < w; ++i) out[(int64_t)i * ldb] = xc[i * kBsBN];
 }
 
 // Grid for a thread-per-column row interchange: one thread per column up to 8 CTAs per SM.
