@@ -397,15 +397,31 @@ int khp_stage_timing_read(int32_t stage, double* ms, int64_t* marks);
  * FP64-accurate batched complex product on the bf16 tensor cores (no counterpart in the
  * reference; the mixed-precision solve forms its FP64 eigen-residuals and V = Q W this way).
  * C[b] = A[b] B[b]; A: complex [batch] m x k (row stride lda, batch stride bsA, in complex
- * elements), B: k x n, C: m x n.  Each operand is split exactly into seven 8-bit digits per row
- * (A) or column (B) and the 28 leading digit products are summed exactly in FP32/int32; the
- * error per element is ~2^-55 * 2k * max|A row| * max|B column|, an FP64 product's own bound.
- * k <= 4096.  Scratch: khp_zgemm_fp64_tc_workspace(batch, m, n, k) bytes.
+ * elements), B: k x n, C: m x n.  Each operand is split exactly into signed digits per row (A)
+ * or column (B): for k <= 288, eight 7-bit digits whose 36 leading products are accumulated per
+ * level in tensor memory (tcgen05); above, seven 8-bit digits and 28 products on mma.sync with
+ * FP32/int32 level sums.  The error per element is ~2^-55 * 2k * max|A row| * max|B column|, an
+ * FP64 product's own bound.  k <= 4096.  Scratch: khp_zgemm_fp64_tc_workspace(batch, m, n, k)
+ * bytes.
  */
 size_t khp_zgemm_fp64_tc_workspace(int64_t batch, int32_t m, int32_t n, int32_t k);
 int khp_zgemm_fp64_tc(int64_t batch, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda, int64_t bsA,
                       const double* B, int64_t ldb, int64_t bsB, double* C, int64_t ldc, int64_t bsC, void* workspace,
                       size_t ws_bytes, void* stream);
+
+/*
+ * Batched explicit inverse of complex n x n matrices, the reference's numpy.linalg.inv / solve
+ * building block (khepri/alternative.py:24-27, 50-55, 164-165, 182-193; khepri/layer.py:158;
+ * khepri/crystal.py:372): blocked LU with partial pivoting, then A^-1 = U^-1 L^-1 P.
+ * precision: 0 = FP64 (A, Ainv complex128), 1 = FP32 (complex64).  A [batch] n x n row-major,
+ * batch stride a_stride (complex elements), is overwritten by the LU factors; Ainv [batch] n x n,
+ * batch stride inv_stride.  status: int32 [batch], OR-ed: SINGULAR (an exactly zero pivot
+ * column) or NONFINITE (non-finite values in a pivot column); the inverse is then not meaningful.
+ * Scratch: khp_inverse_workspace(batch, n) bytes.
+ */
+size_t khp_inverse_workspace(int64_t batch, int32_t n);
+int khp_inverse(int64_t batch, int32_t n, int32_t precision, void* A, int64_t a_stride, void* Ainv,
+                int64_t inv_stride, int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 #ifdef __cplusplus
 }

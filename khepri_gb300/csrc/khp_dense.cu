@@ -2,6 +2,7 @@
 // (team algorithms of khp_dense.cuh), a tiled kernel for the products, element-wise helpers.
 #include <algorithm>
 
+#include "khepri_gb300.h"
 #include "khp_dense.cuh"
 #include "khp_launch.h"
 
@@ -392,6 +393,55 @@ __global__ void k_laswp(int64_t batch, int n, int k0, int k1, int c0, int c1, cp
   }
 }
 
+// The row interchanges piv[kb:kb+w] of one panel applied to every column outside the panel
+// [kb, kb+w).  The w sequential swaps are first resolved in shared memory into a permutation of
+// the (at most 2w) rows they touch; then each thread (a column) loads all of the moved rows
+// before it stores any, instead of one dependent round trip per swap.  CTA per (column chunk,
+// problem), kSwpThreads threads; dynamic shared memory laswp_panel_smem<T>(n).
+constexpr int kSwpThreads = 64;
+template <typename T>
+size_t laswp_panel_smem(int n) {
+  // stage [2 NB][threads] complex, then content [n], touched [n], rows [2 NB] and the count
+  return sizeof(cplx<T>) * 2 * KHP_NB * kSwpThreads + sizeof(int) * (2 * (size_t)n + 2 * KHP_NB + 1);
+}
+template <typename T>
+__global__ void __launch_bounds__(kSwpThreads) k_laswp_panel(int n, int kb, int w, cplx<T>* A, int64_t lda,
+                                                             int64_t bsA, const int* __restrict__ piv) {
+  extern __shared__ unsigned char dyn_sw[];
+  cplx<T>* stage = reinterpret_cast<cplx<T>*>(dyn_sw);         // [2 KHP_NB][kSwpThreads]
+  int* content = reinterpret_cast<int*>(stage + 2 * KHP_NB * kSwpThreads);  // [n]: source row now at r
+  int* touched = content + n;                                   // [n]: row already listed
+  int* rows = touched + n;                                      // [<= 2 w]: the moved rows
+  int* cnt = rows + 2 * KHP_NB;
+  const int64_t b = blockIdx.y;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    content[r] = r;
+    touched[r] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = kb; k < kb + w; ++k) {
+      const int p = piv[b * n + k];
+      if (p == k) continue;
+      const int t = content[k];
+      content[k] = content[p];
+      content[p] = t;
+      if (!touched[k]) { touched[k] = 1; rows[c++] = k; }
+      if (!touched[p]) { touched[p] = 1; rows[c++] = p; }
+    }
+    *cnt = c;
+  }
+  __syncthreads();
+  const int nr = *cnt;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;  // q-th column outside the panel
+  if (nr == 0 || q >= n - w) return;
+  const int col = q < kb ? q : q + w;
+  cplx<T>* Ab = A + b * bsA + col;
+  for (int i = 0; i < nr; ++i) stage[i * kSwpThreads + threadIdx.x] = Ab[(int64_t)content[rows[i]] * lda];
+  for (int i = 0; i < nr; ++i) Ab[(int64_t)rows[i] * lda] = stage[i * kSwpThreads + threadIdx.x];
+}
+
 // B[r0:r0+w, 0:m] <- T^-1 B[r0:r0+w, 0:m] with T = the diagonal block A[d0:d0+w, d0:d0+w]
 // (unit lower when lower, else upper with its diagonal).  Thread per column of B; T in smem.
 template <typename T>
@@ -700,14 +750,24 @@ int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t 
     // row swaps of this panel to the columns left and right of it
     const int other = n - w;
     if (other > 0) {
-      if (kb > 0) {
-        k_laswp<T><<<swp_blocks(batch * kb), 256, 0, s>>>(batch, n, kb, kb + w, 0, kb,
-                                                                                             A, lda, bsA, piv);
-        count_launches(1);
-      }
-      if (kb + w < n) {
-        k_laswp<T><<<swp_blocks(batch * (n - kb - w)), 256, 0, s>>>(batch, n, kb, kb + w, kb + w, n, A, lda, bsA, piv);
-        count_launches(1);
+      const size_t ssm = laswp_panel_smem<T>(n);
+      if (ssm <= 48 * 1024) {
+        for (int64_t off = 0; off < batch; off += kMaxGridY) {
+          const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
+          k_laswp_panel<T><<<dim3((other + kSwpThreads - 1) / kSwpThreads, nb), kSwpThreads, ssm, s>>>(
+              n, kb, w, A + off * bsA, lda, bsA, piv + off * n);
+          count_launches(1);
+        }
+      } else {
+        if (kb > 0) {
+          k_laswp<T><<<swp_blocks(batch * kb), 256, 0, s>>>(batch, n, kb, kb + w, 0, kb, A, lda, bsA, piv);
+          count_launches(1);
+        }
+        if (kb + w < n) {
+          k_laswp<T><<<swp_blocks(batch * (n - kb - w)), 256, 0, s>>>(batch, n, kb, kb + w, kb + w, n, A, lda,
+                                                                      bsA, piv);
+          count_launches(1);
+        }
       }
     }
     const int rest = n - kb - w;
@@ -843,3 +903,29 @@ KHP_INSTANTIATE(double)
 KHP_INSTANTIATE(float)
 
 }  // namespace khp
+
+extern "C" {
+
+size_t khp_inverse_workspace(int64_t batch, int32_t n) {
+  if (batch < 0 || n < 1) return 0;
+  return sizeof(int) * (size_t)batch * n;  // pivots
+}
+
+int khp_inverse(int64_t batch, int32_t n, int32_t precision, void* A, int64_t a_stride, void* Ainv,
+                int64_t inv_stride, int32_t* status, void* workspace, size_t ws_bytes, void* stream) {
+  using namespace khp;
+  if (batch < 0 || n < 1 || (precision != 0 && precision != 1) || !A || !Ainv || !status ||
+      a_stride < (int64_t)n * n || inv_stride < (int64_t)n * n)
+    return KHP_ERR_INVALID_ARG;
+  if (batch == 0) return KHP_OK;
+  if (!workspace || ws_bytes < khp_inverse_workspace(batch, n)) return KHP_ERR_WORKSPACE;
+  int* piv = static_cast<int*>(workspace);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (precision == 0)
+    return launch_inverse_blocked<double>(batch, n, static_cast<cplx<double>*>(A), n, a_stride,
+                                          static_cast<cplx<double>*>(Ainv), n, inv_stride, piv, status, s);
+  return launch_inverse_blocked<float>(batch, n, static_cast<cplx<float>*>(A), n, a_stride,
+                                       static_cast<cplx<float>*>(Ainv), n, inv_stride, piv, status, s);
+}
+
+}  // extern "C"
