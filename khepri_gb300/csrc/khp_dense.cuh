@@ -702,29 +702,30 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
       for (int k = k0; k < k1; ++k) {
         const int lk = k - r0;  // window row of k
         const int ck = k - c0;  // window column of k
+        // every lane forms the same rotation from the same (broadcast) window entries, so c and
+        // s come from registers instead of through shared memory from one lane; lane 0 records
+        // them for the strip updates and writes r, 0 into column k - 1
+        cplx<T> x, y;
+        if (k == lo) {
+          x = win[lk * WS + ck] - mu;
+          y = win[(lk + 1) * WS + ck];
+        } else {
+          x = win[lk * WS + ck - 1];
+          y = win[(lk + 1) * WS + ck - 1];
+        }
+        T c;
+        cplx<T> s, r;
+        givens(x, y, c, s, r);
+        t.warp_sync();  // every lane has read x and y before the window changes
         if (lane == 0) {
-          cplx<T> x, y;
-          if (k == lo) {
-            x = win[lk * WS + ck] - mu;
-            y = win[(lk + 1) * WS + ck];
-          } else {
-            x = win[lk * WS + ck - 1];
-            y = win[(lk + 1) * WS + ck - 1];
-          }
-          T c;
-          cplx<T> s, r;
-          givens(x, y, c, s, r);
+          rc[k - k0] = c;
+          rs[k - k0] = s;
           if (k > lo) {
             win[lk * WS + ck - 1] = r;
             win[(lk + 1) * WS + ck - 1] = mk(T(0));
           }
-          rc[k - k0] = c;
-          rs[k - k0] = s;
         }
-        t.warp_sync();
-        const T c = rc[k - k0];
-        const cplx<T> s = rs[k - k0];
-        // row rotation from column k (column k-1 already holds r and 0 when k > lo)
+        // row rotation from column k (column k - 1, written above, is not read by the rotations)
         for (int j = ck + lane; j < nc; j += lanes) {
           const cplx<T> h1 = win[lk * WS + j], h2 = win[(lk + 1) * WS + j];
           win[lk * WS + j] = c * h1 + s * h2;
