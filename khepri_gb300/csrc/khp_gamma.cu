@@ -174,15 +174,15 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     const cd* Cm = reinterpret_cast<const cd*>(conv);
     GT_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps, p.midx[m],
           status);
-    GT_EW(k_assemble_pq_t<T>, batch * nn, batch, nh, Cm, reinterpret_cast<const cd*>(hx),
-          reinterpret_cast<const cd*>(hy), p.midx[m], gx, gy, kp, k0, p.M);
+    GT_TRY(launch_assemble_pq<T>(batch, nh, Cm, reinterpret_cast<const cd*>(hx), reinterpret_cast<const cd*>(hy),
+                                 p.midx[m], gx, gy, kp, k0, p.M, s));
     GT_TRY(launch_geev<T>(batch, n, p.M, n, nn, p.Z, p.W[m], n, nn, p.lam[m], n, status, s));
     GT_EW(k_sqrt_lam_t<T>, batch * n, batch * n, p.lam[m]);
     cplx<T>* CWt = p.CW;
     cplx<T>* CWb = p.CW + batch * hn;
     GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m], n, nn, zero, CWt, n, hn, s, p.midx[m]));
     GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m] + hn, n, nn, zero, CWb, n, hn, s, p.midx[m]));
-    GT_EW(k_modes_v_t<T>, batch * nn, batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, hn, p.lam[m], p.V[m], status);
+    GT_TRY(launch_modes_v<T>(batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, hn, p.lam[m], p.V[m], status, s));
     GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.lu, n, nn, s));
     GT_TRY(launch_inverse<T>(batch, n, p.lu, n, nn, p.Wi[m], n, nn, p.piv, status, s));
     GT_TRY(launch_copy<T>(batch, n, n, p.V[m], n, nn, p.lu, n, nn, s));

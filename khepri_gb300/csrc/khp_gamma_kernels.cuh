@@ -64,37 +64,64 @@ __global__ void k_convert(int64_t count, const cd* __restrict__ in, cplx<T>* out
 
 // M = P Q of one pixmap for every problem (same identity as khp_layer_modes); problem b uses
 // map midx[b] of the [nmaps][nh][nh] arrays C, Hx, Hy.
+// One grid row per problem (b = boff + blockIdx.y): the problem's per-harmonic wave vectors are
+// tabulated in shared memory first (dynamic, 2 nh complex), so no element divides.  Launched by
+// launch_assemble_pq.
 template <typename T>
-__global__ void k_assemble_pq_t(int64_t batch, int nh, const cd* __restrict__ Cm, const cd* __restrict__ Hxm,
+__global__ void k_assemble_pq_t(int64_t boff, int nh, const cd* __restrict__ Cm, const cd* __restrict__ Hxm,
                                 const cd* __restrict__ Hym, const int* __restrict__ midx, const double* gx,
                                 const double* gy, const double* kp, const double* k0, cplx<T>* M) {
-  const int n = 2 * nh;
-  const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int rc = (int)(e % nn);
-    const int r = rc / n, c = rc % n;
-    const int i = r % nh, j = c % nh;
-    const int bi = r / nh, bj = c / nh;
+  extern __shared__ cd kt_pq[];
+  cd* kxs = kt_pq;
+  cd* kys = kt_pq + nh;
+  const int64_t b = boff + blockIdx.y;
+  for (int g = threadIdx.x; g < nh; g += blockDim.x) phys::kvec(kp, k0, gx, gy, b, g, kxs[g], kys[g]);
+  __syncthreads();
+  const int n = 2 * nh, nn = n * n;
+  const int64_t moff = (int64_t)midx[b] * nh * nh;
+  const cd* C = Cm + moff;
+  const cd* Hx = Hxm + moff;
+  const cd* Hy = Hym + moff;
+  const double k = k0[b], ik = 1.0 / k;
+  const cd ax = mk(kp[4 * b + 0] / k, kp[4 * b + 1] / k), ay = mk(kp[4 * b + 2] / k, kp[4 * b + 3] / k);
+  cplx<T>* Mb = M + b * (int64_t)nn;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int r = rc / n, c = rc - r * n;
+    const int bi = r >= nh ? 1 : 0, bj = c >= nh ? 1 : 0;
+    const int i = r - bi * nh, j = c - bj * nh;
     const int64_t mo = (int64_t)i * nh + j;
-    const int64_t moff = (int64_t)midx[b] * nh * nh;
-    const cd* C = Cm + moff;
-    const cd* Hx = Hxm + moff;
-    const cd* Hy = Hym + moff;
-    const double k = k0[b];
-    const cd ax = mk(kp[4 * b + 0] / k, kp[4 * b + 1] / k), ay = mk(kp[4 * b + 2] / k, kp[4 * b + 3] / k);
-    cd kxi, kyi;
-    phys::kvec(kp, k0, gx, gy, b, i, kxi, kyi);
+    const cd kxi = kxs[i], kyi = kys[i];
     const bool dg = (i == j);
-    const cd gxv = Hx[mo] * (1.0 / k) + (dg ? ax : mk(0.0));
-    const cd gyv = Hy[mo] * (1.0 / k) + (dg ? ay : mk(0.0));
+    const cd gxv = Hx[mo] * ik + (dg ? ax : mk(0.0));
+    const cd gyv = Hy[mo] * ik + (dg ? ay : mk(0.0));
     cd v;
     if (bi == 0 && bj == 0) v = kxi * gxv - C[mo] + (dg ? kyi * kyi : mk(0.0));
     else if (bi == 0) v = kxi * gyv - (dg ? kxi * kyi : mk(0.0));
     else if (bj == 0) v = kyi * gxv - (dg ? kxi * kyi : mk(0.0));
     else v = kyi * gyv - C[mo] + (dg ? kxi * kxi : mk(0.0));
-    M[e] = to_t<T>(v);
+    Mb[rc] = to_t<T>(v);
   }
+}
+
+// CTAs per problem of the per-problem element-wise kernels: ~2048 elements each, at most 64.
+inline unsigned per_problem_blocks(int64_t elems) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((elems + 2047) / 2048, 64));
+}
+
+// M = P Q of every problem (k_assemble_pq_t), in launches of at most 65535 problems.
+template <typename T>
+int launch_assemble_pq(int64_t batch, int nh, const cd* Cm, const cd* Hx, const cd* Hy, const int* midx,
+                       const double* gx, const double* gy, const double* kp, const double* k0, cplx<T>* M,
+                       cudaStream_t s) {
+  const size_t smem = sizeof(cd) * 2 * (size_t)nh;
+  if (smem > 48 * 1024) return KHP_ERR_TOO_LARGE;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned nb = (unsigned)std::min<int64_t>(batch - off, 65535);
+    k_assemble_pq_t<T><<<dim3(per_problem_blocks(4 * (int64_t)nh * nh), nb), 256, smem, s>>>(off, nh, Cm, Hx, Hy,
+                                                                                         midx, gx, gy, kp, k0, M);
+    count_launches(1);
+  }
+  return cuda_status();
 }
 
 template <typename T>
@@ -104,30 +131,57 @@ __global__ void k_sqrt_lam_t(int64_t count, cplx<T>* lam) {
 }
 
 // V = Q W / lam (alternative.py:167-176), CWt = C W_top, CWb = C W_bottom ([nh][n] each, batch
-// stride cws).
+// stride cws).  One grid row per problem (b = boff + blockIdx.y) with the problem's wave vectors and
+// the reciprocals of its lam tabulated in shared memory (dynamic, 4 nh complex); launched by
+// launch_modes_v.
 template <typename T>
-__global__ void k_modes_v_t(int64_t batch, int nh, const double* gx, const double* gy, const double* kp,
+__global__ void k_modes_v_t(int64_t boff, int nh, const double* gx, const double* gy, const double* kp,
                             const double* k0, const cplx<T>* __restrict__ W, const cplx<T>* __restrict__ CWt,
                             const cplx<T>* __restrict__ CWb, int64_t cws, const cplx<T>* __restrict__ lam, cplx<T>* V,
                             int* status) {
-  const int n = 2 * nh;
-  const int64_t nn = (int64_t)n * n, hn = cws;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int rc = (int)(e % nn);
-    const int r = rc / n, c = rc % n;
-    const int i = r % nh;
-    cd kx, ky;
-    phys::kvec(kp, k0, gx, gy, b, i, kx, ky);
-    const cd wt = to_d(W[b * nn + (int64_t)i * n + c]), wb = to_d(W[b * nn + (int64_t)(nh + i) * n + c]);
+  extern __shared__ cd kt_v[];
+  const int n = 2 * nh, nn = n * n;
+  cd* kxs = kt_v;
+  cd* kys = kxs + nh;
+  cd* il = kys + nh;  // 1 / lam[c]
+  const int64_t b = boff + blockIdx.y;
+  for (int g = threadIdx.x; g < nh; g += blockDim.x) phys::kvec(kp, k0, gx, gy, b, g, kxs[g], kys[g]);
+  for (int c = threadIdx.x; c < n; c += blockDim.x) il[c] = cdiv(mk(1.0), to_d(lam[b * n + c]));
+  __syncthreads();
+  const cplx<T>* Wb = W + b * (int64_t)nn;
+  const cplx<T>* Ct = CWt + b * cws;
+  const cplx<T>* Cb = CWb + b * cws;
+  cplx<T>* Vb = V + b * (int64_t)nn;
+  bool bad = false;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int r = rc / n, c = rc - r * n;
+    const int i = r < nh ? r : r - nh;
+    const cd kx = kxs[i], ky = kys[i];
+    const cd wt = to_d(Wb[(int64_t)i * n + c]), wb = to_d(Wb[(int64_t)(nh + i) * n + c]);
     const cd kxy = kx * ky;
     cd q;
-    if (r < nh) q = kxy * wt - kx * kx * wb + to_d(CWb[b * hn + (int64_t)i * n + c]);
-    else q = ky * ky * wt - to_d(CWt[b * hn + (int64_t)i * n + c]) - kxy * wb;
-    const cd v = cdiv(q, to_d(lam[b * n + c]));
-    V[e] = to_t<T>(v);
-    if (!cfinite(v)) atomicOr(status + b, KHP_BIT_NONFINITE);
+    if (r < nh) q = kxy * wt - kx * kx * wb + to_d(Cb[(int64_t)i * n + c]);
+    else q = ky * ky * wt - to_d(Ct[(int64_t)i * n + c]) - kxy * wb;
+    const cd v = q * il[c];
+    Vb[rc] = to_t<T>(v);
+    bad |= !cfinite(v);
   }
+  if (bad) atomicOr(status + b, KHP_BIT_NONFINITE);
+}
+
+template <typename T>
+int launch_modes_v(int64_t batch, int nh, const double* gx, const double* gy, const double* kp, const double* k0,
+                   const cplx<T>* W, const cplx<T>* CWt, const cplx<T>* CWb, int64_t cws, const cplx<T>* lam,
+                   cplx<T>* V, int* status, cudaStream_t s) {
+  const size_t smem = sizeof(cd) * 4 * (size_t)nh;
+  if (smem > 48 * 1024) return KHP_ERR_TOO_LARGE;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned nb = (unsigned)std::min<int64_t>(batch - off, 65535);
+    k_modes_v_t<T><<<dim3(per_problem_blocks(4 * (int64_t)nh * nh), nb), 256, smem, s>>>(off, nh, gx, gy, kp, k0, W,
+                                                                                    CWt, CWb, cws, lam, V, status);
+    count_launches(1);
+  }
+  return cuda_status();
 }
 
 // Free-space V0 blocks and their inverses per problem and harmonic, [batch][nh] (FP64; computed

@@ -1046,13 +1046,13 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     for (int m = 0; m < S; ++m)
       MX_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps,
             midx + (int64_t)m * batch, sx + (int64_t)m * batch);
-    MX_EW(k_assemble_pq_t<float>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32);
+    MX_TRY(launch_assemble_pq<float>(bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32, s));
     stage_begin(KHP_STAGE_EIGENSOLVE, s);
     MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s));
     stage_end(KHP_STAGE_EIGENSOLVE, s);
     // Refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 inverse of the current W, held
     // in Wi until the final inverse), mu += diag(E), W += W F.
-    MX_EW(k_assemble_pq_t<double>, bm * nn, bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M64);
+    MX_TRY(launch_assemble_pq<double>(bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M64, s));
     MX_EW(k_to_double, bm * nn, bm * nn, W32, W64);
     MX_EW(k_to_double, bm * n, bm * n, lam32, p.mu64);
     MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
@@ -1094,7 +1094,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     cd* CWb = p.CW64 + hn;
     MX_TRY(ozaki_zgemm(bm, nh, n, nh, Cm, nh, hh, midx, W64, n, nn, CWt, n, nn, p.oz, s));
     MX_TRY(ozaki_zgemm(bm, nh, n, nh, Cm, nh, hh, midx, W64 + hn, n, nn, CWb, n, nn, p.oz, s));
-    MX_EW(k_modes_v_t<double>, bm * nn, bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, nn, lam64, V64, sx);
+    MX_TRY(launch_modes_v<double>(bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, nn, lam64, V64, sx, s));
     MX_EW(k_round, bm * nn, bm * nn, V64, V32);
     // FP32 inverses and V0 products
     MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
