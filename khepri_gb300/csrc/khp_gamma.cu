@@ -201,10 +201,10 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
   GT_EW(k_gamma_from_blocks<T>, batch * nn, batch, nh, p.trn, 0, p.G);
   for (int l = nlayers - 1; l >= 0; --l) {
     if (kinds[l] != 1) {
-      GT_EW(k_i_minus_sg<T>, batch * nn, batch, nh, p.blocks[l], p.G, p.lu1[l]);
+      GT_TRY(launch_i_minus_sg<T>(batch, nh, p.blocks[l], p.G, p.lu1[l], s));
       GT_TRY(launch_getrf<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], status, s));
       GT_TRY(launch_getrs_right<T>(batch, n, p.lu1[l], n, nn, p.piv1[l], p.G, n, nn, n, s));  // G <- G M^-1
-      GT_EW(k_sandwich<T>, batch * nn, batch, nh, p.blocks[l], p.G, p.F);
+      GT_TRY(launch_sandwich<T>(batch, nh, p.blocks[l], p.G, p.F, s));
       std::swap(p.G, p.F);
     } else {
       const int m = slot[l];
@@ -229,7 +229,7 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     }
   }
   // ---- incidence half-space: M0 = I - S22 G, u = M0^-1 S21 c, r = S11 c + S12 G u ----
-  GT_EW(k_i_minus_sg<T>, batch * nn, batch, nh, p.inc, p.G, p.lu);
+  GT_TRY(launch_i_minus_sg<T>(batch, nh, p.inc, p.G, p.lu, s));
   GT_TRY(launch_getrf<T>(batch, n, p.lu, n, nn, p.pivs, status, s));
   GT_EW(k_src_cols<T>, batch * n * 2, batch, nh, p.inc, 2, p.u);
   GT_TRY(launch_getrs<T>(batch, n, p.lu, n, nn, p.pivs, p.u, 2, 2 * n, 2, s));

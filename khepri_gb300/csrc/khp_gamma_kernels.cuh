@@ -267,45 +267,100 @@ __global__ void k_gamma_from_blocks(int64_t batch, int nh, const M2* __restrict_
   }
 }
 
-// out = I - S22 Gamma (S22 per-harmonic blocks).
+// A 2x2 block in the output precision (per-problem tables of the kernels below).
 template <typename T>
-__global__ void k_i_minus_sg(int64_t batch, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ G,
+struct M2t {
+  cplx<T> a, b, c, d;
+};
+template <typename T>
+__device__ __forceinline__ M2t<T> to_m2t(const M2& m) {
+  return M2t<T>{to_t<T>(m.a), to_t<T>(m.b), to_t<T>(m.c), to_t<T>(m.d)};
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> blkt(const M2t<T>& m, int r, int c) {
+  return r == 0 ? (c == 0 ? m.a : m.b) : (c == 0 ? m.c : m.d);
+}
+
+// out = I - S22 Gamma (S22 per-harmonic blocks), in T.  One grid row per problem (b = boff +
+// blockIdx.y), the problem's S22 blocks tabulated in shared memory; launch_i_minus_sg.
+template <typename T>
+__global__ void k_i_minus_sg(int64_t boff, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ G,
                              cplx<T>* out) {
-  const int n = 2 * nh;
-  const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int rc = (int)(e % nn);
-    const int r = rc / n, c = rc % n;
-    const int g = r % nh, rb = r / nh;
-    const M2& s22 = S[(b * nh + g) * 4 + 3];
-    const cd v = blk(s22, rb, 0) * to_d(G[b * nn + (int64_t)g * n + c]) + blk(s22, rb, 1) * to_d(G[b * nn + (int64_t)(nh + g) * n + c]);
-    out[e] = to_t<T>((r == c ? mk(1.0) : mk(0.0)) - v);
+  extern __shared__ unsigned char kt_sg[];
+  M2t<T>* s22 = reinterpret_cast<M2t<T>*>(kt_sg);
+  const int64_t b = boff + blockIdx.y;
+  for (int g = threadIdx.x; g < nh; g += blockDim.x) s22[g] = to_m2t<T>(S[(b * nh + g) * 4 + 3]);
+  __syncthreads();
+  const int n = 2 * nh, nn = n * n;
+  const cplx<T>* Gb = G + b * (int64_t)nn;
+  cplx<T>* ob = out + b * (int64_t)nn;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int r = rc / n, c = rc - r * n;
+    const int rb = r >= nh ? 1 : 0, g = r - rb * nh;
+    const M2t<T> m = s22[g];
+    const cplx<T> v = blkt(m, rb, 0) * Gb[(int64_t)g * n + c] + blkt(m, rb, 1) * Gb[(int64_t)(nh + g) * n + c];
+    ob[rc] = (r == c ? mk(T(1)) : mk(T(0))) - v;
   }
 }
 
-// out = S11 + S12 Z S21 (all S blocks per-harmonic).
+// out = S11 + S12 Z S21 (all S blocks per-harmonic), in T; layout as k_i_minus_sg, the problem's
+// S11, S12 and S21 blocks tabulated; launch_sandwich.
 template <typename T>
-__global__ void k_sandwich(int64_t batch, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ Z, cplx<T>* out) {
-  const int n = 2 * nh;
-  const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int rc = (int)(e % nn);
-    const int r = rc / n, c = rc % n;
-    const int gi = r % nh, ri = r / nh, gj = c % nh, cj = c / nh;
-    const M2* Si = S + (b * nh + gi) * 4;
-    const M2* Sj = S + (b * nh + gj) * 4;
-    const cplx<T>* Zb = Z + b * nn;
-    cd acc = gi == gj ? blk(Si[0], ri, cj) : mk(0.0);
-    for (int ra = 0; ra < 2; ++ra) {
-      const cd s12 = blk(Si[1], ri, ra);
-      const int a = ra * nh + gi;
-      const cd z0 = to_d(Zb[(int64_t)a * n + gj]), z1 = to_d(Zb[(int64_t)a * n + nh + gj]);
-      acc += s12 * (z0 * blk(Sj[2], 0, cj) + z1 * blk(Sj[2], 1, cj));
-    }
-    out[e] = to_t<T>(acc);
+__global__ void k_sandwich(int64_t boff, int nh, const M2* __restrict__ S, const cplx<T>* __restrict__ Z,
+                           cplx<T>* out) {
+  extern __shared__ unsigned char kt_sw[];
+  M2t<T>* s11 = reinterpret_cast<M2t<T>*>(kt_sw);
+  M2t<T>* s12 = s11 + nh;
+  M2t<T>* s21 = s12 + nh;
+  const int64_t b = boff + blockIdx.y;
+  for (int g = threadIdx.x; g < nh; g += blockDim.x) {
+    const M2* Sg = S + (b * nh + g) * 4;
+    s11[g] = to_m2t<T>(Sg[0]);
+    s12[g] = to_m2t<T>(Sg[1]);
+    s21[g] = to_m2t<T>(Sg[2]);
   }
+  __syncthreads();
+  const int n = 2 * nh, nn = n * n;
+  const cplx<T>* Zb = Z + b * (int64_t)nn;
+  cplx<T>* ob = out + b * (int64_t)nn;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int r = rc / n, c = rc - r * n;
+    const int ri = r >= nh ? 1 : 0, cj = c >= nh ? 1 : 0;
+    const int gi = r - ri * nh, gj = c - cj * nh;
+    const M2t<T> sj = s21[gj];
+    cplx<T> acc = gi == gj ? blkt(s11[gi], ri, cj) : mk(T(0));
+    for (int ra = 0; ra < 2; ++ra) {
+      const cplx<T> sv = blkt(s12[gi], ri, ra);
+      const int a = ra * nh + gi;
+      const cplx<T> z0 = Zb[(int64_t)a * n + gj], z1 = Zb[(int64_t)a * n + nh + gj];
+      acc += sv * (z0 * blkt(sj, 0, cj) + z1 * blkt(sj, 1, cj));
+    }
+    ob[rc] = acc;
+  }
+}
+
+template <typename T>
+int launch_i_minus_sg(int64_t batch, int nh, const M2* S, const cplx<T>* G, cplx<T>* out, cudaStream_t s) {
+  const size_t smem = sizeof(M2t<T>) * (size_t)nh;
+  if (smem > 48 * 1024) return KHP_ERR_TOO_LARGE;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned nb = (unsigned)std::min<int64_t>(batch - off, 65535);
+    k_i_minus_sg<T><<<dim3(per_problem_blocks(4 * (int64_t)nh * nh), nb), 256, smem, s>>>(off, nh, S, G, out);
+    count_launches(1);
+  }
+  return cuda_status();
+}
+
+template <typename T>
+int launch_sandwich(int64_t batch, int nh, const M2* S, const cplx<T>* Z, cplx<T>* out, cudaStream_t s) {
+  const size_t smem = sizeof(M2t<T>) * 3 * (size_t)nh;
+  if (smem > 48 * 1024) return KHP_ERR_TOO_LARGE;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned nb = (unsigned)std::min<int64_t>(batch - off, 65535);
+    k_sandwich<T><<<dim3(per_problem_blocks(4 * (int64_t)nh * nh), nb), 256, smem, s>>>(off, nh, S, Z, out);
+    count_launches(1);
+  }
+  return cuda_status();
 }
 
 // A = F - G (into a), B = F + G (into f).

@@ -1124,10 +1124,10 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   for (int l = L - 1; l >= 0; --l) {
     cf* G = gam(l + 1);
     if (kinds[l] != 1) {
-      MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.blocks[l], G, p.lu32);
+      MX_TRY(launch_i_minus_sg<float>(batch, nh, p.blocks[l], G, p.lu32, s));
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, G, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));
-      MX_EW(k_sandwich<float>, batch * nn, batch, nh, p.blocks[l], p.zr[l], gam(l));
+      MX_TRY(launch_sandwich<float>(batch, nh, p.blocks[l], p.zr[l], gam(l), s));
     } else {
       const int m = slot[l];
       MX_TRY(launch_copy<float>(batch, n, n, p.Wi[m], n, nn, p.F, n, nn, s));
@@ -1149,7 +1149,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Gb, n, nn, p.inv2[l], n, nn, zero, gam(l), n, nn, s));
     }
   }
-  MX_EW(k_i_minus_sg<float>, batch * nn, batch, nh, p.inc, gam(0), p.lu32);
+  MX_TRY(launch_i_minus_sg<float>(batch, nh, p.inc, gam(0), p.lu32, s));
   MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv0, n, nn, p.piv, status, s));
   stage_end(KHP_STAGE_RECURSION, s);
   // ---- 3. iterative refinement of the stack equations ----
