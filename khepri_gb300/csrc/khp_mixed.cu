@@ -71,12 +71,15 @@ __global__ void __launch_bounds__(256) k_find_pairs(int n, const cd* __restrict_
   for (int i = t.tid(); i < n; i += t.size()) {
     const double a = cabs(m[i]);
     if (a > big) { big = a; bi = i; }
+    // nearest by squared distance (the same minimum, without a square root per pair)
     double best = 1e300;
     int bj = -1;
+    const cd mi = m[i];
     for (int j = 0; j < n; ++j) {
       if (j == i) continue;
-      const double d = cabs(m[j] - m[i]);
-      if (d < best) { best = d; bj = j; }
+      const double dr = m[j].re - mi.re, di = m[j].im - mi.im;
+      const double d2 = dr * dr + di * di;
+      if (d2 < best) { best = d2; bj = j; }
     }
     nr[i] = bj;
   }
