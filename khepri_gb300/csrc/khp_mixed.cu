@@ -46,12 +46,14 @@ constexpr int kExtraRounds = 12;
 // Eigen-refinement kernels
 // ------------------------------------------------------------------------------------------
 // R32 = (M64 W64 - W64 diag(mu)) in FP32, where MW already holds M64 W64.
-__global__ void k_eig_residual(int64_t batch, int n, const cd* __restrict__ MW, const cd* __restrict__ W64,
+// One grid row per problem (b = boff + blockIdx.y), launched by MX_PP.
+__global__ void k_eig_residual(int64_t boff, int n, const cd* __restrict__ MW, const cd* __restrict__ W64,
                                const cd* __restrict__ mu, cf* R32) {
   const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int j = (int)(e % nn) % n;
+  const int64_t b = boff + blockIdx.y;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int64_t e = b * nn + rc;
+    const int j = rc % n;
     const cd r = MW[e] - W64[e] * mu[b * n + j];
     R32[e] = mk((float)r.re, (float)r.im);
   }
@@ -102,13 +104,14 @@ __device__ __forceinline__ cd pair_den(cd a, cd b, cd c, cd d) {
 
 // mu_out = mu_in + diag(E) and F_ij = E_ij / (mu_j - mu_i), except for close pairs, which take
 // the exact 2x2 update; other pairs closer than 1e-5 relative stay coupled (F = 0).
-__global__ void k_eig_update(int64_t batch, int n, const cd* __restrict__ mu_in, const cf* __restrict__ E, cf* F,
+// (one grid row per problem, b = boff + blockIdx.y, launched by MX_PP)
+__global__ void k_eig_update(int64_t boff, int n, const cd* __restrict__ mu_in, const cf* __restrict__ E, cf* F,
                              cd* mu_out, const int* __restrict__ pair) {
   const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / nn;
-    const int rc = (int)(e % nn);
-    const int i = rc / n, j = rc % n;
+  const int64_t b = boff + blockIdx.y;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int64_t e = b * nn + rc;
+    const int i = rc / n, j = rc - i * n;
     const cf* Eb = E + b * nn;
     const int pi = pair[b * n + i];
     cd out = mk(0.0);
@@ -917,6 +920,18 @@ GradPlan plan_grad(Arena& a, int64_t batch, int nh, int L, int64_t nmaps) {
     MX_TRY(cuda_status());                                               \
   } while (0)
 
+// A per-problem element-wise kernel (first parameter: the problem offset of the launch; one grid
+// row per problem, per_problem_blocks(elems) CTAs along x), in launches of at most 65535 problems.
+#define MX_PP(kernel, nprob, elems, ...)                                                               \
+  do {                                                                                                 \
+    for (int64_t _o = 0; _o < (int64_t)(nprob); _o += 65535) {                                         \
+      const unsigned _nb = (unsigned)std::min<int64_t>((int64_t)(nprob) - _o, 65535);                  \
+      kernel<<<dim3(per_problem_blocks(elems), _nb), 256, 0, s>>>(_o, __VA_ARGS__);                    \
+      count_launches(1);                                                                               \
+    }                                                                                                  \
+    MX_TRY(cuda_status());                                                                             \
+  } while (0)
+
 // Backward stage of khp_solve_batched_mixed_grad (after the forward refinement): loss seeds,
 // the adjoint solve (FP64 transposed residual + FP32 transposed sweep, refine + 3 rounds), the
 // per-layer M-gradients and the convolution-matrix gradient of every map.
@@ -1076,12 +1091,12 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       }
       if (step == 0 || last)
         MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
-      MX_EW(k_eig_residual, bm * nn, bm, n, p.MW64, W64, mu_a, p.E32);
+      MX_PP(k_eig_residual, bm, nn, n, p.MW64, W64, mu_a, p.E32);
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
       k_find_pairs<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
       count_launches(1);
       MX_TRY(cuda_status());
-      MX_EW(k_eig_update, bm * nn, bm, n, mu_a, p.Z32, p.M32, mu_b, p.pair);  // M32 <- F
+      MX_PP(k_eig_update, bm, nn, n, mu_a, p.Z32, p.M32, mu_b, p.pair);  // M32 <- F
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, W32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
       MX_EW(k_add_correction, bm * nn, bm * nn, W64, p.Z32, W32);
       if (!last) {
