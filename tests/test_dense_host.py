@@ -1,0 +1,112 @@
+"""The team-generic dense kernels (Hessenberg reduction, windowed QR, eigenvectors, LU) compiled
+for the host and run by a team of one thread: the same source as the GPU kernels, checked here
+against numpy on every CPU run (tests/host/team_dense_host.cpp)."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("needs g++")
+    out = tmp_path_factory.mktemp("teamhost") / "libteamhost.so"
+    src = os.path.join(ROOT, "tests", "host", "team_dense_host.cpp")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"), "-I",
+                    os.path.join(ROOT, "khepri_gb300", "csrc"), src, "-o", str(out)], check=True)
+    L = ctypes.CDLL(str(out))
+    P, I = ctypes.c_void_p, ctypes.c_int
+    L.host_gehrd.argtypes = [I, P, P, I]
+    L.host_geev.argtypes = [I, P, P, P]
+    L.host_geev_f32.argtypes = [I, P, P, P]
+    L.host_gesv.argtypes = [I, I, P, P]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _rand(n, seed, dtype=np.complex128):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(dtype)
+
+
+@pytest.mark.parametrize("n", [8, 64, 97, 131])
+def test_hessenberg_blocked_matches_unblocked(lib, n):
+    A = _rand(n, n)
+    out = {}
+    for blocked in (0, 1):
+        H = A.copy()
+        Z = np.zeros_like(A)
+        lib.host_gehrd(n, _p(H), _p(Z), blocked)
+        assert np.abs(np.tril(H, -2)).max() == 0.0
+        assert np.abs(Z.conj().T @ Z - np.eye(n)).max() < 1e-13
+        assert np.abs(Z @ H @ Z.conj().T - A).max() / np.abs(A).max() < 1e-13
+        out[blocked] = (H, Z)
+    # the same reflectors, applied in another order: the same H and Q up to rounding
+    assert np.abs(out[0][0] - out[1][0]).max() < 1e-10
+    assert np.abs(out[0][1] - out[1][1]).max() < 1e-11
+
+
+def _match(lam, ref):
+    """max |lam_i - ref_j| over a greedy nearest matching."""
+    ref = list(ref)
+    worst = 0.0
+    for v in lam:
+        k = int(np.argmin(np.abs(np.asarray(ref) - v)))
+        worst = max(worst, abs(ref[k] - v))
+        ref.pop(k)
+    return worst
+
+
+@pytest.mark.parametrize("n", [1, 2, 33, 70, 150])
+def test_geev_fp64(lib, n):
+    A = _rand(n, 100 + n)
+    W = np.zeros_like(A)
+    lam = np.zeros(n, np.complex128)
+    assert lib.host_geev(n, _p(A.copy()), _p(W), _p(lam)) == 0
+    scale = np.abs(A).max() * n
+    assert np.abs(A @ W - W * lam).max() / (scale * np.abs(W).max()) < 1e-13
+    assert _match(lam, np.linalg.eigvals(A)) / scale < 1e-12
+
+
+def test_geev_fp32(lib):
+    n = 80
+    A = _rand(n, 5, np.complex64)
+    W = np.zeros_like(A)
+    lam = np.zeros(n, np.complex64)
+    assert lib.host_geev_f32(n, _p(A.copy()), _p(W), _p(lam)) == 0
+    A64, W64 = A.astype(np.complex128), W.astype(np.complex128)
+    assert np.abs(A64 @ W64 - W64 * lam).max() / (np.abs(A).max() * n * np.abs(W).max()) < 1e-5
+
+
+def test_geev_repeated_and_real_spectrum(lib):
+    # a defect-free matrix with a double eigenvalue and a real one
+    n = 12
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    d = np.array([2.0, 2.0] + list(rng.standard_normal(n - 2)), dtype=np.complex128)
+    A = X @ np.diag(d) @ np.linalg.inv(X)
+    W = np.zeros_like(A)
+    lam = np.zeros(n, np.complex128)
+    assert lib.host_geev(n, _p(A.copy()), _p(W), _p(lam)) == 0
+    assert _match(lam, d) < 1e-8
+
+
+@pytest.mark.parametrize("n,m", [(5, 1), (40, 3), (100, 7)])
+def test_lu_solve(lib, n, m):
+    A = _rand(n, 200 + n)
+    rng = np.random.default_rng(n)
+    B = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+    X = B.copy()
+    assert lib.host_gesv(n, m, _p(A.copy()), _p(X)) == 0
+    ref = np.linalg.solve(A, B)
+    assert np.abs(X - ref).max() / np.abs(ref).max() < 1e-11
