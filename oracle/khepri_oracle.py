@@ -5,7 +5,7 @@ This module restates, in plain numpy complex128 with LAPACK-backed dense solves 
 ``Crystal.solve`` + ``poynting_flux_end`` + ``fields_volume``.  Every function names the
 reference lines it follows (paths relative to the reference project root).
 
-Who may use it: ``tests/``, ``__graft_entry__.smoke()`` (as the checker) and ``bench.py``
+Who may use it: ``tests/``, ``__graft_entry__.smoke()`` (to check the GPU result) and ``bench.py``
 (its ``cpu_baseline`` leg and ``--impl reference`` arm).  The product package
 ``khepri_gb300`` never imports it.
 
