@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_gemm(int n, int m, int k, cplx<T> alpha
                                               int64_t lda, int64_t bsA, const cplx<T>* __restrict__ B, int64_t ldb,
                                               int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
                                               int64_t boff, const int* __restrict__ aidx,
-                                              const int* __restrict__ bidx) {
+                                              const int* __restrict__ bidx, cplx<T> bshift) {
   constexpr int TM = BM / 16, TN = BN / 16;
   constexpr int LA = BM * BK / 256, LB = BK * BN / 256;  // tile elements loaded per thread
   static_assert(LA * 256 == BM * BK && LB * 256 == BK * BN, "tile loads must split evenly over 256 threads");
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256) k_gemm(int n, int m, int k, cplx<T> alpha
     for (int q = 0; q < LB; ++q) {
       const int e = threadIdx.x + 256 * q, r = e / BN, c = e % BN;
       const int gr = k0 + r, gc = col0 + c;
-      rb[q] = (gr < k && gc < m) ? B[(int64_t)gr * ldb + gc] : mk(T(0));
+      rb[q] = (gr < k && gc < m) ? B[(int64_t)gr * ldb + gc] + (gr == gc ? bshift : mk(T(0))) : mk(T(0));
     }
   };
   auto stage = [&]() {
@@ -629,7 +629,7 @@ int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bs
 template <typename T>
 int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda, int64_t bsA,
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
-                cudaStream_t s, const int* aidx, const int* bidx) {
+                cudaStream_t s, const int* aidx, const int* bidx, cplx<T> bshift) {
   if (batch <= 0 || n <= 0 || m <= 0) return KHP_OK;
   // 64 x 64 tiles (4 x 4 outputs per thread) once both output dimensions reach 64; 32 x 128
   // (2 x 8) for outputs of at most 32 rows and at least 128 columns (the block rows of the
@@ -642,13 +642,13 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
     dim3 grid((m + BN - 1) / BN, (n + BM - 1) / BM, nb);
     if (wide)
       k_gemm<T, 32, 128, 16><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
-                                                  aidx, bidx);
+                                                  aidx, bidx, bshift);
     else if (big)
       k_gemm<T, 64, 64, 8><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
-                                                aidx, bidx);
+                                                aidx, bidx, bshift);
     else
       k_gemm<T, 32, 32, 16><<<grid, 256, 0, s>>>(n, m, k, alpha, A, lda, bsA, B, ldb, bsB, beta, C, ldc, bsC, off,
-                                                 aidx, bidx);
+                                                 aidx, bidx, bshift);
     count_launches(1);
   }
   return cuda_status();
@@ -883,7 +883,7 @@ int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_
                                int64_t, int, cudaStream_t);                                                     \
   template int launch_gemm<T>(int64_t, int, int, int, cplx<T>, const cplx<T>*, int64_t, int64_t, const cplx<T>*, \
                               int64_t, int64_t, cplx<T>, cplx<T>*, int64_t, int64_t, cudaStream_t, const int*, \
-                              const int*);                                                                      \
+                              const int*, cplx<T>);                                                             \
   template int launch_geev<T>(int64_t, int, cplx<T>*, int64_t, int64_t, cplx<T>*, cplx<T>*, int64_t, int64_t,  \
                               cplx<T>*, int64_t, int*, cudaStream_t);                                           \
   template int launch_copy<T>(int64_t, int, int, const cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t,  \

@@ -23,7 +23,7 @@ int launch_getrs(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bs
 template <typename T>
 int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>* A, int64_t lda, int64_t bsA,
                 const cplx<T>* B, int64_t ldb, int64_t bsB, cplx<T> beta, cplx<T>* C, int64_t ldc, int64_t bsC,
-                cudaStream_t s, const int* aidx = nullptr, const int* bidx = nullptr);
+                cudaStream_t s, const int* aidx = nullptr, const int* bidx = nullptr, cplx<T> bshift = cplx<T>{});
 
 // Eigen-decomposition A W = W diag(lam); A destroyed; Z: batch x n x n scratch (ld n).
 template <typename T>

@@ -1171,20 +1171,22 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_TRY(launch_sandwich<float>(batch, nh, p.blocks[l], p.zr[l], gam(l), s));
     } else {
       const int m = slot[l];
-      MX_TRY(launch_copy<float>(batch, n, n, p.Wi[m], n, nn, p.F, n, nn, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, G, n, nn, one, p.F, n, nn, s));
-      MX_TRY(launch_copy<float>(batch, n, n, p.Q0[m], n, nn, p.Gb, n, nn, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Q0[m], n, nn, G, n, nn, mone, p.Gb, n, nn, s));
+      // F = Wi (G + I), Gb = Q0 (G - I): the identity added to G's diagonal as the tiles load
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, G, n, nn, zero, p.F, n, nn, s, nullptr, nullptr,
+                                one));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Q0[m], n, nn, G, n, nn, zero, p.Gb, n, nn, s, nullptr, nullptr,
+                                mone));
       MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.F, p.Gb, p.lu32);
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.F, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));  // rho
       MX_TRY(launch_copy<float>(batch, n, n, p.zr[l], n, nn, p.F, n, nn, s));
       MX_EW(k_xvec<float>, batch * n, batch, n, p.lam32[m], depth_of(l), k0, p.xv);
       MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.xv, p.F);
-      MX_TRY(launch_copy<float>(batch, n, n, p.W32[m], n, nn, p.Gb, n, nn, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, one, p.Gb, n, nn, s));
-      MX_TRY(launch_copy<float>(batch, n, n, p.Vt[m], n, nn, p.P, n, nn, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Vt[m], n, nn, p.F, n, nn, mone, p.P, n, nn, s));
+      // Gb = W (F + I), P = Vt (F - I)
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, zero, p.Gb, n, nn, s, nullptr,
+                                nullptr, one));
+      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Vt[m], n, nn, p.F, n, nn, zero, p.P, n, nn, s, nullptr,
+                                nullptr, mone));
       MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.Gb, p.P, p.lu32);
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv2[l], n, nn, p.piv, status, s));
       MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Gb, n, nn, p.inv2[l], n, nn, zero, gam(l), n, nn, s));
