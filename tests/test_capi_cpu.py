@@ -65,6 +65,31 @@ def test_invalid_arguments_rejected_without_gpu(lib):
                         None, None) == 1
 
 
+def test_newer_entry_points_validate_before_any_gpu_work(lib):
+    # Each call below returns before it touches a pointer or the GPU: a bad argument (1), an
+    # empty batch (0) or missing scratch (2).  P is a non-null placeholder that is never used.
+    P = ctypes.c_void_p(256)
+    # batched inverse: null operands, unknown precision, short stride, empty batch, no workspace
+    assert lib.khp_inverse(1, 8, 0, None, 64, None, 64, None, None, 0, None) == 1
+    assert lib.khp_inverse(1, 8, 3, P, 64, P, 64, P, None, 0, None) == 1
+    assert lib.khp_inverse(1, 8, 0, P, 63, P, 64, P, None, 0, None) == 1
+    assert lib.khp_inverse(0, 8, 0, P, 64, P, 64, P, None, 0, None) == 0
+    assert lib.khp_inverse(2, 8, 0, P, 64, P, 64, P, None, 0, None) == 2
+    # FP64-accurate tensor-core product: inner size above 4096, empty batch, no workspace
+    assert lib.khp_zgemm_fp64_tc(1, 4, 4, 4097, P, 4097, 0, P, 4, 0, P, 4, 0, None, 0, None) == 1
+    assert lib.khp_zgemm_fp64_tc(0, 4, 4, 4, P, 4, 16, P, 4, 16, P, 4, 16, None, 0, None) == 0
+    assert lib.khp_zgemm_fp64_tc(1, 4, 4, 4, P, 4, 16, P, 4, 16, P, 4, 16, None, 0, None) == 2
+    # band structure from S: null S, empty batch
+    assert lib.khp_scattering_eig(1, 2, None, 64, None, None, None, None, None, 0, None) == 1
+    assert lib.khp_scattering_eig(0, 2, P, 64, P, None, None, P, None, 0, None) == 0
+    # beams: empty supercell, no workspace
+    assert lib.khp_bzi_amplitudes(0, 1, 4, P, P, P, P, 9, P, P, P, None, 0, None) == 1
+    assert lib.khp_bzi_amplitudes(2, 2, 4, P, P, P, P, 9, P, P, P, None, 0, None) == 2
+    # tmat star product and S assembly: short stride, empty batch
+    assert lib.khp_tmat_multS(1, 2, P, 63, P, 64, P, P, None, 0, None) == 1
+    assert lib.khp_tmat_matrix_s(0, 2, P, P, P, None, 0, None) == 0
+
+
 def test_no_gpu_means_loud_failure():
     import torch
     if torch.cuda.is_available():
