@@ -382,9 +382,11 @@ class OracleCrystal:
         self.S = None
 
     def add_layer_uniform(self, name, epsilon, depth):
+        """crystal.py:97-103."""
         self.layers[name] = SimpleNamespace(kind="uniform", eps=epsilon, depth=depth, fields=False)
 
     def add_layer_pixmap(self, name, epsilon, depth):
+        """crystal.py:113-117 (the array is kept by reference, layer.py:108)."""
         self.layers[name] = SimpleNamespace(kind="pixmap", eps=epsilon, depth=depth, fields=False)
 
     def add_layer_analytical(self, name, epsilon, epsilon_host, depth):
@@ -407,6 +409,7 @@ class OracleCrystal:
 
     @property
     def depth(self):
+        """crystal.py:166-178."""
         return sum(self.layers[n].depth for n in self.device_stack)
 
     def set_source(self, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, kp=None):
@@ -526,7 +529,8 @@ class OracleCrystal:
 
 def solve_rt(pw, layers, stack, wavelength, te=1.0, tm=1.0, theta=0.0, phi=0.0, kp=None,
              lattice="square", epsi=1, epse=1, only_total=True):
-    """Convenience wrapper: build a Crystal, solve once, return poynting_flux_end()."""
+    """Convenience wrapper: build a Crystal, solve once, return poynting_flux_end() (the user
+    loop of README.md:52-58 over crystal.py:180-206 and 363-396)."""
     cl = OracleCrystal(pw, lattice=lattice, epsi=epsi, epse=epse)
     for name, (kind, eps, depth) in layers.items():
         if kind == "uniform":
