@@ -38,14 +38,17 @@ class Layer:
 
     @classmethod
     def uniform(cls, expansion, epsilon, depth):
+        """layer.py:113-120."""
         return cls("uniform", epsilon, depth)
 
     @classmethod
     def pixmap(cls, expansion, pixmap, depth):
+        """layer.py:96-111."""
         return cls("pixmap", pixmap, depth)
 
     @classmethod
     def pixmap_or_uniform(cls, expansion, pixmap, depth):
+        """layer.py:77-94: a uniform layer when every pixel holds the same value."""
         eps0 = np.asarray(pixmap).flatten()[0]
         if np.all(np.asarray(pixmap) == eps0):
             return cls.uniform(expansion, eps0, depth)
@@ -58,6 +61,8 @@ class Layer:
 
     @classmethod
     def half_infinite(cls, expansion, type, epsilon):
+        """layer.py:132-143: "reflexion" (incidence side) or "transmission"; other types raise
+        (the reference prints "ERROR")."""
         if type == "reflexion":
             return cls("inc", epsilon, 0)
         if type == "transmission":
@@ -65,11 +70,13 @@ class Layer:
         raise ValueError(f"unknown half-space type {type!r}")
 
     def spec(self):
+        """The layer as the engine's LayerSpec."""
         return LayerSpec(self.kind, self.epsilon, self.depth)
 
 
 class Crystal:
-    """GPU drop-in for khepri.crystal.Crystal (square, hexagonal or explicit lattices)."""
+    """GPU drop-in for khepri.crystal.Crystal (crystal.py:42-81; square, hexagonal or explicit
+    lattices)."""
 
     def __init__(self, pw, lattice="square", lattice_pitch=1, void=False, epsi=1, epse=1, device="cuda"):
         self.pw = tuple(pw)
@@ -89,9 +96,11 @@ class Crystal:
 
     # -- layers ----------------------------------------------------------------------------
     def add_layer_uniform(self, name, epsilon, depth):
+        """crystal.py:97-103."""
         self.layers[name] = Layer("uniform", epsilon, depth)
 
     def add_pixmap_or_uniform(self, name, epsilon, depth):
+        """crystal.py:104-111."""
         sample = np.asarray(epsilon).flatten()[0]
         if np.all(np.asarray(epsilon) == sample):
             self.add_layer_uniform(name, sample, depth)
@@ -99,6 +108,7 @@ class Crystal:
             self.add_layer_pixmap(name, epsilon, depth)
 
     def add_layer_pixmap(self, name, epsilon, depth):
+        """crystal.py:113-117 (the array is kept by reference, as layer.py:108 does)."""
         self.layers[name] = Layer("pixmap", epsilon, depth)
 
     def add_layer_analytical(self, name, epsilon, epsilon_host, depth):
@@ -106,6 +116,7 @@ class Crystal:
         self.layers[name] = Layer.analytical(None, epsilon, epsilon_host, depth)
 
     def add_layer(self, name, layer, extended=False):
+        """crystal.py:125-129; extended layers belong to khepri_gb300.twisted."""
         if extended:
             raise NotImplementedError("extended (twisted) layers are not part of this GPU path")
         self.layers[name] = layer
@@ -133,18 +144,22 @@ class Crystal:
 
     @property
     def depth(self):
+        """crystal.py:166-170."""
         return sum(self.layers[name].depth for name in self.device_stack)
 
     @property
     def source_defined(self):
+        """crystal.py:172-174."""
         return self.source is not None
 
     @property
     def solved(self):
+        """crystal.py:176-178."""
         return self.S is not None
 
     @property
     def zmax(self):
+        """crystal.py:398-400."""
         return self.stack_positions[-2]
 
     # -- source / solve --------------------------------------------------------------------

@@ -45,12 +45,14 @@ def lattice_vectors(lattice="square", pitch=1.0):
 
 
 def reciprocal_basis(lat):
+    """Reciprocal lattice vectors (tools.py:64-69, reciproc)."""
     a1, a2 = lat[0], lat[1]
     s = TWOPI / (a1[0] * a2[1] - a1[1] * a2[0])
     return np.array([[a2[1] * s, -a2[0] * s], [-a1[1] * s, a1[0] * s]])
 
 
 def expansion_indices(pw):
+    """Harmonic index set, m fastest (expansion.py:4-16); odd counts only, as the reference asserts."""
     px, py = pw
     if px % 2 != 1 or py % 2 != 1:
         raise AssertionError("harmonic counts must be odd")
@@ -61,6 +63,7 @@ def expansion_indices(pw):
 
 
 def g_vectors(pw, lat):
+    """G vectors of the expansion, [2][Nh] (expansion.py:76-84)."""
     rec = reciprocal_basis(lat)
     idx = expansion_indices(pw)
     return rec[0][:, None] * idx[0][None, :] + rec[1][:, None] * idx[1][None, :]
@@ -92,14 +95,17 @@ class StageTimer:
         _TIMER = None
 
     def record(self, name):
+        """A CUDA event recorded now on the current stream."""
         e = torch.cuda.Event(enable_timing=True)
         e.record()
         return e
 
     def add(self, name, e0, e1):
+        """An interval of stage ``name`` between two recorded events."""
         self.events.setdefault(name, []).append((e0, e1))
 
     def totals_ms(self):
+        """{stage: (total ms, intervals)} (synchronises)."""
         torch.cuda.synchronize()
         return {k: (sum(a.elapsed_time(b) for a, b in v), len(v)) for k, v in self.events.items()}
 
@@ -127,6 +133,7 @@ _WS = {}
 
 
 def workspace(nbytes, device):
+    """A reusable device byte buffer of at least ``nbytes`` per device (grown, never shrunk)."""
     key = str(device)
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
@@ -172,6 +179,7 @@ def _digest(a):
 # ------------------------------------------------------------------------------------------
 @dataclass
 class LayerSpec:
+    """One layer of a stack: kind, permittivity (map or scalar) and depth."""
     kind: str  # "pixmap" | "uniform" | "inc" | "trn"
     eps: object  # 2-D array for pixmaps, complex scalar otherwise
     depth: float
@@ -245,6 +253,7 @@ class Problems:
 
     @property
     def batch(self):
+        """Number of problems."""
         return int(self.k0.shape[0])
 
     def subset(self, idx: torch.Tensor) -> "Problems":
@@ -254,6 +263,7 @@ class Problems:
 
     @classmethod
     def make(cls, wavelengths, kp, te, tm, device):
+        """Problems from host wavelengths, in-plane k (crystal.py:345-360 conventions) and sources."""
         wl = np.atleast_1d(np.asarray(wavelengths, dtype=float))
         B = wl.shape[0]
         kpa = np.asarray(kp, dtype=complex).reshape(B, 2)
@@ -268,6 +278,7 @@ class Problems:
 
 @dataclass
 class LayerState:
+    """A solved layer: its S-matrix and, for field reconstruction, its modes."""
     S: torch.Tensor  # [B, 2, 2, n, n]
     W: torch.Tensor | None = None
     V: torch.Tensor | None = None
@@ -299,6 +310,7 @@ def layer_modes(struct: StructureGPU, entry, prob: Problems, status):
 
 
 def layer_smatrix(struct: StructureGPU, W, V, lam, depth, prob: Problems, status):
+    """S-matrix of a patterned layer from its modes (alternative.py:181-195, build_scatmat)."""
     B, nh, n = prob.batch, struct.nh, struct.n
     dev = struct.device
     S = torch.empty((B, 2, 2, n, n), dtype=C128, device=dev)
@@ -318,6 +330,7 @@ _KIND = {"uniform": 0, "inc": 1, "trn": 2}
 
 
 def closed_form(struct: StructureGPU, kind, eps, depth, prob: Problems, status, want_modes=False):
+    """S-matrix of a uniform layer or a half-space in closed form (alternative.py:32-82, 130-156)."""
     B, nh, n = prob.batch, struct.nh, struct.n
     dev = struct.device
     S = torch.empty((B, 2, 2, n, n), dtype=C128, device=dev)
@@ -363,6 +376,7 @@ def identity_smatrix(B, n, device):
 
 
 def flux(struct: StructureGPU, Stot, prob: Problems, epsi, epse, orders=False):
+    """R, T (and per-order powers) from the global S (crystal.py:363-396; alternative.py:235-245)."""
     B, nh, n = prob.batch, struct.nh, struct.n
     dev = struct.device
     R = torch.empty(B, dtype=F64, device=dev)

@@ -34,9 +34,11 @@ class Expansion:
 
     @property
     def g_vectors(self):
+        """expansion.py:76-84 (a copy of the [2][Nh] G vectors)."""
         return self._g_vectors.copy()
 
     def rotate(self, angle_rad):
+        """expansion.py:52-53: rotates the G vectors in place."""
         c, s = np.cos(angle_rad), np.sin(angle_rad)
         self._g_vectors = np.array([[c, -s], [s, c]]) @ self._g_vectors
 
@@ -51,12 +53,14 @@ class Expansion:
         return e
 
     def g_vectors_expanded(self, mul):
+        """expansion.py:86-93: G vectors of a grid ``mul`` times finer (used by analytical layers)."""
         epw = [p * mul if p > 1 else 1 for p in self.pw]
         idx = engine.expansion_indices(epw)
         g = np.sum(self.reciprocal[:, :, None] * idx[:, None], axis=0)
         return g[0], g[1], epw
 
     def k_vectors(self, k_parallel, wavelength, epsilon=1):
+        """expansion.py:95-97 with _compute_k_vector (43-50): K = (k_par + G) and Kz."""
         k0 = 2 * np.pi / wavelength
         k = np.zeros((3, self._g_vectors.shape[1]), dtype=np.complex128)
         k[0:2] = np.asarray(k_parallel)[:, None] + self._g_vectors
