@@ -190,64 +190,82 @@ class CartesianLattice:
 
     @property
     def nx(self):
+        """lattice.py:61-63."""
         return (self.q[0] // 4, (self.q[0] - 1) // 4)[self.q[0] % 2]
 
     @property
     def ny(self):
+        """lattice.py:65-67."""
         return (self.q[1] // 4, (self.q[1] - 1) // 4)[self.q[1] % 2]
 
     @property
     def gx(self):
+        """lattice.py:69-75."""
         return self.Gx[self.nx:self.q[0] - self.nx, self.ny:self.q[0] - self.ny]
 
     @property
     def gy(self):
+        """lattice.py:81-86."""
         return self.Gy[self.nx:self.q[0] - self.nx, self.ny:self.q[0] - self.ny]
 
     @property
     def eta_normal(self):
+        """lattice.py:92-98 (cached)."""
         if self.eta_ is None:
             self.eta_ = compute_eta(self.gx, self.gy)
         return self.eta_
 
     def eta(self, wavelength, kp):
+        """lattice.py:100-105."""
         return compute_eta(self.gx, self.gy, kp=kp)
 
     def kp_angle(self, wavelength, theta_deg, phi_deg):
+        """lattice.py:107-111."""
         return engine.compute_kplanar(self.eps_incid, wavelength, theta_deg, phi_deg)
 
     def kzi(self, wavelength, kp):
+        """lattice.py:113-117."""
         return compute_kz(self.gx, self.gy, self.eps_incid, wavelength, kp)
 
     def kze(self, wavelength, kp):
+        """lattice.py:119-123."""
         return compute_kz(self.gx, self.gy, self.eps_emerg, wavelength, kp)
 
     def mugi(self, wavelength, kp):
+        """lattice.py:125-126."""
         return compute_mu(self.gx, self.gy, self.kzi(wavelength, kp), self.eps_incid, wavelength, kp)
 
     def muge(self, wavelength, kp):
+        """lattice.py:128-129."""
         return compute_mu(self.gx, self.gy, self.kze(wavelength, kp), self.eps_emerg, wavelength, kp)
 
     def u_blocks(self, wavelength, kp):
+        """the 4x4 blocks of diagonals of U (lattice.py:131-139), as the GPU kernels take them."""
         return _u_blocks(self.kzi(wavelength, kp), self.eta(wavelength, kp), self.mugi(wavelength, kp),
                          self.eps_incid, wavelength)
 
     def vi_blocks(self, wavelength, kp):
+        """the 4x4 blocks of diagonals of Vi (lattice.py:141-149)."""
         return _v_blocks(self.eta(wavelength, kp), self.mugi(wavelength, kp), self.eps_incid)
 
     def ve_blocks(self, wavelength, kp):
+        """the 4x4 blocks of diagonals of Ve (lattice.py:151-159)."""
         return _v_blocks(self.eta(wavelength, kp), self.muge(wavelength, kp), self.eps_emerg)
 
     def U(self, wavelength, kp):
+        """lattice.py:131-139 (dense)."""
         return _dense(self.u_blocks(wavelength, kp))
 
     def Vi(self, wavelength, kp):
+        """lattice.py:141-149 (dense)."""
         return _dense(self.vi_blocks(wavelength, kp))
 
     def Ve(self, wavelength, kp):
+        """lattice.py:151-159 (dense)."""
         return _dense(self.ve_blocks(wavelength, kp))
 
     def bz_path(self, k_points, resolutions=(), a=1.0):
+        """lattice.py:161-178."""
         main = {"G": (0, 0), "X": (0, 0.99 * np.pi / a), "M": (0.99 * np.pi / a, 0.99 * np.pi / a)}
         assert len(k_points) > 1, "Give at least two k-points"
         res = list(resolutions)
@@ -264,14 +282,17 @@ class CartesianLattice:
         return traj
 
     def g_vectors(self):
+        """lattice.py:180-183."""
         g = np.stack((self.gx.real.flat, self.gy.real.flat), axis=0).T
         yield from g
 
     def G_vectors(self):
+        """lattice.py:185-188."""
         g = np.stack((self.Gx.real.flat, self.Gy.real.flat), axis=0).T
         yield from g
 
     def restrict_radius_mask(self, radius):
+        """lattice.py:212-213."""
         return np.linalg.norm(np.array(list(self.g_vectors())), axis=-1) < radius
 
 
@@ -344,9 +365,11 @@ class LayerMatrix:
         self.S = S
 
     def numpy(self):
+        """scattering.py:13-14: the S-matrix as a numpy array."""
         return self.S.cpu().numpy() if isinstance(self.S, torch.Tensor) else self.S
 
     def copy(self):
+        """scattering.py:16-17: an independent copy."""
         return LayerMatrix(self.S.clone() if isinstance(self.S, torch.Tensor) else self.S.copy())
 
     def __matmul__(self, rhs):
