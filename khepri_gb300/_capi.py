@@ -122,10 +122,12 @@ def exported_symbols():
 
 
 def status_string(code: int) -> str:
+    """Static description of a return code (khp_status_string)."""
     return load().khp_status_string(int(code)).decode()
 
 
 def check(code: int, what: str):
+    """Raise KhpError for a non-zero return code of a libkhp call."""
     if code != 0:
         raise KhpError(f"{what} failed: {status_string(code)} (code {code})")
 
@@ -138,11 +140,13 @@ def ptr(t):
 
 
 def stream_ptr(stream=None):
+    """The CUDA stream handle for a libkhp call (torch's current stream by default)."""
     s = torch.cuda.current_stream() if stream is None else stream
     return ctypes.c_void_p(s.cuda_stream)
 
 
 def require_cuda():
+    """Raise KhpError when no CUDA device is present: the path has no CPU fallback."""
     if not torch.cuda.is_available():
         raise KhpError("libkhp needs a CUDA device; none is available (there is no CPU fallback)")
     load()
@@ -153,6 +157,7 @@ STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-fini
 
 
 def decode_status(word: int) -> str:
+    """The per-problem status bits of a status word, in words."""
     return ", ".join(v for k, v in STATUS_BITS.items() if word & k) or "ok"
 
 

@@ -24,6 +24,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE
 
 
 def nvcc():
+    """Path of nvcc (PATH, then the CUDA toolkit default)."""
     path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(path):
         raise RuntimeError("nvcc not found: libkhp needs the CUDA toolkit to build")
@@ -31,6 +32,7 @@ def nvcc():
 
 
 def sources():
+    """The CUDA sources of libkhp."""
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
