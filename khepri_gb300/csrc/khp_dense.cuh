@@ -498,12 +498,19 @@ KHP_HD void team_gehrd(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z,
 // Updates H to upper triangular T and Z <- Z Q.  Returns status bits (NOT_CONVERGED when
 // the iteration cap 30*n + 60 is reached: every loop in here is bounded).
 // ------------------------------------------------------------------------------------------
+// FP32 deflation tolerance in units of FP32's ulp (FP64: always 1).  The FP32 eigensolver only
+// starts the FP64 refinement, whose quadratic steps absorb the ~3x larger eigenvalue error;
+// measured on 242 x 242 P Q matrices: 12 % fewer rotations at 32 ulp.
+#ifndef KHP_HQR_DEFL_F32
+#define KHP_HQR_DEFL_F32 32
+#endif
+
 template <typename T>
 KHP_HD bool hqr_negligible(const cplx<T>* H, int64_t ld, int k, int hi, T smlnum) {
   const cplx<T> h = H[k * ld + k - 1];
   const T ah = abs1(h);
   if (ah <= smlnum) return true;
-  const T ulp = Eps<T>::ulp;
+  const T ulp = Eps<T>::ulp * (sizeof(T) == 4 ? T(KHP_HQR_DEFL_F32) : T(1));
   T tst = abs1(H[(k - 1) * ld + k - 1]) + abs1(H[k * ld + k]);
   if (tst == T(0)) {
     if (k - 2 >= 0) tst += fabs(H[(k - 1) * ld + k - 2].re);
