@@ -66,7 +66,7 @@ TC_FLOPS_PER_MATRIX = TC_PAIRS * 2 * (2 * _up128(N_MAT) * _up64(2 * N_MAT) * _up
                                       + 2 * _up128(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
 BF16_PEAK = 1935.4  # TFLOP/s, MEASURED_PEAKS.json bf16_tflops (burst)
 # DRAM bytes per matrix of the FP32 eigensolver (read + write of k_gehrd and k_geev_schur) at
-# 456 matrices per launch, from one ncu capture (profiles/geev_fp32_n242_batch456_traffic.md)
+# 456 matrices per launch, from one ncu capture of the bench's eigensolver launches
 GEEV_TRAFFIC_PER_MATRIX = (23328427776 + 9063487744 + 90695730432 + 99780031744) / 456
 
 
@@ -104,6 +104,9 @@ def parse():
     ap.add_argument("--tc-product", type=int, default=0,
                     help="only time khp_zgemm_fp64_tc (FP64-accurate tensor-core product) on this many random "
                          "242 x 242 complex problems (kernel profiling)")
+    ap.add_argument("--cpu-rate-only", type=int, default=0,
+                    help="time the CPU oracle alone on this many in-cone sweep problems and print the seconds "
+                         "(used in a child process whose BLAS threads are pinned)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -130,6 +133,26 @@ def time_oracle(problems, st, wl, kp):
         cl.source.te, cl.source.tm = 0.0, 1.0
         cl.poynting_flux_end()
     return time.perf_counter() - t0
+
+
+def cpu_sample(count):
+    """The bench's seeded sample of in-cone 11x11 sweep problems for the CPU oracle."""
+    from khepri_gb300 import workloads
+    st = workloads.batched_structure(0)
+    wl_all, kp_all = workloads.batched_problems()
+    inside = np.flatnonzero(np.hypot(kp_all[:, 0], kp_all[:, 1]) < 2 * np.pi / wl_all)
+    return np.random.default_rng(1).choice(inside, count, replace=False), st, wl_all, kp_all
+
+
+def cpu_rate_one_thread(count):
+    """Solves/s of the CPU oracle on the sample with one BLAS/OpenMP thread, timed in a child
+    process (the thread count of numpy's BLAS is fixed when it loads)."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-rate-only", str(count)], env=env,
+                       capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return None
+    return count / float(r.stdout.strip().splitlines()[-1])
 
 
 def cpu_threads():
@@ -386,11 +409,25 @@ def run_gpu(args):
     prec = args.precision
 
     def step(k):
-        return batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k], precision=prec,
-                                                 refine=args.refine)
+        """Enqueue chunk k; returns the chunk's deferred repair (its flags are read only after the
+        next chunk is enqueued, so the device never idles while the host looks at them)."""
+        out = batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k], precision=prec,
+                                                refine=args.refine, ws_slot=k % 2, defer_repair=prec == "mixed")
+        return out[2] if prec == "mixed" else (lambda: None)
 
-    for k in range(args.warmup):
-        step(k)
+    def run_steps(ks, between=None):
+        pending = None
+        for k in ks:
+            if between is not None:
+                between()
+            fix = step(k)
+            if pending is not None:
+                pending()
+            pending = fix
+        if pending is not None:
+            pending()
+
+    run_steps(range(args.warmup))
     torch.cuda.synchronize()
 
     def barrier():
@@ -398,7 +435,6 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
-    results = []
     _capi.check(lib.khp_stage_timing(1), "khp_stage_timing")
     launches0 = lib.khp_launch_count()
     repairs0 = dict(batch.STATS)
@@ -408,9 +444,7 @@ def run_gpu(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        for k in range(args.warmup, nsteps):
-            flush.zero_()
-            results.append(step(k))
+        run_steps(range(args.warmup, nsteps), between=flush.zero_)
         e1.record()
         torch.cuda.synchronize()
         barrier()
@@ -506,30 +540,32 @@ def run_gpu(args):
         torch.cuda.synchronize()
         plain_rate = args.plain / (time.perf_counter() - t0)
 
-    # end to end through the public API: host numpy inputs -> host R, T
-    e2e_steps = max(1, min(args.steps, 3))
+    # end to end through the public API: host numpy inputs -> host R, T, over exactly the chunks of
+    # the timed region (one solve_rt call; it pipelines the chunks as the timed loop does)
+    e2e_idx = np.concatenate([chunk(k) for k in range(args.warmup, nsteps)])
     torch.cuda.synchronize()
     barrier()
+    rep_e0 = dict(batch.STATS)
     t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        idx = chunk(args.warmup + k)
-        batch.solve_rt(st.pw, st.layers, st.stack, wl_all[idx], kp_all[idx], chunk=B, struct=struct,
-                       strict=False, both_pols=True, method="mixed" if prec == "mixed" else "gamma",
-                       refine=args.refine)
+    batch.solve_rt(st.pw, st.layers, st.stack, wl_all[e2e_idx], kp_all[e2e_idx], chunk=B, struct=struct,
+                   strict=False, both_pols=True, method="mixed" if prec == "mixed" else "gamma", refine=args.refine)
     torch.cuda.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
+    e2e_repairs = {k: batch.STATS[k] - rep_e0[k] for k in batch.STATS}
     h2d = B * (8 + 32 + 16 + 16)  # k0, kp, te, tm per problem
     d2h = B * (2 * 2 * 8 + 4)      # R, T for two polarisations, status
 
     cpu = None
     if rank == 0 and args.cpu_sample > 0:
-        inside = np.flatnonzero(np.hypot(kp_all[:, 0], kp_all[:, 1]) < 2 * np.pi / wl_all)
-        sample = np.random.default_rng(1).choice(inside, args.cpu_sample, replace=False)
+        sample, _, _, _ = cpu_sample(args.cpu_sample)
         t_cpu = time_oracle(sample, st, wl_all, kp_all)
+        one = cpu_rate_one_thread(args.cpu_sample)
         cpu = {"value": args.cpu_sample / t_cpu, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
                "sample": f"{args.cpu_sample} in-cone problems of the 11x11 sweep, both polarisations, CPU oracle "
-                         f"(numpy/LAPACK), {t_cpu:.1f} s"}
+                         f"(numpy/LAPACK), {t_cpu:.1f} s",
+               "one_thread": {"value": one, "unit": UNIT, "cores": 1,
+                              "sample": "the same problems, BLAS and OpenMP pinned to one thread"}}
 
     grad_info = uneven_info = twisted_info = None
     if rank == 0:
@@ -559,8 +595,9 @@ def run_gpu(args):
                        "repairs": repairs,
                        "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info},
             "roofline": roof, "cpu_baseline": cpu,
-            "e2e": {"value": world * B * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": {"value": world * len(e2e_idx) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": args.steps, "repairs": e2e_repairs,
+                    "path": "batch.solve_rt, host numpy in (pinned staging) -> host R, T, status out"},
             "gpu_launches": int(launches), "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -609,7 +646,10 @@ def run_tc_product(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.cpu_rate_only > 0:
+        sample, st, wl_all, kp_all = cpu_sample(args.cpu_rate_only)
+        print(time_oracle(sample, st, wl_all, kp_all), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.tc_product > 0:
         run_tc_product(args)

@@ -167,7 +167,9 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
  * A problem whose refinement has not converged (estimated error of its reflected or
  * transmitted amplitudes above 1e-9, e.g. an ill-conditioned system next to a Wood anomaly)
  * gets status bit 8; its R, T must then be recomputed with khp_solve_batched (the Python API
- * does this).
+ * does this).  After the eigen-refinement every mode is checked in FP64: a problem with a mode
+ * whose relative residual |M w - mu w| / (max|mu| |w|) exceeds 1e-8 gets status bit 32 and must
+ * be recomputed the same way.
  */
 size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
                                          const int32_t* layer_map);
@@ -179,6 +181,30 @@ int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlaye
                             const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
                             int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
                             size_t ws_bytes, void* stream);
+
+/*
+ * FP64 re-solve of problems that khp_solve_batched_mixed flagged with status bit 8 (its stack
+ * refinement did not converge), from that call's refined FP64 modes: the reflection-matrix
+ * recursion of khp_solve_batched in FP64, without its FP64 eigensolve.  Replaces, like
+ * khp_solve_batched, crystal.py:180-206 (layer.py:35-60, alternative.py:19-30, 181-195) and
+ * crystal.py:363-396 for the problems it is given.
+ *   The first arguments describe the problems to re-solve (batch of them: their kp, k0, te, tm,
+ *   problem_map, problem_depth) exactly as for khp_solve_batched; mixed_index: device int32
+ *   [batch], each problem's row in the earlier khp_solve_batched_mixed call of mixed_batch
+ *   problems on the same stack (same nlayers, layer_kind, layer_map), whose workspace
+ *   (mixed_workspace, mixed_ws_bytes) must be unchanged since.  Workspace:
+ *   khp_solve_batched_workspace(batch, ...).  A bit-32 problem (modes that missed their own
+ *   residual test) must go to khp_solve_batched instead.
+ */
+int khp_solve_batched_mixed_repair(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                                   const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                                   const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                                   const double* conv, const double* hx, const double* hy, const double* gx,
+                                   const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
+                                   const double* kp, const double* k0, int32_t npol, const double* te,
+                                   const double* tm, int64_t mixed_batch, const int32_t* mixed_index,
+                                   const void* mixed_workspace, size_t mixed_ws_bytes, double* R, double* T,
+                                   int32_t* status, void* workspace, size_t ws_bytes, void* stream);
 
 /*
  * Solve + gradient: khp_solve_batched_mixed and, in the same call, the gradient of
@@ -246,8 +272,11 @@ int khp_twisted_rt(int64_t batch, int32_t nbase, const double* s_left, const dou
  * inside libkhp, held by every GPU that loads the library until the process exits; batches
  * whose khp_star_product_workspace(batch, n) exceeds it return KHP_ERR_TOO_LARGE.
  * The first call on a device looks up the array's device address (with that device current),
- * so make it before any stream capture.  All calls share the one array and it keeps the last
- * call's contents: calls that overlap on the GPU (other streams, other host threads) race.
+ * so make it before any stream capture.  The address is cached for the life of the process:
+ * a cudaDeviceReset unloads the library's module and may move the array, so a process that
+ * resets a device must not call this entry point on it afterwards.  All calls share the one
+ * array and it keeps the last call's contents: calls that overlap on the GPU (other streams,
+ * other host threads) race.
  */
 #define KHP_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int khp_star_product_noalloc(int64_t batch, int32_t n, const double* SA, int64_t sa_stride, const double* SB,

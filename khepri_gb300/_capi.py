@@ -55,6 +55,12 @@ _SIGNATURES = {
                                                _c_i64, _c_p,
                                                _c_p, _c_p, _c_p, _c_p, _c_d, _c_d, _c_d, _c_d, _c_p, _c_p, _c_i32,
                                                _c_p, _c_p, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
+    # khp_solve_batched's arguments up to tm, then mixed_batch, mixed_index, mixed_workspace, mixed_ws_bytes,
+    # R, T, status, ws, ws_bytes, stream
+    "khp_solve_batched_mixed_repair": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p,
+                                                      _c_p, _c_i64, _c_p, _c_p, _c_p, _c_p, _c_p, _c_d, _c_d, _c_d,
+                                                      _c_d, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_i64, _c_p, _c_p,
+                                                      _c_sz, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_solve_batched_mixed_grad_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_p, _c_p, _c_i64]),
     # batch, px, py, nlayers, kind, map, eps, depth, pmap, pdepth, nmaps, conv, ic, hx, hy, gx, gy, epsi (2),
     # epse (2), kp, k0, npol, te, tm, refine, dR, dT, R, T, R_orders, T_orders, dconv, status, ws, ws_bytes, stream
@@ -153,7 +159,8 @@ def require_cuda():
 
 
 STATUS_BITS = {1: "singular pivot", 2: "eigensolver not converged", 4: "non-finite value",
-               8: "mixed-precision refinement not converged", 16: "per-problem input out of range"}
+               8: "mixed-precision refinement not converged", 16: "per-problem input out of range",
+               32: "mixed-precision eigen-refinement not converged"}
 
 
 def decode_status(word: int) -> str:

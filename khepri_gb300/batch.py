@@ -9,6 +9,7 @@ that share a pixmap share one eigensolve per problem.
 from __future__ import annotations
 
 import ctypes
+import functools
 
 import numpy as np
 import torch
@@ -110,14 +111,17 @@ def _host(a):
 
 
 def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, tm=None, precision="fp64",
-                      refine=2, pmap=None, pdepth=None, repair=True):
+                      refine=2, pmap=None, pdepth=None, repair=True, ws_slot=0, defer_repair=False):
     """R, T of one chunk by the reflection-matrix recursion (khp_solve_batched).
 
     te, tm: optional [B, npol] complex device tensors (default: prob.te, prob.tm as one
     polarisation); the recursion runs once and every polarisation is read from it.
     pmap, pdepth: optional device tensors [L, B] (int32 map index into plan's maps, float64
     depth) giving every problem its own maps and depths.
-    repair: re-solve problems whose mixed refinement did not converge (status bit 8).
+    repair: re-solve the problems the mixed path flagged (status bits 8 and 32, see
+    _repair_unconverged).  ws_slot: workspace slot of the call (engine.workspace).
+    defer_repair: return (R, T, repair_fn) instead, where repair_fn() checks the flags and
+    re-solves later (it reads this call's workspace, so the slot must not be reused before).
     Returns R, T of shape [B] (one polarisation) or [B, npol].
     """
     B = prob.batch
@@ -144,64 +148,107 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
               _capi.ptr(plan.hx), _capi.ptr(plan.hy),
               _capi.ptr(struct.gx), _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
               _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm))
+    fix = None
     if precision == "mixed":
         ws = engine.workspace(lib.khp_solve_batched_mixed_workspace(B, struct.nh, L, _host(plan.kinds),
-                                                                     _host(plan.maps)), dev)
+                                                                     _host(plan.maps)), dev, ws_slot)
         with engine._stage("khp_solve_batched_mixed"):
             code = lib.khp_solve_batched_mixed(*common, int(refine), _capi.ptr(R), _capi.ptr(T), _capi.ptr(status),
                                                _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
         _capi.check(code, "khp_solve_batched_mixed")
-        if repair:
-            _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap, pdepth)
+        if repair or defer_repair:
+            fix = functools.partial(_repair_unconverged, struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap,
+                                    pdepth, ws)
+            if not defer_repair:
+                fix()
+                fix = None
     else:
         ws = engine.workspace(lib.khp_solve_batched_workspace(B, struct.nh, L, _host(plan.kinds), _host(plan.maps)),
-                              dev)
+                              dev, ws_slot)
         with engine._stage("khp_solve_batched"):
             code = lib.khp_solve_batched(*common, _capi.ptr(R), _capi.ptr(T), _capi.ptr(status), _capi.ptr(ws),
                                          ws.numel(), _capi.stream_ptr())
         _capi.check(code, "khp_solve_batched")
     if one_pol:
-        return R[:, 0], T[:, 0]
+        R, T = R[:, 0], T[:, 0]
+    if defer_repair:
+        return R, T, (fix if fix is not None else (lambda: None))
     return R, T
 
 
 REFINE_BIT = 8
-# problems re-solved after a non-converged mixed refinement: with longer refinement (mixed) and,
-# if that still does not converge, in FP64
+MODES_BIT = 32
+# Problems re-solved after the mixed path flagged them: "refine_repairs" (status bit 8, the stack
+# refinement did not converge) are re-solved in FP64 from the mixed path's refined modes;
+# "fp64_repairs" (status bit 32, a refined mode missed its residual test) by the full FP64 path.
 STATS = {"refine_repairs": 0, "fp64_repairs": 0}
-REPAIR_REFINE = 8  # refinement rounds of the repair solve (plus the adaptive extra rounds)
+REPAIR_WS_SLOT = 7  # workspace slot of the re-solves (the flagged call's own slot must stay intact)
 
 
-def _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap=None, pdepth=None):
-    """Re-solve the problems whose mixed-precision refinement did not converge (status bit 8: an
-    ill-conditioned stack, e.g. next to a Wood anomaly, where the FP32 factors make the
-    refinement converge at ~0.3 per round): first by the mixed path with REPAIR_REFINE rounds,
-    then in FP64 (khp_solve_batched) for any still unconverged; R, T and status in place."""
-    flagged = (status & REFINE_BIT) != 0
+def _sub_args(pmap, pdepth, te, tm, idx):
+    pm = None if pmap is None else pmap[:, idx].contiguous()
+    pd = None if pdepth is None else pdepth[:, idx].contiguous()
+    return pm, pd, te[idx].contiguous(), tm[idx].contiguous()
+
+
+def resolve_fp64(struct, plan, prob, sel, te, tm, epsi=1.0, epse=1.0, pmap=None, pdepth=None, mixed_ws=None):
+    """R, T [K, npol] and status [K] of the problems at device indices ``sel`` of a chunk, by the
+    FP64 reflection-matrix recursion.  With ``mixed_ws`` (the workspace of the chunk's
+    khp_solve_batched_mixed call, unchanged since) the recursion starts from that call's refined
+    FP64 modes (khp_solve_batched_mixed_repair); without, it runs its own FP64 eigensolve
+    (khp_solve_batched).  te, tm: the chunk's [B, npol] source weights."""
+    lib = _capi.load()
+    dev = struct.device
+    epsi, epse = complex(epsi), complex(epse)
+    K, L, npol = int(sel.numel()), len(plan.kinds), te.shape[1]
+    sub = prob.subset(sel)
+    pm, pd, te_s, tm_s = _sub_args(pmap, pdepth, te, tm, sel)
+    st = torch.zeros(K, dtype=torch.int32, device=dev)
+    r = torch.empty((K, npol), dtype=torch.float64, device=dev)
+    t = torch.empty_like(r)
+    common = (K, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
+              _host(plan.depth), _capi.ptr(pm), _capi.ptr(pd), plan.nmaps, _capi.ptr(plan.conv),
+              _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
+              epsi.real, epsi.imag, epse.real, epse.imag, _capi.ptr(sub.kp), _capi.ptr(sub.k0), npol,
+              _capi.ptr(te_s), _capi.ptr(tm_s))
+    ws = engine.workspace(lib.khp_solve_batched_workspace(K, struct.nh, L, _host(plan.kinds), _host(plan.maps)),
+                          dev, REPAIR_WS_SLOT)
+    if mixed_ws is None:
+        code = lib.khp_solve_batched(*common, _capi.ptr(r), _capi.ptr(t), _capi.ptr(st), _capi.ptr(ws), ws.numel(),
+                                     _capi.stream_ptr())
+        _capi.check(code, "khp_solve_batched")
+    else:
+        rows = sel.to(torch.int32).contiguous()
+        code = lib.khp_solve_batched_mixed_repair(*common, prob.batch, _capi.ptr(rows), _capi.ptr(mixed_ws),
+                                                  mixed_ws.numel(), _capi.ptr(r), _capi.ptr(t), _capi.ptr(st),
+                                                  _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+        _capi.check(code, "khp_solve_batched_mixed_repair")
+    return r, t, st
+
+
+def _repair_unconverged(struct, plan, prob, status, epsi, epse, te, tm, R, T, pmap, pdepth, mixed_ws):
+    """Re-solve the problems a mixed-precision call flagged; R, T and status in place.
+
+    Status bit 8 (the stack refinement did not converge: an ill-conditioned stack, e.g. next to a
+    Wood anomaly, where the FP32 factors make the refinement converge too slowly): the FP64
+    reflection-matrix recursion from that call's refined FP64 modes, read from its workspace
+    (no second eigensolve).  Status bit 32 (a refined mode missed its FP64 residual test): the
+    full FP64 path with its own FP64 eigensolve."""
+    flagged = (status & (REFINE_BIT | MODES_BIT)) != 0
     if not bool(flagged.any()):
         return
     idx = torch.nonzero(flagged).flatten()
-    STATS["refine_repairs"] += int(idx.numel())
-    sub = prob.subset(idx)
-    st = torch.zeros(idx.numel(), dtype=torch.int32, device=status.device)
-    pm = None if pmap is None else pmap[:, idx]
-    pd = None if pdepth is None else pdepth[:, idx]
-    r, t = solve_chunk_gamma(struct, plan, sub, st, epsi, epse, te[idx].contiguous(), tm[idx].contiguous(),
-                             precision="mixed", refine=REPAIR_REFINE, pmap=pm, pdepth=pd, repair=False)
-    still = (st & REFINE_BIT) != 0
-    if bool(still.any()):
-        j = torch.nonzero(still).flatten()
-        STATS["fp64_repairs"] += int(j.numel())
-        st64 = torch.zeros(j.numel(), dtype=torch.int32, device=status.device)
-        r64, t64 = solve_chunk_gamma(struct, plan, sub.subset(j), st64, epsi, epse, te[idx][j].contiguous(),
-                                     tm[idx][j].contiguous(), precision="fp64",
-                                     pmap=None if pm is None else pm[:, j], pdepth=None if pd is None else pd[:, j])
-        r[j] = r64
-        t[j] = t64
-        st[j] = st64
-    R[idx] = r
-    T[idx] = t
-    status[idx] = (status[idx] & ~REFINE_BIT) | st
+    modes_bad = (status[idx] & MODES_BIT) != 0
+    for sel, full in ((idx[~modes_bad], False), (idx[modes_bad], True)):
+        K = int(sel.numel())
+        if K == 0:
+            continue
+        STATS["fp64_repairs" if full else "refine_repairs"] += K
+        r, t, st = resolve_fp64(struct, plan, prob, sel, te, tm, epsi, epse, pmap, pdepth,
+                                None if full else mixed_ws)
+        R[sel] = r
+        T[sel] = t
+        status[sel] = (status[sel] & ~(REFINE_BIT | MODES_BIT)) | st
 
 
 def both_pol_weights(B, device):
@@ -213,10 +260,15 @@ def both_pol_weights(B, device):
     return te, tm
 
 
-def solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi=1.0, epse=1.0, precision="fp64", refine=2):
-    """R, T [B, 2] for (te, tm) = (1, 0) and (0, 1) from one recursion per problem."""
+def solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi=1.0, epse=1.0, precision="fp64", refine=2, **kw):
+    """R, T [B, 2] for (te, tm) = (1, 0) and (0, 1) from one recursion per problem (keyword
+    arguments as solve_chunk_gamma: repair, ws_slot, defer_repair)."""
     te, tm = both_pol_weights(prob.batch, struct.device)
-    return solve_chunk_gamma(struct, plan, prob, status, epsi, epse, te, tm, precision, refine)
+    return solve_chunk_gamma(struct, plan, prob, status, epsi, epse, te, tm, precision, refine, **kw)
+
+
+def _no_repair():
+    return None
 
 
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
@@ -252,27 +304,46 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     ro = np.empty((P, struct.nh)) if orders else None
     to = np.empty((P, struct.nh)) if orders else None
     st = np.zeros(P, dtype=np.int32)
-    for s in range(0, P, chunk):
-        e = min(P, s + chunk)
-        prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
-        status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
-        if method in ("gamma", "mixed"):
-            r_o = t_o = None
-            if both_pols:
-                r, t = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine)
-            else:
-                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine)
-        elif both_pols:
-            r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
-            r_o = t_o = None
-        else:
-            r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
+
+    def finish(job):
+        # the chunk's deferred re-solve of flagged problems, then its results to the host
+        s, e, r, t, r_o, t_o, status, fix = job
+        fix()
         R[s:e] = r.cpu().numpy()
         T[s:e] = t.cpu().numpy()
         if orders:
             ro[s:e] = r_o.cpu().numpy()
             to[s:e] = t_o.cpu().numpy()
         st[s:e] = status.cpu().numpy()
+
+    # Chunk c is finished (flags read, flagged problems re-solved, results copied back) only after
+    # chunk c + 1 is enqueued, so the device never waits for the host's look at the flags; the two
+    # chunks in flight use alternate workspace slots.
+    pending = None
+    for c, s in enumerate(range(0, P, chunk)):
+        e = min(P, s + chunk)
+        prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
+        status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
+        r_o = t_o = None
+        fix = _no_repair
+        if method in ("gamma", "mixed"):
+            kw = dict(ws_slot=c % 2, defer_repair=prec == "mixed")
+            if both_pols:
+                out = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine, **kw)
+            else:
+                out = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine, **kw)
+            r, t = out[0], out[1]
+            if prec == "mixed":
+                fix = out[2]
+        elif both_pols:
+            r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
+        else:
+            r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
+        if pending is not None:
+            finish(pending)
+        pending = (s, e, r, t, r_o, t_o, status, fix)
+    if pending is not None:
+        finish(pending)
     if strict and st.any():
         bad = int(np.flatnonzero(st)[0])
         raise _capi.KhpError(f"problem {bad}: {_capi.decode_status(int(st[bad]))}")

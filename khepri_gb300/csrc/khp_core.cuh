@@ -51,6 +51,7 @@ enum StatusBit : int {
   KHP_BIT_NONFINITE = 4,
   KHP_BIT_REFINE = 8,      // mixed-precision iterative refinement did not converge: re-solve in FP64
   KHP_BIT_BAD_INPUT = 16,  // a per-problem input outside its range (e.g. a map index)
+  KHP_BIT_MODES = 32,      // mixed-precision eigen-refinement left a residual above 1e-8: re-solve in FP64
 };
 
 // ---- complex scalar with the memory layout of numpy/torch complex64 / complex128 ----------

@@ -138,12 +138,40 @@ int launch_getrs_right(int64_t batch, int n, const cplx<T>* A, int64_t lda, int6
     GT_TRY(cuda_status());                                               \
   } while (0)
 
+// Modes computed elsewhere (the refined FP64 modes of a mixed-precision solve): slot m of
+// problem b is row idx[b] of [slots][src_batch] arrays W, V ([n][n]) and lam ([n]).
+struct GivenModes {
+  const cd* W;
+  const cd* V;
+  const cd* lam;
+  int64_t src_batch;
+  const int* idx;
+};
+
+// Wd, Vd, lamd of every problem from slot `slot` of the given modes; an index outside
+// [0, src_batch) sets KHP_BIT_BAD_INPUT and leaves zeros (then a singular W is reported too).
+__global__ void k_gather_modes(int64_t batch, int n, GivenModes g, int slot, cd* Wd, cd* Vd, cd* lamd, int* status) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn, r = e - b * nn;
+    const int src = g.idx[b];
+    const bool ok = src >= 0 && src < g.src_batch;
+    const int64_t row = ok ? (int64_t)slot * g.src_batch + src : 0;
+    Wd[e] = ok ? g.W[row * nn + r] : mk(0.0);
+    Vd[e] = ok ? g.V[row * nn + r] : mk(0.0);
+    if (r < n) lamd[b * n + r] = ok ? g.lam[row * n + r] : mk(0.0);
+    if (!ok && r == 0) atomicOr(status + b, KHP_BIT_BAD_INPUT);
+  }
+}
+
 template <typename T>
 int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, const int* maps, const double* eps,
                 const double* depths, const int* pmap, const double* pdepth, int64_t nmaps, const double* conv,
                 const double* hx, const double* hy, const double* gx, const double* gy, cd epsi, cd epse,
                 const double* kp, const double* k0, int npol, const double* te, const double* tm, double* R,
-                double* Tt, int* status, void* workspace, size_t ws_bytes, cudaStream_t s) {
+                double* Tt, int* status, void* workspace, size_t ws_bytes, cudaStream_t s,
+                const GivenModes* given = nullptr) {
   static_assert(sizeof(T) == sizeof(double), "the FP64 recursion reads the caller's FP64 maps directly");
   const int nh = px * py, n = 2 * nh;
   const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh, hn = (int64_t)nh * n;
@@ -174,15 +202,20 @@ int solve_gamma(int64_t batch, int px, int py, int nlayers, const int* kinds, co
     const cd* Cm = reinterpret_cast<const cd*>(conv);
     GT_EW(k_select_maps, batch, batch, pmap ? pmap + (int64_t)first[m] * batch : nullptr, used[m], nmaps, p.midx[m],
           status);
-    GT_TRY(launch_assemble_pq<T>(batch, nh, Cm, reinterpret_cast<const cd*>(hx), reinterpret_cast<const cd*>(hy),
-                                 p.midx[m], gx, gy, kp, k0, p.M, s));
-    GT_TRY(launch_geev<T>(batch, n, p.M, n, nn, p.Z, p.W[m], n, nn, p.lam[m], n, status, s));
-    GT_EW(k_sqrt_lam_t<T>, batch * n, batch * n, p.lam[m]);
-    cplx<T>* CWt = p.CW;
-    cplx<T>* CWb = p.CW + batch * hn;
-    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m], n, nn, zero, CWt, n, hn, s, p.midx[m]));
-    GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m] + hn, n, nn, zero, CWb, n, hn, s, p.midx[m]));
-    GT_TRY(launch_modes_v<T>(batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, hn, p.lam[m], p.V[m], status, s));
+    if (given) {
+      GT_EW(k_gather_modes, batch * nn, batch, n, *given, (int)m, p.W[m], p.V[m], p.lam[m], status);
+    } else {
+      GT_TRY(launch_assemble_pq<T>(batch, nh, Cm, reinterpret_cast<const cd*>(hx), reinterpret_cast<const cd*>(hy),
+                                   p.midx[m], gx, gy, kp, k0, p.M, s));
+      GT_TRY(launch_geev<T>(batch, n, p.M, n, nn, p.Z, p.W[m], n, nn, p.lam[m], n, status, s));
+      GT_EW(k_sqrt_lam_t<T>, batch * n, batch * n, p.lam[m]);
+      cplx<T>* CWt = p.CW;
+      cplx<T>* CWb = p.CW + batch * hn;
+      GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m], n, nn, zero, CWt, n, hn, s, p.midx[m]));
+      GT_TRY(launch_gemm<T>(batch, nh, n, nh, one, Cm, nh, hh, p.W[m] + hn, n, nn, zero, CWb, n, hn, s,
+                            p.midx[m]));
+      GT_TRY(launch_modes_v<T>(batch, nh, gx, gy, kp, k0, p.W[m], CWt, CWb, hn, p.lam[m], p.V[m], status, s));
+    }
     GT_TRY(launch_copy<T>(batch, n, n, p.W[m], n, nn, p.lu, n, nn, s));
     GT_TRY(launch_inverse<T>(batch, n, p.lu, n, nn, p.Wi[m], n, nn, p.piv, status, s));
     GT_TRY(launch_copy<T>(batch, n, n, p.V[m], n, nn, p.lu, n, nn, s));
@@ -299,6 +332,35 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
                              problem_depth, nmaps, conv, hx, hy, gx, gy, mk(epsi_re, epsi_im), mk(epse_re, epse_im),
                              kp, k0, npol, te, tm, R, T, status, workspace, ws_bytes,
                              reinterpret_cast<cudaStream_t>(stream));
+}
+
+int khp_solve_batched_mixed_repair(int64_t batch, int32_t px, int32_t py, int32_t nlayers, const int32_t* layer_kind,
+                                   const int32_t* layer_map, const double* layer_eps, const double* layer_depth,
+                                   const int32_t* problem_map, const double* problem_depth, int64_t nmaps,
+                                   const double* conv, const double* hx, const double* hy, const double* gx,
+                                   const double* gy, double epsi_re, double epsi_im, double epse_re, double epse_im,
+                                   const double* kp, const double* k0, int32_t npol, const double* te,
+                                   const double* tm, int64_t mixed_batch, const int32_t* mixed_index,
+                                   const void* mixed_workspace, size_t mixed_ws_bytes, double* R, double* T,
+                                   int32_t* status, void* workspace, size_t ws_bytes, void* stream) {
+  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || !gx || !gy || !kp || !k0 || !te || !tm || !R || !T ||
+      !status || mixed_batch < 0 || (batch > 0 && (!mixed_index || !mixed_workspace)))
+    return KHP_ERR_INVALID_ARG;
+  if (nlayers > 0 && (!layer_kind || !layer_map || !layer_eps || !layer_depth)) return KHP_ERR_INVALID_ARG;
+  for (int l = 0; l < nlayers; ++l) {
+    if (layer_kind[l] != 0 && layer_kind[l] != 1) return KHP_ERR_INVALID_ARG;
+    if (layer_kind[l] == 1 && (layer_map[l] < 0 || layer_map[l] >= nmaps || !conv || !hx || !hy))
+      return KHP_ERR_INVALID_ARG;
+  }
+  if (batch == 0) return KHP_OK;
+  GivenModes g{nullptr, nullptr, nullptr, mixed_batch, mixed_index};
+  const int st = mixed_modes_in_workspace(mixed_batch, px * py, nlayers, layer_kind, layer_map, mixed_workspace,
+                                          mixed_ws_bytes, &g.W, &g.V, &g.lam);
+  if (st) return st;
+  return solve_gamma<double>(batch, px, py, nlayers, layer_kind, layer_map, layer_eps, layer_depth, problem_map,
+                             problem_depth, nmaps, conv, hx, hy, gx, gy, mk(epsi_re, epsi_im), mk(epse_re, epse_im),
+                             kp, k0, npol, te, tm, R, T, status, workspace, ws_bytes,
+                             reinterpret_cast<cudaStream_t>(stream), g.W ? &g : nullptr);
 }
 
 }  // extern "C"

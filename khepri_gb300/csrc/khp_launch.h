@@ -96,6 +96,13 @@ int tc_product(int64_t batch, int m, int n, int k, const cplx<TI>* A, int64_t ld
                const cplx<TI>* B, int64_t ldb, int64_t bsB, const int* bidx, cplx<TO> alpha, cplx<TO> beta,
                cplx<TO>* C, int64_t ldc, int64_t bsC, const OzakiWs& w, cudaStream_t s);
 
+// The refined FP64 modes a khp_solve_batched_mixed call left in its workspace (same batch and
+// stack description as that call): W, V [slots][batch][n][n] and lam [slots][batch][n], one
+// slot per distinct map in order of first use (all null when the stack has no patterned layer).
+int mixed_modes_in_workspace(int64_t batch, int nh, int L, const int* kinds, const int* maps, const void* ws,
+                             size_t ws_bytes, const cplx<double>** W, const cplx<double>** V,
+                             const cplx<double>** lam);
+
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 
 // Adds k to the process-wide launch counter reported by khp_launch_count().

@@ -5,11 +5,12 @@
 // of a few 1e-6 on the 11x11 sweep).  This pipeline:
 //   1. modes: FP32 eigensolve of M = P Q, then three FP64 refinement steps of the eigenpairs:
 //      E = W^-1 (M W - W mu) with the residual formed in FP64 and the solve in FP32,
-//      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i); mutually nearest eigenvalues
-//      closer than 3e-3 max|mu| take the exact 2x2 update of their block of E instead (first
-//      order converges slowly there); other pairs closer than 1e-5 relative stay coupled
-//      (second-order error);  V = Q W / lam in FP64.  The FP64 products M W and C W run on the
-//      bf16 tensor cores with exact digit splitting (ozaki_zgemm), FP64-accurate;
+//      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i); clusters of eigenvalues closer
+//      than 3e-3 max|mu| take the exact eigen-decomposition of their block of diag(mu) + E
+//      instead (cyclic 2x2 Jacobi sweeps), composed with the first-order correction of their
+//      columns; an FP64 residual test of every mode follows (status bit 32 where it fails);
+//      V = Q W / lam in FP64.  The FP64 products M W and C W run on the bf16 tensor cores with
+//      exact digit splitting (ozaki_zgemm), FP64-accurate;
 //   2. the reflection-matrix recursion of khp_solve_batched on the FP32-rounded refined modes,
 //      keeping every factor it makes (the explicit inverses, rho, Gamma at every gap, Gamma M^-1),
 //      with every O(n^3) step a blocked LU / inverse or a tiled product;
@@ -37,7 +38,8 @@ using cf = cplx<float>;
 
 constexpr int kMaxLayers = 16;
 // Eigen-refinement steps.  From this FP32 solver's eigenvectors (relative residual ~1e-6 on the
-// 11x11 P.Q) three pair-aware steps reach ~1e-10 even for eigenvalue pairs 1e-4 apart.
+// 11x11 P.Q) three cluster-aware steps with M W formed in FP64 at every step reach ~1e-15, also
+// for exactly degenerate pairs and for clusters of close eigenvalues.
 constexpr int kEigSteps = 3;
 // Refinement rounds beyond the requested ones, run only for problems not yet converged.
 constexpr int kExtraRounds = 12;
@@ -59,103 +61,239 @@ __global__ void k_eig_residual(int64_t boff, int n, const cd* __restrict__ MW, c
   }
 }
 
-// Close eigenvalue pairs: pair[i] = j when i and j are each other's nearest eigenvalue and closer
-// than 3e-3 max|mu|, else -1.  One CTA per problem.
-__global__ void __launch_bounds__(256) k_find_pairs(int n, const cd* __restrict__ mu, int* pair, int* nearest) {
-  __shared__ TeamShared sh;
-  TeamCta t;
-  const int64_t b = blockIdx.x;
-  const cd* m = mu + b * n;
-  int* pr = pair + b * n;
-  int* nr = nearest + b * n;
-  double big = 0.0;
-  int bi = 0;
-  for (int i = t.tid(); i < n; i += t.size()) {
-    const double a = cabs(m[i]);
-    if (a > big) { big = a; bi = i; }
-    // nearest by squared distance (the same minimum, without a square root per pair)
-    double best = 1e300;
-    int bj = -1;
-    const cd mi = m[i];
-    for (int j = 0; j < n; ++j) {
-      if (j == i) continue;
-      const double dr = m[j].re - mi.re, di = m[j].im - mi.im;
-      const double d2 = dr * dr + di * di;
-      if (d2 < best) { best = d2; bj = j; }
-    }
-    nr[i] = bj;
-  }
-  team_argmax(t, big, bi, &sh);  // big = max |mu| for every thread
-  t.sync();
-  for (int i = t.tid(); i < n; i += t.size()) {
-    const int j = nr[i];
-    pr[i] = (j >= 0 && nr[j] == i && cabs(m[j] - m[i]) < 3e-3 * big) ? j : -1;
-  }
-}
-
-// The 2x2 eigen-decomposition of K = [[a, b], [c, d]] (a, d: the pair's updated diagonal),
-// with eigenvectors scaled to unit diagonal: returns den with v12 = -b/den, v21 = c/den,
-// new eigenvalues a + bc/den and d - bc/den (the root near a first).
+// The 2x2 eigen-decomposition of K = [[a, b], [c, d]] with eigenvectors scaled to unit
+// diagonal: returns den with v12 = -b/den, v21 = c/den, new eigenvalues a + bc/den and
+// d - bc/den (the root near a first).
 __device__ __forceinline__ cd pair_den(cd a, cd b, cd c, cd d) {
   const cd h = 0.5 * (a - d);
   const cd sq = csqrt(h * h + b * c);
   return (h.re * sq.re + h.im * sq.im >= 0.0) ? h + sq : h - sq;
 }
 
-// mu_out = mu_in + diag(E) and F_ij = E_ij / (mu_j - mu_i), except for close pairs, which take
-// the exact 2x2 update; other pairs closer than 1e-5 relative stay coupled (F = 0).
-// (one grid row per problem, b = boff + blockIdx.y, launched by MX_PP)
-__global__ void k_eig_update(int64_t boff, int n, const cd* __restrict__ mu_in, const cf* __restrict__ E, cf* F,
-                             cd* mu_out, const int* __restrict__ pair) {
-  const int64_t nn = (int64_t)n * n;
-  const int64_t b = boff + blockIdx.y;
-  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
-    const int64_t e = b * nn + rc;
-    const int i = rc / n, j = rc - i * n;
-    const cf* Eb = E + b * nn;
-    const int pi = pair[b * n + i];
-    cd out = mk(0.0);
-    if (pi >= 0 && (i == j || pi == j)) {
-      const int p = i < pi ? i : pi, q = i < pi ? pi : i;  // the pair, p < q
-      const cf epp = Eb[(int64_t)p * n + p], eqq = Eb[(int64_t)q * n + q];
-      const cf epq = Eb[(int64_t)p * n + q], eqp = Eb[(int64_t)q * n + p];
-      const cd a = mu_in[b * n + p] + mk((double)epp.re, (double)epp.im);
-      const cd d = mu_in[b * n + q] + mk((double)eqq.re, (double)eqq.im);
-      const cd bq = mk((double)epq.re, (double)epq.im), cq = mk((double)eqp.re, (double)eqp.im);
-      const cd den = pair_den(a, bq, cq, d);
-      const bool ok = !(den.re == 0.0 && den.im == 0.0);
-      if (i == j) {
-        mu_out[b * n + i] = ok ? (i == p ? a + cdiv(bq * cq, den) : d - cdiv(bq * cq, den)) : (i == p ? a : d);
-      } else if (ok) {
-        out = i == p ? -cdiv(bq, den) : cdiv(cq, den);
-      }
-    } else {
-      const cf ev = Eb[(int64_t)i * n + j];
-      const cd mi = mu_in[b * n + i];
-      if (i == j) {
-        mu_out[b * n + i] = mi + mk((double)ev.re, (double)ev.im);
-      } else {
-        // the difference in FP64 (no cancellation for close pairs), the quotient in FP32
-        const cd mj = mu_in[b * n + j];
-        const cd dd = mj - mi;
-        const cf d32 = mk((float)dd.re, (float)dd.im);
-        const float ad = cabs(d32);
-        const float am = cabs(mk((float)mi.re, (float)mi.im)) + cabs(mk((float)mj.re, (float)mj.im));
-        if (ad > 1e-5f * am) {
-          const cf q = cdiv(ev, d32);
-          F[e] = q;
-          continue;
+// Eigenvalue clusters of the refinement: the connected components of the graph joining
+// eigenvalues closer than kClusterTol max|mu|.  Inside a cluster a first-order step converges
+// slowly or not at all (its correction E_ij / (mu_j - mu_i) is not small), so every cluster of
+// 2..kClusterMax members takes the exact eigen-decomposition of its block of diag(mu) + E instead.
+constexpr double kClusterTol = 3e-3;
+constexpr int kClusterMax = 12;
+// Cluster members whose 2x2 sub-block does not resolve two directions (|den| below this times
+// max|mu|) are degenerate to within the refinement's noise (e.g. the two modes of a
+// two-dimensional representation of a symmetric pixmap at normal incidence): any basis of an
+// exactly degenerate subspace is an eigenbasis, and a rotation computed from noise is O(1).
+constexpr double kDegenerateTol = 1e-9;
+
+// Cyclic 2x2 Jacobi sweeps for a non-normal k x k matrix K close to diagonal: each step is the
+// similarity S^-1 K S with S = [[1, v12], [v21, 1]] on rows and columns (a, b), the 2x2 block's
+// eigenvectors scaled to unit diagonal, which zeroes K_ab and K_ba; X accumulates the S.  Pairs
+// degenerate within the noise, or whose S is nearly singular, are left alone.  At most 16 sweeps,
+// stopping once every off-diagonal entry is below 1e-15 max|mu|.
+__device__ void cluster_jacobi(int k, cd* K, cd* X, double big) {
+  for (int i = 0; i < k * k; ++i) X[i] = mk(0.0);
+  for (int i = 0; i < k; ++i) X[i * k + i] = mk(1.0);
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    double off = 0.0;
+    for (int a = 0; a < k; ++a) {
+      for (int b = a + 1; b < k; ++b) {
+        const cd kab = K[a * k + b], kba = K[b * k + a];
+        off = fmax(off, fmax(cabs(kab), cabs(kba)));
+        const cd den = pair_den(K[a * k + a], kab, kba, K[b * k + b]);
+        if (!(cabs(den) > kDegenerateTol * big)) continue;
+        const cd v12 = cdiv(mk(-kab.re, -kab.im), den), v21 = cdiv(kba, den);
+        const cd det = mk(1.0) - v12 * v21;
+        if (!(cabs(det) > 1e-3)) continue;
+        const cd idet = cdiv(mk(1.0), det);
+        // columns a, b of K and X: [ca, cb] <- [ca + v21 cb, cb + v12 ca]
+        for (int r = 0; r < k; ++r) {
+          const cd ca = K[r * k + a], cb = K[r * k + b];
+          K[r * k + a] = ca + v21 * cb;
+          K[r * k + b] = cb + v12 * ca;
+          const cd xa = X[r * k + a], xb = X[r * k + b];
+          X[r * k + a] = xa + v21 * xb;
+          X[r * k + b] = xb + v12 * xa;
+        }
+        // rows a, b of K: [ra; rb] <- (1 / det) [ra - v12 rb; rb - v21 ra]
+        for (int c = 0; c < k; ++c) {
+          const cd ra = K[a * k + c], rb = K[b * k + c];
+          K[a * k + c] = idet * (ra - v12 * rb);
+          K[b * k + c] = idet * (rb - v21 * ra);
         }
       }
     }
-    F[e] = mk((float)out.re, (float)out.im);
+    if (off < 1e-15 * big) break;
   }
 }
 
-// A64 += D32
-__global__ void k_accumulate(int64_t count, cd* A64, const cf* __restrict__ D) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
-    A64[e] += mk((double)D[e].re, (double)D[e].im);
+// Clusters of one refinement step (one CTA per problem).  Writes, per column j: lab[j] (the
+// smallest index of its cluster), pos[j] (its rank among the members), csz[j] (the cluster size,
+// 1 for a singleton), the updated eigenvalue mu_out[j], and for members of clusters of size
+// 2..kClusterMax the members (memb[j][p]) and column pos[j] of the cluster's transform
+// (xc[j][p] = X[p][pos[j]]).  Columns of larger clusters are treated as singletons.
+__global__ void __launch_bounds__(256) k_clusters(int n, const cd* __restrict__ mu, const cf* __restrict__ E,
+                                                  int* lab, int* pos, int* csz, int* memb, cf* xc, cd* mu_out) {
+  __shared__ TeamShared sh;
+  __shared__ int changed;
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  const int64_t nn = (int64_t)n * n;
+  const cd* m = mu + b * n;
+  const cf* Eb = E + b * nn;
+  int* lb = lab + b * n;
+  double big = 0.0;
+  int bi = 0;
+  for (int i = t.tid(); i < n; i += t.size()) {
+    big = fmax(big, cabs(m[i]));
+    lb[i] = i;
+  }
+  team_argmax(t, big, bi, &sh);
+  const double tol2 = (kClusterTol * big) * (kClusterTol * big);
+  // connected components by repeated minimum-label propagation (bounded; a component whose labels
+  // have not settled is only split, and each part is still handled consistently)
+  for (int it = 0; it < 64; ++it) {
+    if (t.tid() == 0) changed = 0;
+    t.sync();
+    for (int i = t.tid(); i < n; i += t.size()) {
+      const cd mi = m[i];
+      int best = lb[i];
+      for (int j = 0; j < n; ++j) {
+        const double dr = m[j].re - mi.re, di = m[j].im - mi.im;
+        if (dr * dr + di * di < tol2) best = min(best, lb[j]);
+      }
+      if (best < lb[i]) {
+        lb[i] = best;
+        changed = 1;
+      }
+    }
+    t.sync();
+    if (!changed) break;
+    t.sync();
+  }
+  // ranks and sizes (deterministic: by index)
+  for (int i = t.tid(); i < n; i += t.size()) {
+    const int l = lb[i];
+    int r = 0, c = 0;
+    for (int j = 0; j < n; ++j) {
+      if (lb[j] != l) continue;
+      r += j < i;
+      ++c;
+    }
+    pos[b * n + i] = r;
+    csz[b * n + i] = c;
+    const cf e = Eb[(int64_t)i * n + i];
+    mu_out[b * n + i] = m[i] + mk((double)e.re, (double)e.im);
+  }
+  t.sync();
+  // one thread per cluster of 2..kClusterMax members
+  for (int r = t.tid(); r < n; r += t.size()) {
+    if (lb[r] != r) continue;
+    const int k = csz[b * n + r];
+    if (k < 2 || k > kClusterMax) continue;
+    int mem[kClusterMax];
+    cd K[kClusterMax * kClusterMax], X[kClusterMax * kClusterMax];
+    int c = 0;
+    for (int j = r; j < n && c < k; ++j)
+      if (lb[j] == r) mem[c++] = j;
+    for (int p = 0; p < k; ++p)
+      for (int q = 0; q < k; ++q) {
+        const cf e = Eb[(int64_t)mem[p] * n + mem[q]];
+        K[p * k + q] = mk((double)e.re, (double)e.im) + (p == q ? m[mem[p]] : mk(0.0));
+      }
+    cluster_jacobi(k, K, X, big);
+    for (int q = 0; q < k; ++q) {
+      const int j = mem[q];
+      mu_out[b * n + j] = K[q * k + q];
+      for (int p = 0; p < k; ++p) {
+        memb[(b * n + j) * kClusterMax + p] = mem[p];
+        xc[(b * n + j) * kClusterMax + p] = mk((float)X[p * k + q].re, (float)X[p * k + q].im);
+      }
+    }
+  }
+}
+
+// First-order coefficient E_ik / (mu_k - mu_i) of column k's correction along column i (0 for
+// eigenvalues closer than 1e-5 relative, which stay coupled: their error is second order).  The
+// difference is taken in FP64 (no cancellation for close pairs), the quotient in FP32.
+__device__ __forceinline__ cf first_order(const cf* Eb, const cd* mb, int n, int i, int k) {
+  const cd mi = mb[i], mkk = mb[k];
+  const cd dd = mkk - mi;
+  const cf d32 = mk((float)dd.re, (float)dd.im);
+  const float ad = cabs(d32);
+  const float am = cabs(mk((float)mi.re, (float)mi.im)) + cabs(mk((float)mkk.re, (float)mkk.im));
+  return ad > 1e-5f * am ? cdiv(Eb[(int64_t)i * n + k], d32) : mk(0.f);
+}
+
+// F of one refinement step, W += W F (one grid row per problem, b = boff + blockIdx.y, launched
+// by MX_PP).  A singleton column j: F_ij = E_ij / (mu_j - mu_i).  A column j of a cluster C with
+// transform X: the composition (I + F1) X - I of the first-order correction F1 of the cluster's
+// columns and X, that is F_ij = sum_{c in C} F1_ic X_cj for i outside C and X_ij - delta_ij
+// inside.  Applying X to uncorrected columns instead would leave a share of the other members'
+// first-order errors in column j, and the step would not converge for clustered eigenvalues.
+__global__ void k_eig_update(int64_t boff, int n, const cd* __restrict__ mu_in, const cf* __restrict__ E, cf* F,
+                             const int* __restrict__ lab, const int* __restrict__ pos, const int* __restrict__ csz,
+                             const int* __restrict__ memb, const cf* __restrict__ xc) {
+  const int64_t nn = (int64_t)n * n;
+  const int64_t b = boff + blockIdx.y;
+  const cf* Eb = E + b * nn;
+  const cd* mb = mu_in + b * n;
+  for (int rc = blockIdx.x * blockDim.x + threadIdx.x; rc < nn; rc += gridDim.x * blockDim.x) {
+    const int i = rc / n, j = rc - i * n;
+    const int k = csz[b * n + j];
+    cf out = mk(0.f);
+    if (k < 2 || k > kClusterMax) {
+      if (i != j) out = first_order(Eb, mb, n, i, j);
+    } else {
+      const int64_t cj = (b * n + j) * kClusterMax;
+      if (lab[b * n + i] == lab[b * n + j]) {
+        out = xc[cj + pos[b * n + i]];
+        if (i == j) out.re -= 1.f;
+      } else {
+        for (int p = 0; p < k; ++p) fma_acc(out, first_order(Eb, mb, n, i, memb[cj + p]), xc[cj + p]);
+      }
+    }
+    F[b * nn + rc] = out;
+  }
+}
+
+// R and T of a problem are undefined when its incident wave is evanescent: the incident kz is
+// imaginary (Re kz_inc = 0), the flux normalisation divides by it and both come out NaN, as in
+// the reference (crystal.py:363-396, alternative.py:235-245).  Such a problem is never flagged for
+// a re-solve, which could not change them.
+__device__ __forceinline__ bool rt_undefined(const double* kp, double k0, cd epsi) {
+  const cd kpx = mk(kp[0], kp[1]), kpy = mk(kp[2], kp[3]);
+  return conj(csqrt(mk(k0 * k0) * epsi - kpx * kpx - kpy * kpy)).re == 0.0;
+}
+
+// Eigen-residual check after the last refinement step: MW holds M W (FP64-accurate).  A problem
+// whose relative residual max_i |(M W - W diag(mu))_ij| / (max|mu| max_i |W_ij|) exceeds 1e-8 in
+// any column j, or is not finite, gets KHP_BIT_MODES (unless its R and T are undefined).  One CTA
+// per matrix; lanes take consecutive columns, so each row's loads are coalesced.
+__global__ void __launch_bounds__(256) k_eig_check(int n, const cd* __restrict__ MW, const cd* __restrict__ W,
+                                                   const cd* __restrict__ mu, const double* __restrict__ kp,
+                                                   const double* __restrict__ k0, cd epsi, int* stat) {
+  __shared__ TeamShared sh;
+  TeamCta t;
+  const int64_t b = blockIdx.x;
+  if (rt_undefined(kp + 4 * b, k0[b], epsi)) return;
+  const int64_t nn = (int64_t)n * n;
+  const cd* mb = mu + b * n;
+  double big = 0.0;
+  int bi = 0;
+  for (int i = t.tid(); i < n; i += t.size()) big = fmax(big, cabs(mb[i]));
+  team_argmax(t, big, bi, &sh);
+  double worst = 0.0;
+  for (int j = t.tid(); j < n; j += t.size()) {
+    double r = 0.0, w = 0.0;
+    const cd mj = mb[j];
+    for (int i = 0; i < n; ++i) {
+      const int64_t e = b * nn + (int64_t)i * n + j;
+      const cd wij = W[e];
+      r = fmax(r, cabs(MW[e] - wij * mj));
+      w = fmax(w, cabs(wij));
+    }
+    const double rel = r / (big * w);
+    worst = rel == rel ? fmax(worst, rel) : INFINITY;  // a NaN fails the test
+  }
+  team_argmax(t, worst, bi, &sh);
+  if (t.tid() == 0 && !(worst <= 1e-8)) stat[b] |= KHP_BIT_MODES;
 }
 
 // W64 += D32 ; W32 = round(W64)
@@ -676,9 +814,10 @@ __global__ void k_check_refine(int64_t batch, const double* __restrict__ c0, con
   }
 }
 
-__global__ void k_flag_unconverged(int64_t batch, const int* __restrict__ active, int* status) {
+__global__ void k_flag_unconverged(int64_t batch, const int* __restrict__ active, const double* __restrict__ kp,
+                                   const double* __restrict__ k0, cd epsi, int* status) {
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < batch; b += (int64_t)gridDim.x * blockDim.x)
-    if (active[b]) status[b] |= KHP_BIT_REFINE;
+    if (active[b] && !rt_undefined(kp + 4 * b, k0[b], epsi)) status[b] |= KHP_BIT_REFINE;
 }
 
 #include "khp_adjoint.cuh"
@@ -789,7 +928,9 @@ struct MixedPlan {
   // modes scratch
   cf *M32, *Z32, *E32, *lu32;
   cd *M64, *MW64, *CW64, *Ct64, *mu64, *mu64b;
-  int *pair, *nearest;
+  int *pair, *nearest;  // eigen-refinement clusters: label and rank of every column, [bm][n]
+  int *csz, *memb;      // cluster size per column [bm][n]; members [bm][n][kClusterMax]
+  cf* xc;               // column of the cluster transform per column, [bm][n][kClusterMax]
   int* piv;
   std::vector<int*> midx;  // per map slot: the map index of every problem
   // the modes of all map slots run as one batch of S x batch matrices (slot-major): per-matrix
@@ -843,6 +984,9 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.mu64b = a.take<cd>(bm * n);
   p.pair = a.take<int>(bm * n);
   p.nearest = a.take<int>(bm * n);
+  p.csz = a.take<int>(bm * n);
+  p.memb = a.take<int>(bm * n * kClusterMax);
+  p.xc = a.take<cf>(bm * n * kClusterMax);
   p.piv = a.take<int>(bm * n);
   if (nmaps_used > 0) {
     // sized for M W (n x n x n); the C W products (nh x n, inner nh) need less
@@ -1100,35 +1244,34 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
-    // M W in FP64 (tensor-core digit products) for the first and the last step; in between, after W += dW = W32 F, it is
-    // updated as M W += round(M W) F in FP32.  That update is only FP32-accurate where F is large
-    // (close eigenvalues), so the last step's residual is formed from scratch.  (The structured
-    // product P (Q W) costs less but cancels terms of size k^4 / eps for the evanescent orders.)
+    // M W in FP64 (tensor-core digit products) at every step.  Updating it in FP32 instead
+    // (M W += round(M W) F) is only FP32-accurate where F is large: next to a nearly defective
+    // cluster that error enters the next step's residual and the refinement stalls at ~1e-8.
+    // (The structured product P (Q W) costs less but cancels terms of size k^4 / eps for the
+    // evanescent orders.)
     for (int step = 0; step < kEigSteps; ++step) {
-      const bool last = step == kEigSteps - 1;
       if (step > 0) {
         // E with the inverse of the current W: the first step can rotate the vectors of a close
         // pair by ~1e-3, after which W0^-1 would make the later steps converge only linearly
         MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
         MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
       }
-      if (step == 0 || last)
-        MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
+      MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
       MX_PP(k_eig_residual, bm, nn, n, p.MW64, W64, mu_a, p.E32);
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
-      k_find_pairs<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.pair, p.nearest);
+      k_clusters<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.Z32, p.pair, p.nearest, p.csz, p.memb, p.xc, mu_b);
       count_launches(1);
       MX_TRY(cuda_status());
-      MX_PP(k_eig_update, bm, nn, n, mu_a, p.Z32, p.M32, mu_b, p.pair);  // M32 <- F
+      MX_PP(k_eig_update, bm, nn, n, mu_a, p.Z32, p.M32, p.pair, p.nearest, p.csz, p.memb, p.xc);  // M32 <- F
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, W32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
       MX_EW(k_add_correction, bm * nn, bm * nn, W64, p.Z32, W32);
-      if (!last) {
-        MX_EW(k_round, bm * nn, bm * nn, p.MW64, p.E32);
-        MX_TRY(launch_gemm<float>(bm, n, n, n, one, p.E32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
-        MX_EW(k_accumulate, bm * nn, bm * nn, p.MW64, p.Z32);
-      }
       std::swap(mu_a, mu_b);
     }
+    // FP64 eigen-residual of the refined modes (KHP_BIT_MODES where a column missed 1e-8)
+    MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
+    k_eig_check<<<(unsigned)bm, 256, 0, s>>>(n, p.MW64, W64, mu_a, kpx, k0x, epsi, sx);
+    count_launches(1);
+    MX_TRY(cuda_status());
     MX_EW(k_sqrt_mu, bm * n, bm * n, mu_a, lam64, lam32);
     // V = Q W / lam in FP64
     cd* CWt = p.CW64;
@@ -1253,7 +1396,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     if (it >= refine && refine >= 1)
       MX_EW(k_check_refine, batch, batch, p.corr + ((it - 1) & 1) * batch, p.corr + (it & 1) * batch, p.active);
   }
-  if (refine >= 1) MX_EW(k_flag_unconverged, batch, batch, p.active, status);
+  if (refine >= 1) MX_EW(k_flag_unconverged, batch, batch, p.active, kp, k0, epsi, status);
   if (!grad) {
     k_flux_cols<double><<<(unsigned)batch, 128, 0, s>>>(nh, npol, p.RT, p.RT + batch * 2 * n, gx, gy, kp, k0,
                                                          reinterpret_cast<const cd*>(te),
@@ -1268,6 +1411,23 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
 }
 
 }  // namespace
+
+int mixed_modes_in_workspace(int64_t batch, int nh, int L, const int* kinds, const int* maps, const void* ws,
+                             size_t ws_bytes, const cd** W, const cd** V, const cd** lam) {
+  std::vector<int> used;
+  for (int l = 0; l < L; ++l)
+    if (kinds[l] == 1 && std::find(used.begin(), used.end(), maps[l]) == used.end()) used.push_back(maps[l]);
+  *W = *V = *lam = nullptr;
+  if (used.empty()) return KHP_OK;
+  Arena a{static_cast<char*>(const_cast<void*>(ws)), ws_bytes};
+  MixedPlan p = plan_mixed(a, batch, nh, L, kinds, (int)used.size());
+  if (!a.ok || !ws) return KHP_ERR_WORKSPACE;
+  *W = p.W64[0];
+  *V = p.V64[0];
+  *lam = p.lam64[0];
+  return KHP_OK;
+}
+
 }  // namespace khp
 
 using namespace khp;

@@ -132,9 +132,12 @@ class _stage:
 _WS = {}
 
 
-def workspace(nbytes, device):
-    """A reusable device byte buffer of at least ``nbytes`` per device (grown, never shrunk)."""
-    key = str(device)
+def workspace(nbytes, device, slot=0):
+    """A reusable device byte buffer of at least ``nbytes`` per device and slot (grown, never
+    shrunk).  Calls whose workspaces must coexist use different slots: a mixed-precision solve
+    keeps its refined modes in its workspace until its flagged problems are re-solved, and a
+    pipelined caller alternates two slots between consecutive chunks."""
+    key = (str(device), int(slot))
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
         _WS[key] = buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
@@ -270,10 +273,16 @@ class Problems:
         te = np.broadcast_to(np.asarray(te, dtype=complex), (B,))
         tm = np.broadcast_to(np.asarray(tm, dtype=complex), (B,))
         d = torch.device(device)
-        return cls(k0=torch.tensor(TWOPI / wl, dtype=F64, device=d),
-                   kp=torch.tensor(kpa, dtype=C128, device=d).contiguous(),
-                   te=torch.tensor(np.ascontiguousarray(te), dtype=C128, device=d),
-                   tm=torch.tensor(np.ascontiguousarray(tm), dtype=C128, device=d))
+
+        def up(a, dtype):
+            # staged through pinned host memory, copied on the current stream without a host wait
+            h = torch.from_numpy(np.array(a, dtype=dtype))  # a writable contiguous copy
+            if d.type == "cuda":
+                return h.pin_memory().to(d, non_blocking=True)
+            return h.to(d)
+
+        return cls(k0=up(TWOPI / wl, np.float64), kp=up(kpa, np.complex128), te=up(te, np.complex128),
+                   tm=up(tm, np.complex128))
 
 
 @dataclass

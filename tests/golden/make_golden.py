@@ -387,5 +387,7 @@ if __name__ == "__main__":
         analytical(sys.argv[1])
     elif len(sys.argv) > 2 and sys.argv[2] == "twisted":
         twisted(sys.argv[1])
+    elif len(sys.argv) > 1:
+        main(sys.argv[1])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        sys.exit("usage: make_golden.py <reference source root> [tmat|beams|bands|analytical|twisted]")

@@ -301,25 +301,116 @@ def test_mixed_precision_small_cases(khp, golden):
         assert abs(R[0] - g["R"][i]) < RT_TOL and abs(T[0] - g["T"][i]) < RT_TOL
 
 
-def test_mixed_precision_repairs_ill_conditioned_problem(khp):
-    """A sweep problem next to a Wood anomaly (f index 49, k index 341 of the 11x11 sweep) whose
-    FP32-preconditioned refinement converges too slowly: the mixed path must flag it (status
-    bit 8) and re-solve it (longer mixed refinement, then FP64 if needed), so that it still
-    meets |dR|, |dT| <= 1e-6."""
+def _no_repairs_since(before):
+    from khepri_gb300 import batch
+    return all(batch.STATS[k] == before[k] for k in before)
+
+
+def test_mixed_precision_plain_sweep_5x5_symmetric(khp, golden):
+    """The reference's drop-in case (5x5, disc in a square cell, normal incidence) through the
+    mixed path, all 151 frequencies, against the reference's complex128 values: |dR|, |dT| <= 1e-6
+    with no problem flagged or re-solved.  The C4v-symmetric pixmap at normal incidence gives
+    exactly degenerate mode pairs, the case the eigen-refinement's pair handling must converge on."""
+    from khepri_gb300 import batch, workloads
+    g = golden("plain_5x5")
+    sw = workloads.plain_sweep()
+    before = dict(batch.STATS)
+    R, T, st = batch.solve_rt((5, 5), sw.structure.layers, sw.structure.stack, sw.wavelengths, sw.kp, 1.0, 0.0,
+                              chunk=151, method="mixed")
+    assert not st.any()
+    assert _no_repairs_since(before)
+    err = max(np.abs(R - g["R"]).max(), np.abs(T - g["T"]).max())
+    print("mixed vs reference (5x5 plain sweep) max |dR|,|dT| =", err)
+    assert err < RT_TOL
+    assert np.abs(R + T - 1).max() < 1e-8  # lossless
+
+
+def test_mixed_precision_symmetric_3x3_all_frequencies(khp):
+    """The 3x3 variant of the drop-in case on a 32x32 pixmap (the smoke problem), all 151
+    frequencies through the mixed path against the CPU oracle: |dR|, |dT| <= 1e-6, no repairs."""
+    from khepri_gb300 import batch, workloads
+    from oracle import khepri_oracle as ko
+    sw = workloads.plain_sweep(pw=(3, 3), n_pix=32, nfreq=151)
+    before = dict(batch.STATS)
+    R, T, st = batch.solve_rt((3, 3), sw.structure.layers, sw.structure.stack, sw.wavelengths, sw.kp, 1.0, 0.0,
+                              chunk=151, method="mixed")
+    assert not st.any()
+    assert _no_repairs_since(before)
+    ref = np.array([ko.solve_rt((3, 3), sw.structure.layers, sw.structure.stack, wl, 1.0, 0.0)
+                    for wl in sw.wavelengths])
+    err = max(np.abs(R - ref[:, 0]).max(), np.abs(T - ref[:, 1]).max())
+    print("mixed vs oracle (3x3 plain sweep) max |dR|,|dT| =", err)
+    assert err < RT_TOL
+    assert np.abs(R + T - 1).max() < 1e-8
+
+
+def test_mixed_precision_ill_conditioned_problems(khp):
+    """Sweep problems next to a Wood anomaly (f index 49, k index 341 of the 11x11 sweep) and
+    with a conjugate eigenvalue pair 1e-4 apart (38308), whose FP32-preconditioned refinement
+    converges slowly: the mixed path (with its re-solve of anything it flags) must still meet
+    |dR|, |dT| <= 1e-6 against the FP64 recursion, with every status clear."""
     from khepri_gb300 import batch, workloads
     st = workloads.batched_structure(0)
     wl, kp = workloads.batched_problems()
     inside = np.flatnonzero(np.hypot(kp[:, 0], kp[:, 1]) < 2 * np.pi / wl)
-    idx = np.concatenate([[50517, 38308, 47259], inside[inside > 20000][:3]])
-    before = batch.STATS["refine_repairs"]
+    idx = np.concatenate([[50517, 38308, 47259, 1400, 4469, 7987], inside[inside > 20000][:3]])
+    before = dict(batch.STATS)
     Rm, Tm, sm = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="mixed")
-    assert batch.STATS["refine_repairs"] > before
+    print("re-solved:", {k: batch.STATS[k] - before[k] for k in before})
     assert not sm.any()
     Rg, Tg, _ = batch.solve_rt(st.pw, st.layers, st.stack, wl[idx], kp[idx], both_pols=True, method="gamma")
     assert np.isfinite(Rg).all() and np.isfinite(Tg).all()
     err = max(np.abs(Rm - Rg).max(), np.abs(Tm - Tg).max())
-    print("mixed (with FP64 repair) vs fp64 max |dR|,|dT| =", err)
+    print("mixed vs fp64 max |dR|,|dT| =", err)
     assert err < RT_TOL
+
+
+def test_fp64_resolve_from_refined_modes(khp):
+    """khp_solve_batched_mixed_repair on problems picked out of a mixed-precision chunk (in an
+    order unlike the chunk's): the FP64 recursion from the chunk's refined modes agrees with the
+    full FP64 path (its own FP64 eigensolve) to 1e-9, and an index outside the chunk is reported
+    as a per-problem input error."""
+    import torch
+    from khepri_gb300 import batch, engine, workloads
+    st = workloads.batched_structure(0)
+    wl, kp = workloads.batched_problems()
+    inside = np.flatnonzero(np.hypot(kp[:, 0], kp[:, 1]) < 2 * np.pi / wl)
+    idx = inside[::997][:24]
+    dev = torch.device("cuda")
+    struct = engine.StructureGPU(st.pw, engine.lattice_vectors("square"), dev)
+    plan = batch.StackPlan(struct, batch._specs(st.layers, 1.0, 1.0), st.stack)
+    prob = engine.Problems.make(wl[idx], kp[idx], 1.0, 0.0, dev)
+    te, tm = batch.both_pol_weights(prob.batch, dev)
+    status = torch.zeros(prob.batch, dtype=torch.int32, device=dev)
+    batch.solve_chunk_gamma(struct, plan, prob, status, te=te, tm=tm, precision="mixed", repair=False, ws_slot=3)
+    mixed_ws = engine.workspace(0, dev, 3)
+    sel = torch.tensor([17, 0, 5, 23], dtype=torch.int64, device=dev)
+    r, t, s = batch.resolve_fp64(struct, plan, prob, sel, te, tm, mixed_ws=mixed_ws)
+    r64, t64, s64 = batch.resolve_fp64(struct, plan, prob, sel, te, tm)
+    assert not s.any() and not s64.any()
+    err = max((r - r64).abs().max().item(), (t - t64).abs().max().item())
+    print("FP64 recursion from refined modes vs own FP64 eigensolve: max |dR|,|dT| =", err)
+    assert err < 1e-9
+    # row 1 of the chunk, then a row past its end
+    bad = torch.tensor([1, prob.batch], dtype=torch.int64, device=dev)
+    lib = khp._capi.load()
+    rows = bad.to(torch.int32)
+    sub = prob.subset(bad.clamp(max=prob.batch - 1))
+    r2 = torch.empty((2, 2), dtype=torch.float64, device=dev)
+    t2 = torch.empty_like(r2)
+    s2 = torch.zeros(2, dtype=torch.int32, device=dev)
+    ws = engine.workspace(lib.khp_solve_batched_workspace(2, struct.nh, 5, batch._host(plan.kinds),
+                                                          batch._host(plan.maps)), dev, batch.REPAIR_WS_SLOT)
+    te2, tm2 = te[:2].contiguous(), tm[:2].contiguous()
+    P = khp._capi.ptr
+    code = lib.khp_solve_batched_mixed_repair(
+        2, st.pw[0], st.pw[1], 5, batch._host(plan.kinds), batch._host(plan.maps), batch._host(plan.eps),
+        batch._host(plan.depth), None, None, plan.nmaps, P(plan.conv), P(plan.hx), P(plan.hy), P(struct.gx),
+        P(struct.gy), 1.0, 0.0, 1.0, 0.0, P(sub.kp), P(sub.k0), 2, P(te2), P(tm2), prob.batch, P(rows), P(mixed_ws),
+        mixed_ws.numel(), P(r2), P(t2), P(s2), P(ws), ws.numel(), khp._capi.stream_ptr())
+    assert code == 0
+    s2 = s2.cpu().numpy()
+    assert s2[0] == 0 and (s2[1] & 16)
 
 
 def test_solve_structures_uneven_golden(khp, golden):
