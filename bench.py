@@ -98,7 +98,8 @@ def parse():
     ap.add_argument("--plain", type=int, default=2, help="single-problem drop-in solves timed for comparison")
     ap.add_argument("--grad-designs", type=int, default=64,
                     help="inverse-design structures (x 16 frequencies) for the solve+grad measurement (0 = skip)")
-    ap.add_argument("--uneven", type=int, default=0, help="uneven structures for the many-structure measurement")
+    ap.add_argument("--uneven", type=int, default=1024,
+                    help="uneven structures (config 3's shapes) for the many-structure measurement (0 = skip)")
     ap.add_argument("--twisted", type=int, default=16,
                     help="twisted-bilayer problems (5x5 base harmonics, n = 1250) for the extended-crystal measurement")
     ap.add_argument("--tc-product", type=int, default=0,
@@ -326,25 +327,42 @@ def bench_grad(args, struct11, st11, wl_all, kp_all):
 
 
 def bench_uneven(args):
-    """Many structures of different sizes (3x3..17x17 harmonics, 1-8 lossy smoothed layers of
-    128x128, one problem each) through solve_structures (mixed), host wall clock."""
+    """Config 3's uneven batch: structures of 3x3..17x17 harmonics with 1-8 lossy smoothed 128x128
+    layers, one problem each, through solve_structures (mixed; grouped by shape, chunks of the
+    autotuned size), host wall clock; R, T and A = 1 - R - T against the CPU oracle on the first
+    structure of every harmonic count."""
     from khepri_gb300 import batch, workloads
+    from oracle import khepri_oracle as ko
     if args.uneven <= 0:
         return None
     sts = workloads.uneven_structures(args.uneven, seed=0)
     ents = [(s.pw, s.layers, s.stack) for s, _, _ in sts]
     wl = np.array([w for _, w, _ in sts])
     kp = np.array([k for _, _, k in sts])
-    small = min(8, len(ents))
 
-    def run(n):
-        return batch.solve_structures(ents[:n], wl[:n], kp[:n], te=1.0, tm=1.0, chunk=64, strict=False)
+    def run(sel):
+        return batch.solve_structures([ents[i] for i in sel], wl[sel], kp[sel], te=1.0, tm=1.0, strict=False)
 
-    run(small)
-    res, t = _timed(lambda: run(len(ents)))
+    run(np.arange(min(64, len(ents))))
+    res, t = _timed(lambda: run(np.arange(len(ents))))
+    R, T, st = res
+    first = {}
+    for i, (s, _, _) in enumerate(sts):
+        first.setdefault(s.pw[0], i)
+    errs = {"R": 0.0, "T": 0.0, "A": 0.0}
+    t_cpu = time.perf_counter()
+    for p_, i in sorted(first.items()):
+        r0, t0 = ko.solve_rt(ents[i][0], ents[i][1], ents[i][2], wl[i], 1.0, 1.0, kp=tuple(kp[i]))
+        errs["R"] = max(errs["R"], abs(R[i] - r0))
+        errs["T"] = max(errs["T"], abs(T[i] - t0))
+        errs["A"] = max(errs["A"], abs((1 - R[i] - T[i]) - (1 - r0 - t0)))
+    t_cpu = time.perf_counter() - t_cpu
     return {"structures_per_s": len(ents) / t, "structures": len(ents), "seconds": t,
-            "problems_with_status": int((res[2] != 0).sum()),
-            "sizes": "pw 3..17 odd, 1..8 layers; grouped by shape into batched calls"}
+            "problems_with_status": int((st != 0).sum()),
+            "sizes": "pw 3..17 odd, 1..8 layers of 128x128 maps; grouped by shape, autotuned chunks",
+            "max_abs_err_vs_oracle": errs,
+            "err_sample": f"the first structure of each of the {len(first)} harmonic counts, CPU oracle "
+                          f"({t_cpu:.1f} s)"}
 
 
 def bench_twisted(args):

@@ -45,6 +45,17 @@ int khp_version(void);
 const char* khp_status_string(int code);
 
 /*
+ * Launch tuning, process-wide (no counterpart in the reference).  param KHP_TUNE_EIG_THREADS:
+ * threads per CTA of the batched eigensolver (Hessenberg reduction and QR) for matrices of
+ * size n (1 <= n <= 4096): a multiple of 32 up to 256, or 0 for the default (256).  The results
+ * do not depend on it; the speed does (small matrices leave a 256-thread team mostly idle).  Set
+ * it before the launches it should affect (it is read when a call enqueues its kernels).
+ * khepri_gb300.autotune measures the choices and writes the table the Python API applies.
+ */
+#define KHP_TUNE_EIG_THREADS 1
+int khp_tune(int32_t param, int32_t n, int32_t value);
+
+/*
  * Convolution (Toeplitz) matrices of pixmaps.  Replaces tools.convolution_matrix
  * (khepri/tools.py:33-56): C[r][c] = eps_hat(p_r - p_c, q_r - q_c) with r = q*px + p and
  * eps_hat(dx, dy) = (1/(nx*ny)) sum_{x,y} eps[x][y] exp(-2 pi i (dx x/nx + dy y/ny)),

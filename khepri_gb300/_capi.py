@@ -77,6 +77,7 @@ _SIGNATURES = {
     "khp_twisted_rt": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_i32, _c_p, _c_p, _c_d, _c_d,
                                       _c_d, _c_d, _c_p, _c_p, _c_p, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_launch_count": (ctypes.c_longlong, []),
+    "khp_tune": (ctypes.c_int, [_c_i32, _c_i32, _c_i32]),
     "khp_probe_fp64_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
     "khp_probe_fp32_tflops": (ctypes.c_double, [_c_p, _c_i64, _c_p]),
     "khp_stage_timing": (ctypes.c_int, [_c_i32]),

@@ -14,7 +14,7 @@ import functools
 import numpy as np
 import torch
 
-from . import _capi, engine
+from . import _capi, autotune, engine
 from .engine import LayerSpec
 
 
@@ -149,6 +149,7 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
               _capi.ptr(struct.gx), _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
               _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm))
     fix = None
+    autotune.ensure_applied()
     if precision == "mixed":
         ws = engine.workspace(lib.khp_solve_batched_mixed_workspace(B, struct.nh, L, _host(plan.kinds),
                                                                      _host(plan.maps)), dev, ws_slot)
@@ -443,8 +444,10 @@ def _group_chunks(structures, which, chunk, lattice, device):
         struct = engine.StructureGPU(pw, lat, device)
         members = np.asarray(members)
         L = len(kinds)
-        for s in range(0, len(members), chunk):
-            idx = members[s:s + chunk]
+        nslots = len({s for k, s in zip(kinds, slots) if k == 1}) or 1
+        step = chunk if chunk else autotune.chunk_for(2 * pw[0] * pw[1], nslots)
+        for s in range(0, len(members), step):
+            idx = members[s:s + step]
             B = len(idx)
             mpos, eps_maps = {}, []
             for sid in dict.fromkeys(which[idx].tolist()):
@@ -487,14 +490,16 @@ def _prep_args(wavelengths, kp, which, te, tm):
 
 
 def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, lattice="square", epsi=1.0,
-                     epse=1.0, chunk=256, both_pols=False, method="mixed", refine=2, strict=True, device="cuda"):
+                     epse=1.0, chunk=None, both_pols=False, method="mixed", refine=2, strict=True, device="cuda"):
     """R and T of problems spread over many structures, batched across structures.
 
     structures: list of (pw, layers, stack) (``layers`` as in solve_rt); which: [P] structure of
     each problem (default: problem i uses structure i).  Structures with the same harmonic set,
     layer kinds, uniform media and pixmap-sharing pattern form one group; each chunk of a group is
     one khp_solve_batched(_mixed) call with per-problem maps and depths (maps of the chunk
-    prepared in one batched launch).  method: "mixed" (default) or "gamma" (FP64).
+    prepared in one batched launch).  chunk: problems per call (None: the autotuned number of
+    mode matrices per call for the group's size, divided by its maps per problem).
+    method: "mixed" (default) or "gamma" (FP64).
     Returns R, T ([P] or [P, 2] with ``both_pols``) and status [P].
     """
     _capi.require_cuda()

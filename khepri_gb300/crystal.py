@@ -13,6 +13,12 @@ Differences a user may notice:
 * The convolution matrix, C^-1 and the Hx/Hy products of a pixmap are computed once per pixmap
   content, not on every ``solve`` (the reference rebuilds them, layer.py:156-158); the pixmap
   is still read at ``solve`` time, so in-place edits between solves are honoured.
+* ``solve`` computes R and T of the source by the batched mixed-precision recursion
+  (khp_solve_batched_mixed: FP32 eigensolve with FP64 refinement, FP64-refined stack
+  equations; within ~1e-10 of complex128).  The S-matrices (``S``, ``Stot``, the stacking
+  matrices) and what needs them (per-order powers, R and T of a source changed after ``solve``,
+  fields) come from the FP64 layer-by-layer chain, built on first use from the same solve's
+  inputs; their values are the reference's either way.
 """
 from __future__ import annotations
 
@@ -24,7 +30,7 @@ from types import SimpleNamespace
 import numpy as np
 import torch
 
-from . import _capi, engine
+from . import _capi, batch, engine
 from .expansion import Expansion
 from .engine import LayerSpec
 
@@ -74,9 +80,35 @@ class Layer:
         return LayerSpec(self.kind, self.epsilon, self.depth)
 
 
+class _Built:
+    """An attribute of a solved Crystal that comes from its S-matrix chain, built on first read."""
+
+    def __set_name__(self, owner, name):
+        self.slot = "_built_" + name
+
+    def __get__(self, obj, owner=None):
+        if obj is None:
+            return self
+        if obj._chain_pending:
+            obj._build_chain()
+        return obj.__dict__.get(self.slot)
+
+    def __set__(self, obj, value):
+        obj.__dict__[self.slot] = value
+
+
 class Crystal:
     """GPU drop-in for khepri.crystal.Crystal (crystal.py:42-81; square, hexagonal or explicit
     lattices)."""
+
+    S = _Built()
+    Stot = _Built()
+    stacking_matrices = _Built()
+    stacking_reverse_matrices = _Built()
+    _states = _Built()
+    _fwd = _Built()
+    _rev = _Built()
+    _Stot_b = _Built()
 
     def __init__(self, pw, lattice="square", lattice_pitch=1, void=False, epsi=1, epse=1, device="cuda"):
         self.pw = tuple(pw)
@@ -90,6 +122,9 @@ class Crystal:
         self._struct = engine.StructureGPU(self.pw, self.lattice, device)
         self.device = self._struct.device
         self.layers = dict()
+        self._chain_pending = False
+        self._solved = False
+        self._rt = None
         self.stacking_matrices = list()
         self.stack_positions = []
         self.S = None
@@ -155,7 +190,7 @@ class Crystal:
     @property
     def solved(self):
         """crystal.py:176-178."""
-        return self.S is not None
+        return self._solved
 
     @property
     def zmax(self):
@@ -176,20 +211,56 @@ class Crystal:
     def _problems(self):
         return engine.Problems.make([self.source.wavelength], [self.kp], self.source.te, self.source.tm, self.device)
 
+    def _source_key(self):
+        src = self.source
+        return (src.wavelength, complex(src.te), complex(src.tm), complex(self.kp[0]), complex(self.kp[1]))
+
+    def _fast_rt(self):
+        """Whether R, T of the source can come from the batched recursion: both half-spaces are
+        the crystal's own media and every device layer is homogeneous or patterned."""
+        if self.void or self.global_stacking[:1] != ["Sref"] or self.global_stacking[-1:] != ["Strans"]:
+            return False
+        if self.layers["Sref"].kind != "inc" or self.layers["Strans"].kind != "trn":
+            return False
+        return all(self.layers[name].kind in ("uniform", "pixmap") for name in self.device_stack)
+
     def solve(self):
-        """crystal.py:180-206: every distinct layer once, then the forward (and, when fields are
-        retained, reverse) star-product chains."""
+        """crystal.py:180-206: R and T of the source now (batched mixed-precision recursion);
+        every distinct layer's S-matrix and the forward (and, when fields are retained, reverse)
+        star-product chains when first read."""
         assert self.source_defined, "Call set_source before solving."
         prob = self._problems()
-        status = torch.zeros(1, dtype=torch.int32, device=self.device)
-        specs = {name: self.layers[name].spec() for name in set(self.global_stacking)}
-        keep = {name for name in specs if self.layers[name].fields}
-        states = engine.solve_layers(self._struct, specs, self.global_stacking, prob, status, keep_modes=keep)
         layer_sizes = [self.layers[name].depth for name in self.global_stacking]
         self.stack_positions = list(np.cumsum(layer_sizes))
         self.stack_positions[-1] = np.inf
         if not self.void:
             self.stack_positions.insert(0, -np.inf)
+        self._prob = prob
+        self._chain_pending = True
+        self._rt = None
+        if self._fast_rt():
+            specs = {name: self.layers[name].spec() for name in self.device_stack}
+            specs["__inc__"] = LayerSpec("inc", self.epsi, 0.0)
+            specs["__trn__"] = LayerSpec("trn", self.epse, 0.0)
+            plan = batch.StackPlan(self._struct, specs, self.device_stack)
+            status = torch.zeros(1, dtype=torch.int32, device=self.device)
+            R, T = batch.solve_chunk_gamma(self._struct, plan, prob, status, self.epsi, self.epse, precision="mixed")
+            word = int(status.item())
+            if word:
+                raise _capi.KhpError(f"solve: {_capi.decode_status(word)}")
+            self._rt = (self._source_key(), float(R[0].item()), float(T[0].item()))
+        else:
+            self._build_chain()
+        self._solved = True
+
+    def _build_chain(self):
+        """The layer S-matrices and star-product chains of the last solve (FP64 throughout)."""
+        self._chain_pending = False
+        prob = self._prob
+        status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        specs = {name: self.layers[name].spec() for name in set(self.global_stacking)}
+        keep = {name for name in specs if self.layers[name].fields}
+        states = engine.solve_layers(self._struct, specs, self.global_stacking, prob, status, keep_modes=keep)
         want_fields = any(self.stack_retain_mask[1:-1])
         fwd, rev, Stot = engine.chain(states, self.global_stacking, self.stack_retain_mask, status,
                                       reverse=want_fields)
@@ -197,7 +268,6 @@ class Crystal:
         if word:
             raise _capi.KhpError(f"solve: {_capi.decode_status(word)}")
         self._states = states
-        self._prob = prob
         self._fwd, self._rev = fwd, rev
         self.stacking_matrices = [None if s is None else s[0] for s in fwd]
         self.stacking_reverse_matrices = None if rev is None else [None if s is None else s[0] for s in rev]
@@ -208,7 +278,11 @@ class Crystal:
     def poynting_flux_end(self, only_total=True):
         """crystal.py:363-396."""
         assert self.solved, "Call solve first"
-        R, T, ro, to = engine.flux(self._struct, self._Stot_b, self._prob, self.epsi, self.epse, orders=not only_total)
+        if only_total and self._rt is not None and self._rt[0] == self._source_key():
+            return self._rt[1], self._rt[2]
+        # the source as it is now (the reference reads self.source here, crystal.py:365-370)
+        R, T, ro, to = engine.flux(self._struct, self._Stot_b, self._problems(), self.epsi, self.epse,
+                                   orders=not only_total)
         if only_total:
             return float(R.item()), float(T.item())
         return (float(R.item()), ro[0].cpu().numpy()), (float(T.item()), to[0].cpu().numpy())

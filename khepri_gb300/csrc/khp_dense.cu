@@ -13,6 +13,16 @@ namespace {
 constexpr int kTeamThreads = 256;
 constexpr int64_t kMaxGridY = 65535;
 
+// Threads per eigensolver CTA by matrix size (khp_tune; 0 = kTeamThreads).  Small matrices leave
+// most of a 256-thread team idle, and smaller teams let more matrices share an SM.
+constexpr int kTuneMaxN = 4096;
+int g_eig_threads[kTuneMaxN + 1] = {0};
+
+int eig_threads(int n) {
+  const int v = n <= kTuneMaxN ? g_eig_threads[n] : 0;
+  return v > 0 ? v : kTeamThreads;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kTeamThreads) k_getrf(int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv,
                                                          int* info) {
@@ -666,8 +676,9 @@ int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_gehrd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
-  k_gehrd<T><<<(unsigned)batch, kTeamThreads, smem, s>>>(n, A, lda, bsA, Z, blocked);
-  k_geev_schur<T><<<(unsigned)batch, kTeamThreads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
+  const int threads = eig_threads(n);
+  k_gehrd<T><<<(unsigned)batch, threads, smem, s>>>(n, A, lda, bsA, Z, blocked);
+  k_geev_schur<T><<<(unsigned)batch, threads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
   count_launches(2);
   int st = cuda_status();
   if (st) return st;
@@ -905,6 +916,14 @@ KHP_INSTANTIATE(float)
 }  // namespace khp
 
 extern "C" {
+
+int khp_tune(int32_t param, int32_t n, int32_t value) {
+  using namespace khp;
+  if (param != KHP_TUNE_EIG_THREADS || n < 1 || n > kTuneMaxN) return KHP_ERR_INVALID_ARG;
+  if (value != 0 && (value < 32 || value > kTeamThreads || value % 32 != 0)) return KHP_ERR_INVALID_ARG;
+  g_eig_threads[n] = value;
+  return KHP_OK;
+}
 
 size_t khp_inverse_workspace(int64_t batch, int32_t n) {
   if (batch < 0 || n < 1) return 0;

@@ -6,7 +6,7 @@
 //   1. modes: FP32 eigensolve of M = P Q, then three FP64 refinement steps of the eigenpairs:
 //      E = W^-1 (M W - W mu) with the residual formed in FP64 and the solve in FP32,
 //      mu += diag(E), W += W F with F_ij = E_ij / (mu_j - mu_i); clusters of eigenvalues closer
-//      than 3e-3 max|mu| take the exact eigen-decomposition of their block of diag(mu) + E
+//      than 1e-3 max|mu| take the exact eigen-decomposition of their block of diag(mu) + E
 //      instead (cyclic 2x2 Jacobi sweeps), composed with the first-order correction of their
 //      columns; an FP64 residual test of every mode follows (status bit 32 where it fails);
 //      V = Q W / lam in FP64.  The FP64 products M W and C W run on the bf16 tensor cores with
@@ -74,8 +74,11 @@ __device__ __forceinline__ cd pair_den(cd a, cd b, cd c, cd d) {
 // eigenvalues closer than kClusterTol max|mu|.  Inside a cluster a first-order step converges
 // slowly or not at all (its correction E_ij / (mu_j - mu_i) is not small), so every cluster of
 // 2..kClusterMax members takes the exact eigen-decomposition of its block of diag(mu) + E instead.
-constexpr double kClusterTol = 3e-3;
+// A component larger than kClusterMax (a chain of close eigenvalues) is split again at a third of
+// the distance, up to kClusterLevels times; what is still too large is treated member by member.
+constexpr double kClusterTol = 1e-3;
 constexpr int kClusterMax = 12;
+constexpr int kClusterLevels = 4;
 // Cluster members whose 2x2 sub-block does not resolve two directions (|den| below this times
 // max|mu|) are degenerate to within the refinement's noise (e.g. the two modes of a
 // two-dimensional representation of a symmetric pixmap at normal incidence): any basis of an
@@ -145,39 +148,63 @@ __global__ void __launch_bounds__(256) k_clusters(int n, const cd* __restrict__ 
     lb[i] = i;
   }
   team_argmax(t, big, bi, &sh);
-  const double tol2 = (kClusterTol * big) * (kClusterTol * big);
-  // connected components by repeated minimum-label propagation (bounded; a component whose labels
-  // have not settled is only split, and each part is still handled consistently)
-  for (int it = 0; it < 64; ++it) {
+  int* sz = csz + b * n;
+  int* act = pos + b * n;  // scratch until the ranks are written: column still being split
+  double tol = kClusterTol * big;
+  for (int level = 0; level < kClusterLevels; ++level, tol *= (1.0 / 3.0)) {
     if (t.tid() == 0) changed = 0;
     t.sync();
     for (int i = t.tid(); i < n; i += t.size()) {
-      const cd mi = m[i];
-      int best = lb[i];
-      for (int j = 0; j < n; ++j) {
-        const double dr = m[j].re - mi.re, di = m[j].im - mi.im;
-        if (dr * dr + di * di < tol2) best = min(best, lb[j]);
-      }
-      if (best < lb[i]) {
-        lb[i] = best;
+      act[i] = level == 0 || sz[i] > kClusterMax;
+      if (act[i]) {
+        lb[i] = i;
         changed = 1;
       }
     }
     t.sync();
     if (!changed) break;
     t.sync();
+    const double tol2 = tol * tol;
+    // connected components among the columns being split, by repeated minimum-label propagation
+    // (bounded; a component whose labels have not settled is only split further, and each part is
+    // still handled consistently)
+    for (int it = 0; it < 64; ++it) {
+      if (t.tid() == 0) changed = 0;
+      t.sync();
+      for (int i = t.tid(); i < n; i += t.size()) {
+        if (!act[i]) continue;
+        const cd mi = m[i];
+        int best = lb[i];
+        for (int j = 0; j < n; ++j) {
+          if (!act[j]) continue;
+          const double dr = m[j].re - mi.re, di = m[j].im - mi.im;
+          if (dr * dr + di * di < tol2) best = min(best, lb[j]);
+        }
+        if (best < lb[i]) {
+          lb[i] = best;
+          changed = 1;
+        }
+      }
+      t.sync();
+      if (!changed) break;
+      t.sync();
+    }
+    // component sizes of the columns just labelled (a label is the smallest index of its
+    // component, so it never equals the label of a column outside it)
+    for (int i = t.tid(); i < n; i += t.size()) {
+      if (!act[i]) continue;
+      int c = 0;
+      for (int j = 0; j < n; ++j) c += lb[j] == lb[i];
+      sz[i] = c;
+    }
+    t.sync();
   }
-  // ranks and sizes (deterministic: by index)
+  // ranks (deterministic: by index)
   for (int i = t.tid(); i < n; i += t.size()) {
     const int l = lb[i];
-    int r = 0, c = 0;
-    for (int j = 0; j < n; ++j) {
-      if (lb[j] != l) continue;
-      r += j < i;
-      ++c;
-    }
+    int r = 0;
+    for (int j = 0; j < i; ++j) r += lb[j] == l;
     pos[b * n + i] = r;
-    csz[b * n + i] = c;
     const cf e = Eb[(int64_t)i * n + i];
     mu_out[b * n + i] = m[i] + mk((double)e.re, (double)e.im);
   }

@@ -76,6 +76,35 @@ def test_plain_sweep_151(khp, golden):
     assert np.abs(R + T - 1).max() < 1e-8  # lossless
 
 
+def test_dropin_source_edit_after_solve(khp):
+    """R, T come from the batched recursion at solve time; a source edited after solve (as in
+    the reference, poynting_flux_end reads self.source) is served from the FP64 S-matrix chain,
+    and per-order powers always are: all against the oracle at 1e-9."""
+    from khepri_gb300 import workloads
+    from oracle import khepri_oracle as ko
+    sw = workloads.plain_sweep()
+    cl = _crystal(khp, (5, 5), sw.structure.layers, sw.structure.stack)
+    ref = ko.OracleCrystal((5, 5))
+    for name, (kind, eps, depth) in sw.structure.layers.items():
+        (ref.add_layer_uniform if kind == "uniform" else ref.add_layer_pixmap)(name, eps, depth)
+    ref.set_device(sw.structure.stack, False)
+    for c in (cl, ref):
+        c.set_source(sw.wavelengths[40], 1.0, 0.0, 12.0, 30.0)
+        c.solve()
+    r, t = cl.poynting_flux_end()
+    r0, t0 = ref.poynting_flux_end()
+    assert abs(r - r0) < TIGHT and abs(t - t0) < TIGHT
+    for c in (cl, ref):
+        c.source.te, c.source.tm = 0.0, 1.0
+    r, t = cl.poynting_flux_end()
+    r0, t0 = ref.poynting_flux_end()
+    assert abs(r - r0) < TIGHT and abs(t - t0) < TIGHT
+    (r, ro), (t, to) = cl.poynting_flux_end(only_total=False)
+    (r0, ro0), (t0, to0) = ref.poynting_flux_end(only_total=False)
+    np.testing.assert_allclose(ro, ro0, atol=TIGHT)
+    np.testing.assert_allclose(to, to0, atol=TIGHT)
+
+
 def test_plain_sweep_batched_matches_dropin(khp, golden):
     from khepri_gb300 import batch, workloads
     g = golden("plain_5x5")
