@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=456,
                     help="problems per call (456 = 3 x 152 SMs: three eigensolver CTAs per SM)")
+    ap.add_argument("--eig-threads", type=int, default=0,
+                    help="eigensolver threads per CTA for the sweep's 242 x 242 matrices (khp_tune; 0 = default)")
     ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -108,6 +110,9 @@ def parse():
     ap.add_argument("--cpu-rate-only", type=int, default=0,
                     help="time the CPU oracle alone on this many in-cone sweep problems and print the seconds "
                          "(used in a child process whose BLAS threads are pinned)")
+    ap.add_argument("--tf32-product", type=int, default=0,
+                    help="only time khp_cgemm_tf32x3 (3xTF32 tensor-core complex product) on this many random "
+                         "242 x 242 complex64 problems against torch's complex64 matmul (kernel profiling)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -402,6 +407,8 @@ def run_gpu(args):
     from khepri_gb300 import _capi, batch, engine, replicas, workloads
 
     lib = _capi.load()
+    if args.eig_threads:
+        _capi.check(lib.khp_tune(1, N_MAT, args.eig_threads), "khp_tune")
     st = workloads.batched_structure(0)
     wl_all, kp_all = workloads.batched_problems()
     P = wl_all.shape[0]
@@ -597,7 +604,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
             "config": {"workload": "batched sweep 11x11 (n=242), 256x256 multi-disc map, [P,U,P,U,P], 64 f x "
                                    "32x32 k, both polarisations per S-matrix",
-                       "batch": B, "harmonics": "11x11",
+                       "batch": B, "harmonics": "11x11", "eig_threads": args.eig_threads or 256,
                        "precision": ("mixed: FP32 O(n^3) work, FP64 eigen-refinement and %d rounds of FP64 "
                                      "iterative refinement" % args.refine) if prec == "mixed"
                        else "fp64 (complex128) throughout",
@@ -662,6 +669,53 @@ def run_tc_product(args):
                       "max_rel_err_vs_torch_fp64": rel}), flush=True)
 
 
+def run_tf32_product(args):
+    """Times the 3xTF32 product alone: C = A B for args.tf32_product random complex64 242 x 242
+    pairs (split and product together), against torch's complex64 matmul, with the error of both
+    against an FP64 product."""
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from khepri_gb300 import _capi
+    lib = _capi.load()
+    b, n = args.tf32_product, N_MAT
+    g = torch.Generator(device="cpu").manual_seed(3)
+    A = torch.randn(b, n, n, generator=g, dtype=torch.complex64).cuda()
+    Bm = torch.randn(b, n, n, generator=g, dtype=torch.complex64).cuda()
+    C = torch.empty_like(A)
+    ws = torch.empty(lib.khp_cgemm_tf32x3_workspace(b, n, n, n), dtype=torch.uint8, device="cuda")
+
+    def call():
+        _capi.check(lib.khp_cgemm_tf32x3(b, n, n, n, _capi.ptr(A), n, n * n, _capi.ptr(Bm), n, n * n, _capi.ptr(C), n,
+                                         n * n, _capi.ptr(ws), ws.numel(), _capi.stream_ptr()), "khp_cgemm_tf32x3")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms = timed(call)
+    ms_ref = timed(lambda: torch.matmul(A, Bm))
+    ref = A.to(torch.complex128) @ Bm.to(torch.complex128)
+    scale = ref.abs().max().item()
+    err = ((C.to(torch.complex128) - ref).abs().max() / scale).item()
+    err_ref = (((A @ Bm).to(torch.complex128) - ref).abs().max() / scale).item()
+    print(json.dumps({"metric": "FP32-accurate complex products (242^3) per second", "value": b / (ms * 1e-3),
+                      "unit": "products/s", "ms_per_call": ms, "problems": b, "steps": args.steps,
+                      "warmup": args.warmup, "fp32_equivalent_tflops": 8.0 * n ** 3 * b / (ms * 1e-3) / 1e12,
+                      "max_rel_err_vs_fp64": err, "torch_complex64_ms": ms_ref,
+                      "torch_complex64_tflops": 8.0 * n ** 3 * b / (ms_ref * 1e-3) / 1e12,
+                      "torch_complex64_max_rel_err": err_ref}), flush=True)
+
+
 def main():
     args = parse()
     if args.cpu_rate_only > 0:
@@ -671,6 +725,8 @@ def main():
         run_reference(args)
     elif args.tc_product > 0:
         run_tc_product(args)
+    elif args.tf32_product > 0:
+        run_tf32_product(args)
     else:
         run_gpu(args)
 

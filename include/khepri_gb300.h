@@ -445,6 +445,20 @@ int khp_stage_timing_read(int32_t stage, double* ms, int64_t* marks);
  * bytes.
  */
 size_t khp_zgemm_fp64_tc_workspace(int64_t batch, int32_t m, int32_t n, int32_t k);
+
+/*
+ * FP32-accurate batched complex product on the tcgen05 tensor cores by 3xTF32 (no counterpart
+ * in the reference; the products of alternative.py:19-30 and 181-195, and of the mixed solve's
+ * recursion, are of this kind).  C[b] = A[b] B[b]: A complex [batch] m x k (row stride lda,
+ * batch stride a_stride, in complex elements), B k x n, C m x n, all FP32.  Every value is split
+ * into a TF32 part and a TF32 remainder, and hi hi + hi lo + lo hi accumulate in FP32 in tensor
+ * memory: the error per element is ~2^-21 * 2k * max|A row| * max|B column|.  Scratch:
+ * khp_cgemm_tf32x3_workspace(batch, m, n, k) bytes (the split operands).
+ */
+size_t khp_cgemm_tf32x3_workspace(int64_t batch, int32_t m, int32_t n, int32_t k);
+int khp_cgemm_tf32x3(int64_t batch, int32_t m, int32_t n, int32_t k, const float* A, int64_t lda, int64_t a_stride,
+                     const float* B, int64_t ldb, int64_t b_stride, float* C, int64_t ldc, int64_t c_stride,
+                     void* workspace, size_t ws_bytes, void* stream);
 int khp_zgemm_fp64_tc(int64_t batch, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda, int64_t bsA,
                       const double* B, int64_t ldb, int64_t bsB, double* C, int64_t ldc, int64_t bsC, void* workspace,
                       size_t ws_bytes, void* stream);

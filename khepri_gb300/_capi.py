@@ -96,6 +96,9 @@ _SIGNATURES = {
     "khp_tmat_multS": (ctypes.c_int, [_c_i64, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_p, _c_sz, _c_p]),
     "khp_inverse_workspace": (_c_sz, [_c_i64, _c_i32]),
     "khp_inverse": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_p, _c_i64, _c_p, _c_i64, _c_p, _c_p, _c_sz, _c_p]),
+    "khp_cgemm_tf32x3_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_i32]),
+    "khp_cgemm_tf32x3": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_i64, _c_i64, _c_p, _c_i64, _c_i64,
+                                        _c_p, _c_i64, _c_i64, _c_p, _c_sz, _c_p]),
     "khp_zgemm_fp64_tc_workspace": (_c_sz, [_c_i64, _c_i32, _c_i32, _c_i32]),
     "khp_zgemm_fp64_tc": (ctypes.c_int, [_c_i64, _c_i32, _c_i32, _c_i32, _c_p, _c_i64, _c_i64, _c_p, _c_i64, _c_i64,
                                          _c_p, _c_i64, _c_i64, _c_p, _c_sz, _c_p]),

@@ -11,8 +11,8 @@ and depend on the GPU rather than on the problem:
 
 ``tune()`` times every candidate pair on synthetic problems of each size (one smoothed, lossy
 random map per structure, the uneven-batch shapes) and writes the fastest per size to
-``tuning.json`` beside this file; the batched API applies that table (``ensure_applied``,
-``chunk_for``).  Run it on the GPU the library will use:
+``tuning.json`` beside this file; ``batch.solve_structures`` applies that table when it picks
+the chunk itself (``chunk_for``, ``tuned_team``).  Run it on the GPU the library will use:
 
     python -m khepri_gb300.autotune [--sizes 3 5 ... 17] [--out path]
 """
@@ -30,7 +30,6 @@ import torch
 from . import _capi
 
 TUNING_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
-_applied = False
 _table = None
 
 
@@ -51,15 +50,25 @@ def table():
     return _table
 
 
-def ensure_applied():
-    """Set every tuned eigensolver team size in libkhp (once per process)."""
-    global _applied
-    if _applied:
-        return
-    lib = _capi.load()
-    for n, e in table().items():
-        _capi.check(lib.khp_tune(1, int(n), int(e.get("eig_threads", 0))), "khp_tune")
-    _applied = True
+class tuned_team:
+    """Context manager: the tuned eigensolver team size for matrices of size n inside, the default
+    after.  The team size is tuned together with the matrices per call, so it applies only to
+    calls that also take ``chunk_for``'s chunk (a 128-thread team that wins at 912 matrices per
+    call loses at 456)."""
+
+    def __init__(self, n):
+        self.n = int(n)
+        self.threads = int(table().get(self.n, {}).get("eig_threads", 0))
+
+    def __enter__(self):
+        if self.threads:
+            _capi.check(_capi.load().khp_tune(1, self.n, self.threads), "khp_tune")
+        return self
+
+    def __exit__(self, *exc):
+        if self.threads:
+            _capi.load().khp_tune(1, self.n, 0)
+        return False
 
 
 def chunk_for(n, slots=1, default=256):
@@ -91,6 +100,7 @@ def _problems(p, count, rng):
 
 def _time_call(ents, wl, kp, chunk):
     from . import batch
+    # an explicit chunk: the team size set by tune() stays in force
     batch.solve_structures(ents, wl, kp, chunk=chunk, strict=False)  # warm-up (maps, workspace, modules)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -102,9 +112,8 @@ def _time_call(ents, wl, kp, chunk):
 def tune(sizes=(3, 5, 7, 9, 11, 13, 15, 17), threads=(64, 128, 256), matrices=(152, 304, 456, 912),
          budget_gb=48.0, out=TUNING_PATH, seed=0, verbose=True):
     """Time every (eig_threads, matrices) pair per size and write the fastest to ``out``."""
-    global _applied, _table
+    global _table
     lib = _capi.load()
-    _applied = True  # the table being measured, not the committed one, sets the team sizes meanwhile
     rng = np.random.default_rng(seed)
     result = {}
     for p in sizes:
@@ -134,7 +143,7 @@ def tune(sizes=(3, 5, 7, 9, 11, 13, 15, 17), threads=(64, 128, 256), matrices=(1
             "sizes": {str(k): v for k, v in sorted(result.items())}}
     with open(out, "w") as f:
         json.dump(data, f, indent=1)
-    _applied, _table = False, None
+    _table = None
     return result
 
 

@@ -8,6 +8,7 @@ that share a pixmap share one eigensolve per problem.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import functools
 
@@ -149,7 +150,6 @@ def solve_chunk_gamma(struct, plan, prob, status, epsi=1.0, epse=1.0, te=None, t
               _capi.ptr(struct.gx), _capi.ptr(struct.gy), epsi.real, epsi.imag, epse.real, epse.imag,
               _capi.ptr(prob.kp), _capi.ptr(prob.k0), npol, _capi.ptr(te), _capi.ptr(tm))
     fix = None
-    autotune.ensure_applied()
     if precision == "mixed":
         ws = engine.workspace(lib.khp_solve_batched_mixed_workspace(B, struct.nh, L, _host(plan.kinds),
                                                                      _host(plan.maps)), dev, ws_slot)
@@ -512,12 +512,14 @@ def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, la
         B = len(idx)
         prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], struct.device)
         status = torch.zeros(B, dtype=torch.int32, device=struct.device)
-        if both_pols:
-            tt, tmm = both_pol_weights(B, struct.device)
-            r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, tt, tmm, prec, refine, pmap, pdepth)
-        else:
-            r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine, pmap=pmap,
-                                     pdepth=pdepth)
+        # the autotuned chunk comes with its tuned eigensolver team size
+        with (autotune.tuned_team(struct.n) if chunk is None else contextlib.nullcontext()):
+            if both_pols:
+                tt, tmm = both_pol_weights(B, struct.device)
+                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, tt, tmm, prec, refine, pmap, pdepth)
+            else:
+                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine,
+                                         pmap=pmap, pdepth=pdepth)
         R[idx] = r.cpu().numpy()
         T[idx] = t.cpu().numpy()
         st_all[idx] = status.cpu().numpy()

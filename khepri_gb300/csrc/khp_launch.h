@@ -103,6 +103,19 @@ int mixed_modes_in_workspace(int64_t batch, int nh, int L, const int* kinds, con
                              size_t ws_bytes, const cplx<double>** W, const cplx<double>** V,
                              const cplx<double>** lam);
 
+// FP32-accurate complex products on the tcgen05 tensor cores, 3xTF32: operands split once into
+// TF32 (hi, lo) planes (elements per problem: tf32x3_a_elems / tf32x3_b_elems), then
+// C = alpha A B + beta C from the planes (err: one device int, set on a tensor-core time-out).
+size_t tf32x3_a_elems(int m, int k);
+size_t tf32x3_b_elems(int k, int n);
+int tf32x3_split_a(int64_t batch, int m, int k, const cplx<float>* A, int64_t lda, int64_t bsA, const int* aidx,
+                   float* planes, cudaStream_t s);
+int tf32x3_split_b(int64_t batch, int k, int n, const cplx<float>* B, int64_t ldb, int64_t bsB, const int* bidx,
+                   float* planes, cudaStream_t s);
+int tf32x3_from_planes(int64_t batch, int m, int n, int k, const float* Aplanes, const float* Bplanes,
+                       cplx<float> alpha, cplx<float> beta, cplx<float>* C, int64_t ldc, int64_t bsC, int* err,
+                       cudaStream_t s);
+
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 
 // Adds k to the process-wide launch counter reported by khp_launch_count().

@@ -473,6 +473,226 @@ inline unsigned grid_of(int64_t total, int threads) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + threads - 1) / threads, 152 * 32));
 }
 
+// ---- 3xTF32 products -------------------------------------------------------------------------
+// C = alpha A B + beta C for complex FP32 A (m x k) and B (k x n), as one real product over the
+// inner index i = 2t + q (q = 0: Re, 1: Im): row r of A' is A's own interleaved row r; row
+// j = 2c + p of B' (one real output column, p = 0: Re C[:, c], 1: Im) holds, at i = 2t + q, entry
+// (p, q) of [[Re b, -Im b], [Im b, Re b]] for b = B[t][c].  Every operand value is split
+// x = hi + lo with hi = x rounded to TF32 and lo = x - hi (exact in FP32) rounded to TF32, and the
+// tile accumulates hi hi' + hi lo' + lo hi' in one FP32 TMEM accumulator; the dropped lo lo' term
+// is ~2^-22 of the product and the rounding of lo ~2^-21: FP32 accuracy at the TF32 tensor rate.
+// Operand planes: [problems][2 (hi, lo)][rows padded to 128][inner padded to 32] FP32.
+
+constexpr int kTfNT = 128;    // real output columns per tile
+constexpr int kTfK = 32;      // inner slice: one 128-byte row of FP32
+constexpr int kTfStages = 2;  // slices in flight
+constexpr uint32_t kTfTmemCols = 128;
+
+inline int tf_rows(int r) { return up_to(r, kM); }
+inline int tf_inner(int k) { return up_to(2 * k, kTfK); }
+constexpr size_t tf_smem_bytes() { return 1024 + (size_t)kTfStages * 4 * kM * 128; }
+
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  hi = __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - hi));
+  lo = __uint_as_float(l);
+}
+
+// A' planes: thread per (problem, padded row, inner index); aidx optional.
+__global__ void k_tf_split_a(int64_t batch, int m, int k, const cplx<float>* __restrict__ A, int64_t lda,
+                             int64_t bsA, const int* __restrict__ aidx, int Mp, int Kp, float* __restrict__ out) {
+  const int64_t per = (int64_t)Mp * Kp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * per;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / per;
+    const int r = (int)((e % per) / Kp), i = (int)(e % Kp);
+    float x = 0.f;
+    if (r < m && i < 2 * k) {
+      const cplx<float> v = A[(aidx ? (int64_t)aidx[b] : b) * bsA + (int64_t)r * lda + (i >> 1)];
+      x = (i & 1) ? v.im : v.re;
+    }
+    float hi, lo;
+    tf32_split(x, hi, lo);
+    out[b * 2 * per + (int64_t)r * Kp + i] = hi;
+    out[b * 2 * per + per + (int64_t)r * Kp + i] = lo;
+  }
+}
+
+// B' planes through shared memory: a block (32, 8) reads a 16 x 16 tile of B (rows t, columns c;
+// coalesced along c) and writes the 32 x 32 tile of B' (rows j = 2c + p, inner i = 2t + q;
+// coalesced along i).
+__global__ void __launch_bounds__(256) k_tf_split_b(int k, int n, const cplx<float>* __restrict__ B, int64_t ldb,
+                                                    int64_t bsB, const int* __restrict__ bidx, int Np, int Kp,
+                                                    float* __restrict__ out) {
+  __shared__ cplx<float> tile[16][17];
+  const int64_t b = blockIdx.z;
+  const int c0 = blockIdx.x * 16, t0 = blockIdx.y * 16;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const cplx<float>* Bb = B + (bidx ? (int64_t)bidx[b] : b) * bsB;
+  {
+    const int tl = tid >> 4, cl = tid & 15;
+    const int t = t0 + tl, c = c0 + cl;
+    tile[tl][cl] = (t < k && c < n) ? Bb[(int64_t)t * ldb + c] : mk(0.f);
+  }
+  __syncthreads();
+  const int64_t per = (int64_t)Np * Kp;
+  float* hi_p = out + b * 2 * per;
+  float* lo_p = hi_p + per;
+  const int il = threadIdx.x;  // inner index in the tile: t = il >> 1, q = il & 1
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int jl = threadIdx.y + 8 * u;  // output row in the tile: c = jl >> 1, p = jl & 1
+    const cplx<float> v = tile[il >> 1][jl >> 1];
+    const int p = jl & 1, q = il & 1;
+    const float x = p == 0 ? (q == 0 ? v.re : -v.im) : (q == 0 ? v.im : v.re);
+    float hi, lo;
+    tf32_split(x, hi, lo);
+    const int64_t o = (int64_t)(2 * c0 + jl) * Kp + 2 * t0 + il;
+    hi_p[o] = hi;
+    lo_p[o] = lo;
+  }
+}
+
+// Instruction descriptor of kind::tf32: TF32 A and B (K-major), FP32 accumulator, M x N.
+__host__ __device__ constexpr uint32_t instr_desc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+// grid: (Np / 128, Mp / 128, problems of this launch).  Warp 0 lane 0 loads each 32-wide inner
+// slice's four tiles (A hi, A lo, B hi, B lo) with TMA into a ring of kTfStages buffers, warp 1
+// lane 0 issues the 3 x 4 MMAs of the slice (K = 8 each) and releases the buffer through its
+// empty mbarrier, and all four warps run the epilogue from TMEM.  Every wait is bounded: on
+// time-out the CTA sets the error flag, frees TMEM and returns.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_tf32x3(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int m, int n, int Kp,
+             cplx<float>* C, int64_t ldc, int64_t bsC, cplx<float> alpha, cplx<float> beta, int use_beta, int* err) {
+  constexpr uint32_t kTile = kM * 128;  // 128 rows x 32 FP32 (A and B tiles alike, kTfNT == kM)
+  constexpr uint32_t kStage = 4 * kTile;
+  constexpr uint32_t kIdesc = instr_desc_tf32(kM, kTfNT);
+  extern __shared__ unsigned char dsm_raw[];
+  __shared__ __align__(8) uint64_t full[kTfStages], empty[kTfStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_err;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t base = (smem_u32(dsm_raw) + 1023u) & ~1023u;
+  const int64_t b = blockIdx.z;
+  const int S = Kp / kTfK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTfTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+#pragma unroll
+    for (int q = 0; q < kTfStages; ++q) {
+      mbar_init(smem_u32(&full[q]), 1);
+      mbar_init(smem_u32(&empty[q]), 1);
+    }
+    mbar_init(smem_u32(&done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    s_err = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    for (int sl = 0; sl < S && !s_err; ++sl) {
+      const int st = sl % kTfStages;
+      if (!mbar_wait(smem_u32(&empty[st]), (uint32_t)(((sl / kTfStages) & 1) ^ 1))) {
+        atomicExch(&s_err, 1);
+        break;
+      }
+      const uint32_t buf = base + st * kStage;
+      mbar_expect_tx(smem_u32(&full[st]), kStage);
+      tma_load_3d(buf, &tmA, sl * kTfK, blockIdx.y * kM, (int)b * 2, smem_u32(&full[st]));
+      tma_load_3d(buf + kTile, &tmA, sl * kTfK, blockIdx.y * kM, (int)b * 2 + 1, smem_u32(&full[st]));
+      tma_load_3d(buf + 2 * kTile, &tmB, sl * kTfK, blockIdx.x * kTfNT, (int)b * 2, smem_u32(&full[st]));
+      tma_load_3d(buf + 3 * kTile, &tmB, sl * kTfK, blockIdx.x * kTfNT, (int)b * 2 + 1, smem_u32(&full[st]));
+    }
+  } else if (warp == 1 && lane == 0) {
+    for (int sl = 0; sl < S && !s_err; ++sl) {
+      const int st = sl % kTfStages;
+      if (!mbar_wait(smem_u32(&full[st]), (uint32_t)((sl / kTfStages) & 1))) {
+        atomicExch(&s_err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t buf = base + st * kStage;
+      const uint64_t ahi = smem_desc(buf), alo = smem_desc(buf + kTile);
+      const uint64_t bhi = smem_desc(buf + 2 * kTile), blo = smem_desc(buf + 3 * kTile);
+#pragma unroll
+      for (int kk = 0; kk < kTfK / 8; ++kk) {
+        const uint64_t o = (uint64_t)(2 * kk);  // 32 bytes per K = 8 step, in 16-byte units
+        mma_tf32(tmem, ahi + o, bhi + o, kIdesc, (sl == 0 && kk == 0) ? 0u : 1u);
+        mma_tf32(tmem, ahi + o, blo + o, kIdesc, 1u);
+        mma_tf32(tmem, alo + o, bhi + o, kIdesc, 1u);
+      }
+      mma_commit(smem_u32(&empty[st]));
+    }
+    mma_commit(smem_u32(&done));
+  }
+  __syncwarp();
+  const bool finished = mbar_wait(smem_u32(&done), 0u);
+  if (!finished) atomicExch(&s_err, 1);
+  __syncthreads();
+  if (!s_err) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const int r = blockIdx.y * kM + tid;  // TMEM lane (32 warp + lane) = tile row
+    cplx<float>* Cb = C + b * bsC;
+    const bool plain = !use_beta && alpha.re == 1.f && alpha.im == 0.f;
+    for (int cc = 0; cc < kTfNT; cc += 16) {
+      uint32_t v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (r >= m) continue;
+#pragma unroll
+      for (int q = 0; q < 16; q += 2) {
+        const int c = (blockIdx.x * kTfNT + cc + q) >> 1;
+        if (c >= n) continue;
+        const cplx<float> val = mk(__uint_as_float(v[q]), __uint_as_float(v[q + 1]));
+        cplx<float>* dst = Cb + (int64_t)r * ldc + c;
+        if (plain) {
+          *dst = val;
+        } else {
+          cplx<float> o = alpha * val;
+          if (use_beta) o += beta * *dst;
+          *dst = o;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTfTmemCols));
+  if (tid == 0 && s_err) atomicExch(err, 1);
+}
+
+// 3-D FP32 operand planes [planes][rows][Kp] with 32 x 128 boxes, 128-byte swizzle.
+bool encode_planes_map(CUtensorMap* map, const float* base, int Kp, int rows, int64_t planes) {
+  const EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
+  const cuuint64_t strides[2] = {(cuuint64_t)Kp * 4, (cuuint64_t)rows * Kp * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)kTfK, (cuuint32_t)kM, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 // Largest inner size (2k padded to 64) for which the levels that matter stay exact.
@@ -536,6 +756,57 @@ int tc_product(int64_t batch, int m, int n, int k, const cplx<TI>* A, int64_t ld
   return cuda_status();
 }
 
+size_t tf32x3_a_elems(int m, int k) { return 2 * (size_t)tf_rows(m) * tf_inner(k); }
+size_t tf32x3_b_elems(int k, int n) { return 2 * (size_t)up_to(2 * n, kTfNT) * tf_inner(k); }
+
+int tf32x3_split_a(int64_t batch, int m, int k, const cplx<float>* A, int64_t lda, int64_t bsA, const int* aidx,
+                   float* planes, cudaStream_t s) {
+  const int Mp = tf_rows(m), Kp = tf_inner(k);
+  k_tf_split_a<<<grid_of(batch * Mp * Kp, 256), 256, 0, s>>>(batch, m, k, A, lda, bsA, aidx, Mp, Kp, planes);
+  count_launches(1);
+  return cuda_status();
+}
+
+int tf32x3_split_b(int64_t batch, int k, int n, const cplx<float>* B, int64_t ldb, int64_t bsB, const int* bidx,
+                   float* planes, cudaStream_t s) {
+  const int Np = up_to(2 * n, kTfNT), Kp = tf_inner(k);
+  const int64_t per = (int64_t)2 * Np * Kp;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned z = (unsigned)std::min<int64_t>(batch - off, 65535);
+    k_tf_split_b<<<dim3((unsigned)(Np / 32), (unsigned)(Kp / 32), z), dim3(32, 8), 0, s>>>(k, n, bidx ? B : B + off * bsB, ldb, bsB, bidx ? bidx + off : nullptr, Np, Kp,
+                                        planes + off * per);
+    count_launches(1);
+  }
+  return cuda_status();
+}
+
+int tf32x3_from_planes(int64_t batch, int m, int n, int k, const float* Aplanes, const float* Bplanes,
+                       cplx<float> alpha, cplx<float> beta, cplx<float>* C, int64_t ldc, int64_t bsC, int* err,
+                       cudaStream_t s) {
+  const int Mp = tf_rows(m), Np = up_to(2 * n, kTfNT), Kp = tf_inner(k);
+  if (m < 1 || n < 1 || k < 1) return KHP_ERR_INVALID_ARG;
+  const size_t smem = tf_smem_bytes();
+  if (cudaFuncSetAttribute(k_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return KHP_ERR_CUDA;
+  if (!err) return KHP_ERR_WORKSPACE;
+  const bool use_beta = !(beta.re == 0.f && beta.im == 0.f);
+  if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return KHP_ERR_CUDA;
+  const int64_t per_a = 2 * (int64_t)Mp * Kp, per_b = 2 * (int64_t)Np * Kp;
+  for (int64_t off = 0; off < batch; off += 65535) {
+    const unsigned z = (unsigned)std::min<int64_t>(batch - off, 65535);
+    CUtensorMap tmA, tmB;
+    if (!encode_planes_map(&tmA, Aplanes + off * per_a, Kp, Mp, 2 * (int64_t)z) ||
+        !encode_planes_map(&tmB, Bplanes + off * per_b, Kp, Np, 2 * (int64_t)z))
+      return KHP_ERR_CUDA;
+    k_tf32x3<<<dim3(Np / kTfNT, Mp / kM, z), kThreads, smem, s>>>(tmA, tmB, m, n, Kp, C + off * bsC, ldc, bsC, alpha,
+                                                                   beta, use_beta ? 1 : 0, err);
+    count_launches(1);
+  }
+  k_tc_poison<float><<<grid_of(batch, 128), 128, 0, s>>>(err, batch, C, bsC);
+  count_launches(1);
+  return cuda_status();
+}
+
 template int tc_product<8, double, double>(int64_t, int, int, int, const cplx<double>*, int64_t, int64_t, const int*,
                                            const cplx<double>*, int64_t, int64_t, const int*, cplx<double>,
                                            cplx<double>, cplx<double>*, int64_t, int64_t, const OzakiWs&,
@@ -545,3 +816,39 @@ template int tc_product<4, float, float>(int64_t, int, int, int, const cplx<floa
                                          cplx<float>*, int64_t, int64_t, const OzakiWs&, cudaStream_t);
 
 }  // namespace khp
+
+extern "C" {
+
+size_t khp_cgemm_tf32x3_workspace(int64_t batch, int32_t m, int32_t n, int32_t k) {
+  if (batch < 0 || m < 1 || n < 1 || k < 1) return 0;
+  const size_t a = (sizeof(float) * khp::tf32x3_a_elems(m, k) * (size_t)batch + 255) & ~size_t(255);
+  const size_t b = (sizeof(float) * khp::tf32x3_b_elems(k, n) * (size_t)batch + 255) & ~size_t(255);
+  return a + b + 256;
+}
+
+int khp_cgemm_tf32x3(int64_t batch, int32_t m, int32_t n, int32_t k, const float* A, int64_t lda, int64_t a_stride,
+                     const float* B, int64_t ldb, int64_t b_stride, float* C, int64_t ldc, int64_t c_stride,
+                     void* workspace, size_t ws_bytes, void* stream) {
+  using namespace khp;
+  if (batch < 0 || m < 1 || n < 1 || k < 1 || !A || !B || !C || lda < k || ldb < n || ldc < n || a_stride < 0 ||
+      b_stride < 0 || c_stride < 0)
+    return KHP_ERR_INVALID_ARG;
+  if (batch == 0) return KHP_OK;
+  if (!workspace || ws_bytes < khp_cgemm_tf32x3_workspace(batch, m, n, k)) return KHP_ERR_WORKSPACE;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char* w = static_cast<char*>(workspace);
+  float* ap = reinterpret_cast<float*>(w);
+  const size_t a = (sizeof(float) * tf32x3_a_elems(m, k) * (size_t)batch + 255) & ~size_t(255);
+  float* bp = reinterpret_cast<float*>(w + a);
+  const size_t b = (sizeof(float) * tf32x3_b_elems(k, n) * (size_t)batch + 255) & ~size_t(255);
+  int* err = reinterpret_cast<int*>(w + a + b);
+  const auto* Ac = reinterpret_cast<const cplx<float>*>(A);
+  const auto* Bc = reinterpret_cast<const cplx<float>*>(B);
+  auto* Cc = reinterpret_cast<cplx<float>*>(C);
+  int st = tf32x3_split_a(batch, m, k, Ac, lda, a_stride, nullptr, ap, s);
+  if (!st) st = tf32x3_split_b(batch, k, n, Bc, ldb, b_stride, nullptr, bp, s);
+  if (!st) st = tf32x3_from_planes(batch, m, n, k, ap, bp, mk(1.f), mk(0.f), Cc, ldc, c_stride, err, s);
+  return st;
+}
+
+}  // extern "C"

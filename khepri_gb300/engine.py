@@ -245,6 +245,25 @@ class StructureGPU:
         return entry
 
 
+# Pinned host copies of inputs whose host-to-device copies are still queued, with the event that
+# follows them on the stream.  A pinned buffer must outlive its copy (released early, the next
+# staging could take the same buffer and overwrite the bytes before the device reads them), so
+# each is held here until its event has completed.
+_STAGED = []
+
+
+def _to_device_async(arrays, device):
+    """Copies of host numpy arrays on ``device``, staged through pinned memory and queued on the
+    current stream without a host wait; the staging buffers are kept until their copies ran."""
+    pinned = [torch.from_numpy(a).pin_memory() for a in arrays]
+    out = [h.to(device, non_blocking=True) for h in pinned]
+    ev = torch.cuda.Event()
+    ev.record()
+    _STAGED[:] = [(h, e) for h, e in _STAGED if not e.query()]
+    _STAGED.append((pinned, ev))
+    return out
+
+
 @dataclass
 class Problems:
     """Device arrays describing a batch of problems."""
@@ -273,16 +292,13 @@ class Problems:
         te = np.broadcast_to(np.asarray(te, dtype=complex), (B,))
         tm = np.broadcast_to(np.asarray(tm, dtype=complex), (B,))
         d = torch.device(device)
-
-        def up(a, dtype):
-            # staged through pinned host memory, copied on the current stream without a host wait
-            h = torch.from_numpy(np.array(a, dtype=dtype))  # a writable contiguous copy
-            if d.type == "cuda":
-                return h.pin_memory().to(d, non_blocking=True)
-            return h.to(d)
-
-        return cls(k0=up(TWOPI / wl, np.float64), kp=up(kpa, np.complex128), te=up(te, np.complex128),
-                   tm=up(tm, np.complex128))
+        # row-major copies: an input built by broadcasting can be column-major (kp of the twisted
+        # path), and the kernels read kp as [B][2]
+        host = [np.array(TWOPI / wl, dtype=np.float64, order="C"), np.array(kpa, dtype=np.complex128, order="C"),
+                np.array(te, dtype=np.complex128, order="C"), np.array(tm, dtype=np.complex128, order="C")]
+        if d.type != "cuda":
+            return cls(*(torch.from_numpy(h).to(d) for h in host))
+        return cls(*_to_device_async(host, d))
 
 
 @dataclass

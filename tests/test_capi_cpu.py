@@ -97,3 +97,16 @@ def test_no_gpu_means_loud_failure():
     from khepri_gb300 import Crystal, KhpError
     with pytest.raises(KhpError):
         Crystal((3, 3))
+
+
+def test_problem_arrays_are_row_major():
+    """Problems.make copies its inputs row-major, whatever their memory order (a kp built by
+    broadcasting against a transposed array is column-major; the kernels read it as [B][2])."""
+    import numpy as np
+    from khepri_gb300 import engine
+    g = np.random.default_rng(1).standard_normal((2, 9))
+    kp = (np.array([[0.3, 0.1]], dtype=complex)[:, None, :] + g.T[None, :, :]).reshape(9, 2)
+    assert not kp.flags["C_CONTIGUOUS"]
+    p = engine.Problems.make(np.ones(9), kp, 1.0, 0.0, "cpu")
+    assert p.kp.is_contiguous() and p.kp.stride() == (2, 1)
+    np.testing.assert_array_equal(p.kp.numpy(), kp)
