@@ -93,6 +93,9 @@ def parse():
                     help="problems per call (456 = 3 x 152 SMs: three eigensolver CTAs per SM)")
     ap.add_argument("--eig-threads", type=int, default=0,
                     help="eigensolver threads per CTA for the sweep's 242 x 242 matrices (khp_tune; 0 = default)")
+    ap.add_argument("--tf32-min-n", type=int, default=-1,
+                    help="smallest n whose recursion products run as 3xTF32 on the tensor cores (khp_tune; 0 = "
+                         "never; -1 = the library default)")
     ap.add_argument("--impl", default="khepri_gb300", choices=["khepri_gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=6)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -102,6 +105,9 @@ def parse():
                     help="inverse-design structures (x 16 frequencies) for the solve+grad measurement (0 = skip)")
     ap.add_argument("--uneven", type=int, default=1024,
                     help="uneven structures (config 3's shapes) for the many-structure measurement (0 = skip)")
+    ap.add_argument("--twisted7", type=int, default=4,
+                    help="twisted-bilayer problems at 7x7 base harmonics (n = 4802) for the extended-crystal "
+                         "measurement (0 = skip)")
     ap.add_argument("--twisted", type=int, default=16,
                     help="twisted-bilayer problems (5x5 base harmonics, n = 1250) for the extended-crystal measurement")
     ap.add_argument("--tc-product", type=int, default=0,
@@ -391,6 +397,27 @@ def bench_twisted(args):
             "max_abs_R_plus_T_minus_1": float(np.abs(R + T - 1).max()), "problems_with_status": int((st != 0).sum())}
 
 
+def bench_twisted7(args):
+    """Twisted bilayers at 7x7 base harmonics (product expansion of 2401 orders, n = 4802): disc
+    gratings eps 12 in 1 (64x64 map, r 0.3, depth 0.3) on each side of a gap (d 0.3), twist 13
+    deg, frequencies 0.4-0.7 at normal incidence, both polarisations; host wall clock through
+    TwistedBilayer.solve_rt after one untimed problem."""
+    from khepri_gb300 import twisted
+    if args.twisted7 <= 0:
+        return None
+    x = np.linspace(-0.5, 0.5, 64)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    disc = np.where(X ** 2 + Y ** 2 < 0.3 ** 2, 12.0, 1.0)
+    tw = twisted.TwistedBilayer((7, 7), "square", np.deg2rad(13.0), [("pixmap", disc, 0.3)],
+                                [("uniform", 1.0, 0.3)], [("pixmap", disc, 0.3)])
+    f = np.linspace(0.4, 0.7, args.twisted7)
+    tw.solve_rt(1.0 / f[:1], np.zeros((1, 2)), both_pols=True)
+    res, t = _timed(lambda: tw.solve_rt(1.0 / f, np.zeros((len(f), 2)), both_pols=True, chunk=4, strict=False))
+    R, T, st = res
+    return {"solves_per_s": len(f) / t, "problems": len(f), "seconds": t, "n_extended": 4802,
+            "max_abs_R_plus_T_minus_1": float(np.abs(R + T - 1).max()), "problems_with_status": int((st != 0).sum())}
+
+
 def run_gpu(args):
     import torch
 
@@ -409,6 +436,8 @@ def run_gpu(args):
     lib = _capi.load()
     if args.eig_threads:
         _capi.check(lib.khp_tune(1, N_MAT, args.eig_threads), "khp_tune")
+    if args.tf32_min_n >= 0:
+        _capi.check(lib.khp_tune(2, 1, args.tf32_min_n), "khp_tune")
     st = workloads.batched_structure(0)
     wl_all, kp_all = workloads.batched_problems()
     P = wl_all.shape[0]
@@ -592,11 +621,12 @@ def run_gpu(args):
                "one_thread": {"value": one, "unit": UNIT, "cores": 1,
                               "sample": "the same problems, BLAS and OpenMP pinned to one thread"}}
 
-    grad_info = uneven_info = twisted_info = None
+    grad_info = uneven_info = twisted_info = twisted7_info = None
     if rank == 0:
         grad_info = bench_grad(args, struct, st, wl_all, kp_all)
         uneven_info = bench_uneven(args)
         twisted_info = bench_twisted(args)
+        twisted7_info = bench_twisted7(args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -605,6 +635,8 @@ def run_gpu(args):
             "config": {"workload": "batched sweep 11x11 (n=242), 256x256 multi-disc map, [P,U,P,U,P], 64 f x "
                                    "32x32 k, both polarisations per S-matrix",
                        "batch": B, "harmonics": "11x11", "eig_threads": args.eig_threads or 256,
+                       "recursion_products": ("3xTF32 tensor cores" if (args.tf32_min_n < 0 and N_MAT >= 128)
+                                              or 0 < args.tf32_min_n <= N_MAT else "FP32 pipe"),
                        "precision": ("mixed: FP32 O(n^3) work, FP64 eigen-refinement and %d rounds of FP64 "
                                      "iterative refinement" % args.refine) if prec == "mixed"
                        else "fp64 (complex128) throughout",
@@ -618,7 +650,8 @@ def run_gpu(args):
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
                        "repairs": repairs,
-                       "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info},
+                       "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info,
+                       "twisted_7x7": twisted7_info},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": world * len(e2e_idx) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.steps, "repairs": e2e_repairs,

@@ -51,8 +51,12 @@ const char* khp_status_string(int code);
  * do not depend on it; the speed does (small matrices leave a 256-thread team mostly idle).  Set
  * it before the launches it should affect (it is read when a call enqueues its kernels).
  * khepri_gb300.autotune measures the choices and writes the table the Python API applies.
+ * param KHP_TUNE_TF32_MIN_N (n ignored): the mixed solve's FP32 recursion products of size
+ * n >= value run as 3xTF32 on the tensor cores (khp_cgemm_tf32x3's method), smaller ones on the
+ * FP32 pipe; 0 = never (default 128).
  */
 #define KHP_TUNE_EIG_THREADS 1
+#define KHP_TUNE_TF32_MIN_N 2
 int khp_tune(int32_t param, int32_t n, int32_t value);
 
 /*

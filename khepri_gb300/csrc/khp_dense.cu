@@ -23,6 +23,16 @@ int eig_threads(int n) {
   return v > 0 ? v : kTeamThreads;
 }
 
+}  // namespace
+
+// Smallest matrix size whose FP32 products in the mixed solve's recursion run as 3xTF32 on the
+// tensor cores (khp_tune KHP_TUNE_TF32_MIN_N; 0 = never).  Below it the 128-row tiles are mostly
+// padding and the SIMT product is faster.
+int g_tf32_min_n = 128;
+bool use_tf32_products(int n) { return g_tf32_min_n > 0 && n >= g_tf32_min_n; }
+
+namespace {
+
 template <typename T>
 __global__ void __launch_bounds__(kTeamThreads) k_getrf(int n, cplx<T>* A, int64_t lda, int64_t bsA, int* piv,
                                                          int* info) {
@@ -919,6 +929,11 @@ extern "C" {
 
 int khp_tune(int32_t param, int32_t n, int32_t value) {
   using namespace khp;
+  if (param == KHP_TUNE_TF32_MIN_N) {
+    if (value < 0) return KHP_ERR_INVALID_ARG;
+    g_tf32_min_n = value;
+    return KHP_OK;
+  }
   if (param != KHP_TUNE_EIG_THREADS || n < 1 || n > kTuneMaxN) return KHP_ERR_INVALID_ARG;
   if (value != 0 && (value < 32 || value > kTeamThreads || value % 32 != 0)) return KHP_ERR_INVALID_ARG;
   g_eig_threads[n] = value;

@@ -111,10 +111,13 @@ size_t tf32x3_b_elems(int k, int n);
 int tf32x3_split_a(int64_t batch, int m, int k, const cplx<float>* A, int64_t lda, int64_t bsA, const int* aidx,
                    float* planes, cudaStream_t s);
 int tf32x3_split_b(int64_t batch, int k, int n, const cplx<float>* B, int64_t ldb, int64_t bsB, const int* bidx,
-                   float* planes, cudaStream_t s);
+                   cplx<float> shift, float* planes, cudaStream_t s);  // planes of B + shift I
 int tf32x3_from_planes(int64_t batch, int m, int n, int k, const float* Aplanes, const float* Bplanes,
                        cplx<float> alpha, cplx<float> beta, cplx<float>* C, int64_t ldc, int64_t bsC, int* err,
                        cudaStream_t s);
+
+// Whether the mixed solve's n x n FP32 products take the 3xTF32 tensor-core path (khp_tune).
+bool use_tf32_products(int n);
 
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 

@@ -957,6 +957,11 @@ struct MixedPlan {
   cd *M64, *MW64, *CW64, *Ct64, *mu64, *mu64b;
   int *pair, *nearest;  // eigen-refinement clusters: label and rank of every column, [bm][n]
   int *csz, *memb;      // cluster size per column [bm][n]; members [bm][n][kClusterMax]
+  // 3xTF32 recursion products: split A operands that stay fixed through the recursion (W^-1, Q0,
+  // W, Vt of every slot), scratch splits of the varying A and of B, the tensor-core error flag
+  float *tfAc, *tfA, *tfB;
+  int* tferr;
+  size_t tfa, tfb;  // elements per problem
   cf* xc;               // column of the cluster transform per column, [bm][n][kClusterMax]
   int* piv;
   std::vector<int*> midx;  // per map slot: the map index of every problem
@@ -1047,6 +1052,17 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   }
   p.inc = a.take<M2>(batch * nh * 4);
   p.trn = a.take<M2>(batch * nh * 4);
+  p.tfAc = p.tfA = p.tfB = nullptr;
+  p.tferr = nullptr;
+  p.tfa = p.tfb = 0;
+  if (use_tf32_products((int)n)) {
+    p.tfa = tf32x3_a_elems((int)n, (int)n);
+    p.tfb = tf32x3_b_elems((int)n, (int)n);
+    p.tfAc = a.take<float>((size_t)4 * S * batch * p.tfa);
+    p.tfA = a.take<float>(batch * p.tfa);
+    p.tfB = a.take<float>(batch * p.tfb);
+    p.tferr = a.take<int>(1);
+  }
   p.gam = a.take<cf>((size_t)(L + 1) * batch * nn);
   p.F = a.take<cf>(batch * nn);
   p.Gb = a.take<cf>(batch * nn);
@@ -1331,35 +1347,55 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   // ---- 2. FP32 backward recursion, keeping every factor (explicit inverses: every O(n^3) step
   //         is then a blocked factorisation or a tiled product) ----
   auto gam = [&](int g) { return p.gam + (int64_t)g * batch * nn; };
+  // The recursion's n x n FP32 products: 3xTF32 on the tensor cores (the split of every fixed A
+  // operand made once per call), or the FP32 tiled product.  C = A (B + shift I).
+  const bool tf = p.tfAc != nullptr;
+  auto fixed_a = [&](int which, int m) { return p.tfAc + ((size_t)which * S + m) * batch * p.tfa; };
+  if (tf) {
+    for (int m = 0; m < S; ++m) {
+      MX_TRY(tf32x3_split_a(batch, n, n, p.Wi[m], n, nn, nullptr, fixed_a(0, m), s));
+      MX_TRY(tf32x3_split_a(batch, n, n, p.Q0[m], n, nn, nullptr, fixed_a(1, m), s));
+      MX_TRY(tf32x3_split_a(batch, n, n, p.W32[m], n, nn, nullptr, fixed_a(2, m), s));
+      MX_TRY(tf32x3_split_a(batch, n, n, p.Vt[m], n, nn, nullptr, fixed_a(3, m), s));
+    }
+  }
+  auto prod_fixed = [&](int which, int m, const cf* A, const cf* B, cf shift, cf* C) -> int {
+    if (!tf) return launch_gemm<float>(batch, n, n, n, one, A, n, nn, B, n, nn, zero, C, n, nn, s, nullptr, nullptr,
+                                       shift);
+    const int st = tf32x3_split_b(batch, n, n, B, n, nn, nullptr, shift, p.tfB, s);
+    return st ? st : tf32x3_from_planes(batch, n, n, n, fixed_a(which, m), p.tfB, one, zero, C, n, nn, p.tferr, s);
+  };
+  auto prod = [&](const cf* A, const cf* B, cf* C) -> int {
+    if (!tf) return launch_gemm<float>(batch, n, n, n, one, A, n, nn, B, n, nn, zero, C, n, nn, s);
+    int st = tf32x3_split_a(batch, n, n, A, n, nn, nullptr, p.tfA, s);
+    if (!st) st = tf32x3_split_b(batch, n, n, B, n, nn, nullptr, zero, p.tfB, s);
+    return st ? st : tf32x3_from_planes(batch, n, n, n, p.tfA, p.tfB, one, zero, C, n, nn, p.tferr, s);
+  };
   MX_EW(k_gamma_from_blocks<float>, batch * nn, batch, nh, p.trn, 0, gam(L));
   for (int l = L - 1; l >= 0; --l) {
     cf* G = gam(l + 1);
     if (kinds[l] != 1) {
       MX_TRY(launch_i_minus_sg<float>(batch, nh, p.blocks[l], G, p.lu32, s));
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, G, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));
+      MX_TRY(prod(G, p.inv1[l], p.zr[l]));
       MX_TRY(launch_sandwich<float>(batch, nh, p.blocks[l], p.zr[l], gam(l), s));
     } else {
       const int m = slot[l];
-      // F = Wi (G + I), Gb = Q0 (G - I): the identity added to G's diagonal as the tiles load
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Wi[m], n, nn, G, n, nn, zero, p.F, n, nn, s, nullptr, nullptr,
-                                one));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Q0[m], n, nn, G, n, nn, zero, p.Gb, n, nn, s, nullptr, nullptr,
-                                mone));
+      // F = Wi (G + I), Gb = Q0 (G - I): the identity added to G's diagonal as it is read
+      MX_TRY(prod_fixed(0, m, p.Wi[m], G, one, p.F));
+      MX_TRY(prod_fixed(1, m, p.Q0[m], G, mone, p.Gb));
       MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.F, p.Gb, p.lu32);
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv1[l], n, nn, p.piv, status, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.F, n, nn, p.inv1[l], n, nn, zero, p.zr[l], n, nn, s));  // rho
+      MX_TRY(prod(p.F, p.inv1[l], p.zr[l]));  // rho
       MX_TRY(launch_copy<float>(batch, n, n, p.zr[l], n, nn, p.F, n, nn, s));
       MX_EW(k_xvec<float>, batch * n, batch, n, p.lam32[m], depth_of(l), k0, p.xv);
       MX_EW(k_xmx_t<float>, batch * nn, batch, n, p.xv, p.F);
       // Gb = W (F + I), P = Vt (F - I)
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.W32[m], n, nn, p.F, n, nn, zero, p.Gb, n, nn, s, nullptr,
-                                nullptr, one));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Vt[m], n, nn, p.F, n, nn, zero, p.P, n, nn, s, nullptr,
-                                nullptr, mone));
+      MX_TRY(prod_fixed(2, m, p.W32[m], p.F, one, p.Gb));
+      MX_TRY(prod_fixed(3, m, p.Vt[m], p.F, mone, p.P));
       MX_EW(k_diff_sum<float>, batch * nn, batch * nn, p.Gb, p.P, p.lu32);
       MX_TRY(launch_inverse_blocked<float>(batch, n, p.lu32, n, nn, p.inv2[l], n, nn, p.piv, status, s));
-      MX_TRY(launch_gemm<float>(batch, n, n, n, one, p.Gb, n, nn, p.inv2[l], n, nn, zero, gam(l), n, nn, s));
+      MX_TRY(prod(p.Gb, p.inv2[l], gam(l)));
     }
   }
   MX_TRY(launch_i_minus_sg<float>(batch, nh, p.inc, gam(0), p.lu32, s));

@@ -485,7 +485,7 @@ inline unsigned grid_of(int64_t total, int threads) {
 
 constexpr int kTfNT = 128;    // real output columns per tile
 constexpr int kTfK = 32;      // inner slice: one 128-byte row of FP32
-constexpr int kTfStages = 2;  // slices in flight
+constexpr int kTfStages = 3;  // slices in flight (3 x 64 KB of shared memory)
 constexpr uint32_t kTfTmemCols = 128;
 
 inline int tf_rows(int r) { return up_to(r, kM); }
@@ -500,32 +500,33 @@ __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
-// A' planes: thread per (problem, padded row, inner index); aidx optional.
-__global__ void k_tf_split_a(int64_t batch, int m, int k, const cplx<float>* __restrict__ A, int64_t lda,
-                             int64_t bsA, const int* __restrict__ aidx, int Mp, int Kp, float* __restrict__ out) {
+// A' planes: a block per (problem, padded row) at a time, threads along the inner index (A's row
+// read as consecutive floats, re and im interleaved exactly as i = 2t + q); aidx optional.
+__global__ void __launch_bounds__(256) k_tf_split_a(int64_t batch, int m, int k, const cplx<float>* __restrict__ A,
+                                                    int64_t lda, int64_t bsA, const int* __restrict__ aidx, int Mp,
+                                                    int Kp, float* __restrict__ out) {
   const int64_t per = (int64_t)Mp * Kp;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * per;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / per;
-    const int r = (int)((e % per) / Kp), i = (int)(e % Kp);
-    float x = 0.f;
-    if (r < m && i < 2 * k) {
-      const cplx<float> v = A[(aidx ? (int64_t)aidx[b] : b) * bsA + (int64_t)r * lda + (i >> 1)];
-      x = (i & 1) ? v.im : v.re;
+  for (int64_t row = blockIdx.x; row < batch * Mp; row += gridDim.x) {
+    const int64_t b = row / Mp;
+    const int r = (int)(row - b * Mp);
+    const float* src = reinterpret_cast<const float*>(A + (aidx ? (int64_t)aidx[b] : b) * bsA + (int64_t)r * lda);
+    float* hi_p = out + b * 2 * per + (int64_t)r * Kp;
+    for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
+      const float x = (r < m && i < 2 * k) ? src[i] : 0.f;
+      float hi, lo;
+      tf32_split(x, hi, lo);
+      hi_p[i] = hi;
+      hi_p[per + i] = lo;
     }
-    float hi, lo;
-    tf32_split(x, hi, lo);
-    out[b * 2 * per + (int64_t)r * Kp + i] = hi;
-    out[b * 2 * per + per + (int64_t)r * Kp + i] = lo;
   }
 }
 
-// B' planes through shared memory: a block (32, 8) reads a 16 x 16 tile of B (rows t, columns c;
-// coalesced along c) and writes the 32 x 32 tile of B' (rows j = 2c + p, inner i = 2t + q;
-// coalesced along i).
+// B' planes of B + shift I through shared memory: a block (32, 8) reads a 16 x 16 tile of B (rows
+// t, columns c; coalesced along c) and writes the 32 x 32 tile of B' (rows j = 2c + p, inner
+// i = 2t + q; coalesced along i).
 __global__ void __launch_bounds__(256) k_tf_split_b(int k, int n, const cplx<float>* __restrict__ B, int64_t ldb,
                                                     int64_t bsB, const int* __restrict__ bidx, int Np, int Kp,
-                                                    float* __restrict__ out) {
+                                                    cplx<float> shift, float* __restrict__ out) {
   __shared__ cplx<float> tile[16][17];
   const int64_t b = blockIdx.z;
   const int c0 = blockIdx.x * 16, t0 = blockIdx.y * 16;
@@ -534,7 +535,9 @@ __global__ void __launch_bounds__(256) k_tf_split_b(int k, int n, const cplx<flo
   {
     const int tl = tid >> 4, cl = tid & 15;
     const int t = t0 + tl, c = c0 + cl;
-    tile[tl][cl] = (t < k && c < n) ? Bb[(int64_t)t * ldb + c] : mk(0.f);
+    cplx<float> v = (t < k && c < n) ? Bb[(int64_t)t * ldb + c] : mk(0.f);
+    if (t == c && t < k && c < n) v += shift;  // B + shift I
+    tile[tl][cl] = v;
   }
   __syncthreads();
   const int64_t per = (int64_t)Np * Kp;
@@ -762,19 +765,20 @@ size_t tf32x3_b_elems(int k, int n) { return 2 * (size_t)up_to(2 * n, kTfNT) * t
 int tf32x3_split_a(int64_t batch, int m, int k, const cplx<float>* A, int64_t lda, int64_t bsA, const int* aidx,
                    float* planes, cudaStream_t s) {
   const int Mp = tf_rows(m), Kp = tf_inner(k);
-  k_tf_split_a<<<grid_of(batch * Mp * Kp, 256), 256, 0, s>>>(batch, m, k, A, lda, bsA, aidx, Mp, Kp, planes);
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(batch * Mp, 152 * 16));
+  k_tf_split_a<<<blocks, 256, 0, s>>>(batch, m, k, A, lda, bsA, aidx, Mp, Kp, planes);
   count_launches(1);
   return cuda_status();
 }
 
 int tf32x3_split_b(int64_t batch, int k, int n, const cplx<float>* B, int64_t ldb, int64_t bsB, const int* bidx,
-                   float* planes, cudaStream_t s) {
+                   cplx<float> shift, float* planes, cudaStream_t s) {
   const int Np = up_to(2 * n, kTfNT), Kp = tf_inner(k);
   const int64_t per = (int64_t)2 * Np * Kp;
   for (int64_t off = 0; off < batch; off += 65535) {
     const unsigned z = (unsigned)std::min<int64_t>(batch - off, 65535);
-    k_tf_split_b<<<dim3((unsigned)(Np / 32), (unsigned)(Kp / 32), z), dim3(32, 8), 0, s>>>(k, n, bidx ? B : B + off * bsB, ldb, bsB, bidx ? bidx + off : nullptr, Np, Kp,
-                                        planes + off * per);
+    k_tf_split_b<<<dim3((unsigned)(Np / 32), (unsigned)(Kp / 32), z), dim3(32, 8), 0, s>>>(
+        k, n, bidx ? B : B + off * bsB, ldb, bsB, bidx ? bidx + off : nullptr, Np, Kp, shift, planes + off * per);
     count_launches(1);
   }
   return cuda_status();
@@ -846,7 +850,7 @@ int khp_cgemm_tf32x3(int64_t batch, int32_t m, int32_t n, int32_t k, const float
   const auto* Bc = reinterpret_cast<const cplx<float>*>(B);
   auto* Cc = reinterpret_cast<cplx<float>*>(C);
   int st = tf32x3_split_a(batch, m, k, Ac, lda, a_stride, nullptr, ap, s);
-  if (!st) st = tf32x3_split_b(batch, k, n, Bc, ldb, b_stride, nullptr, bp, s);
+  if (!st) st = tf32x3_split_b(batch, k, n, Bc, ldb, b_stride, nullptr, mk(0.f), bp, s);
   if (!st) st = tf32x3_from_planes(batch, m, n, k, ap, bp, mk(1.f), mk(0.f), Cc, ldc, c_stride, err, s);
   return st;
 }

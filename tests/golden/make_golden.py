@@ -226,6 +226,40 @@ def twisted(ref_root):
                         n_pix=32)
 
 
+def twisted7(ref_root):
+    """One twisted bilayer at 7x7 base harmonics (product expansion of 2401 orders, n = 4802):
+    disc gratings eps 12 in eps 1 (r = 0.3, depth 0.3) on both sides of a gap (eps 1, d = 0.3),
+    twist 13 deg, square lattice, f = 0.5, oblique kp; R and T of the reference."""
+    sys.path.insert(0, ROOT)
+    Crystal, Drawing, tools = _import_reference(ref_root)
+    from khepri.expansion import Expansion
+    from khepri.layer import Layer
+    x = np.linspace(-0.5, 0.5, 64)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    r, angle_deg, f, d_gap = 0.3, 13.0, 0.5, 0.3
+    disc = np.where(X ** 2 + Y ** 2 < r ** 2, 12.0, 1.0)
+    lat = Crystal((1, 1), lattice="square").lattice
+    e1 = Expansion((7, 7), lattice=lat)
+    e2 = Expansion((7, 7), lattice=lat)
+    e2.rotate(np.deg2rad(angle_deg))
+    cl = Crystal.from_expansion(e1 + e2)
+    etw = cl.expansion
+    cl.add_layer("Sref", Layer.half_infinite(e1, "reflexion", 1), True)
+    cl.add_layer("G1", Layer.pixmap(e1, disc, 0.3), True)
+    cl.add_layer("Gap", Layer.uniform(etw, 1.0, d_gap), False)
+    cl.add_layer("G2", Layer.pixmap(e2, disc, 0.3), True)
+    cl.add_layer("Strans", Layer.half_infinite(e2, "transmission", 1), True)
+    cl.set_device(["G1", "Gap", "G2"], [False] * 3)
+    kp = (0.11 * 2 * np.pi * f, 0.05 * 2 * np.pi * f)
+    cl.set_source(1.0 / f, 1.0, 1.0, kp=kp)
+    t0 = time.time()
+    cl.solve()
+    R, T = cl.poynting_flux_end()
+    print(f"twisted 7x7: R {R}, T {T}, R + T - 1 = {R + T - 1:.2e}, {time.time() - t0:.0f} s")
+    np.savez_compressed(os.path.join(HERE, "twisted_7x7.npz"), case=np.array([0, angle_deg, f, d_gap, r, kp[0], kp[1]]),
+                        RT=np.array([R, T]), n_pix=64, eps_disc=12.0)
+
+
 def analytical(ref_root):
     """Analytical layers (closed-form island transforms, layer.py:161-168): C and R, T of a stack
     [analytical, uniform, analytical] for square (3x5 harmonics) and hexagonal (5x5) lattices."""
@@ -387,6 +421,8 @@ if __name__ == "__main__":
         analytical(sys.argv[1])
     elif len(sys.argv) > 2 and sys.argv[2] == "twisted":
         twisted(sys.argv[1])
+    elif len(sys.argv) > 2 and sys.argv[2] == "twisted7":
+        twisted7(sys.argv[1])
     elif len(sys.argv) > 1:
         main(sys.argv[1])
     else:
