@@ -68,10 +68,12 @@ __global__ void __launch_bounds__(kTeamThreads, 3) k_gehrd(int n, cplx<T>* A, in
 }
 
 // Schur form of the Hessenberg matrix and eigenvectors of the triangular factor (X left in A,
-// Q in Z); the back-transform W = Z X runs afterwards as a batched tiled product.
+// Q in Z); the back-transform W = Z X runs afterwards as a batched tiled product.  With a log
+// region (log_bytes per matrix at logbuf) Z's updates are logged and left for k_hqr_apply_log.
 template <typename T>
 __global__ void __launch_bounds__(kTeamThreads) k_geev_schur(int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z,
-                                                              cplx<T>* lam, int64_t bsLam, int* info) {
+                                                              cplx<T>* lam, int64_t bsLam, int* info,
+                                                              unsigned char* logbuf, int64_t log_bytes) {
   __shared__ TeamShared sh;
   __shared__ cplx<T> win[(KHP_HQR_WIN + 2) * (KHP_HQR_WIN + 2)];
   __shared__ cplx<T> rs[KHP_HQR_WIN];
@@ -80,9 +82,113 @@ __global__ void __launch_bounds__(kTeamThreads) k_geev_schur(int n, cplx<T>* A, 
   const int64_t b = blockIdx.x;
   cplx<T>* Ab = A + b * bsA;
   cplx<T>* Zb = Z + b * (int64_t)n * n;
-  const int st = team_hqr_win(t, Ab, lda, n, Zb, n, win, rc, rs, &sh);
+  int st;
+  if (logbuf) {
+    const HqrLog<T> L = hqr_log_view<T>(logbuf + b * log_bytes, log_bytes, n);
+    st = team_hqr_win(t, Ab, lda, n, Zb, n, win, rc, rs, &sh, &L);
+  } else {
+    st = team_hqr_win(t, Ab, lda, n, Zb, n, win, rc, rs, &sh);
+  }
   team_trevc(t, Ab, lda, n, lam + b * bsLam);
   if (threadIdx.x == 0 && st) info[b] |= st;
+}
+
+// The sweeps left in each matrix's rotation log applied to Z: a CTA of one warp holds
+// kLogRows rows of Z in shared memory (one row per lane, row stride odd so the lanes' accesses
+// fall in distinct banks) and rolls them through the logged rotations, which stream through a
+// double-buffered shared-memory stage (cp.async, kLogChunk rotations per stage).  Every lane
+// follows the same sweeps, so the control flow is uniform across the warp.
+constexpr int kLogRows = 32;
+constexpr int kLogChunk = 256;
+
+template <typename T>
+size_t apply_log_smem(int n) {
+  return 2 * kLogChunk * sizeof(HqrRot<T>) + (size_t)kLogRows * (n | 1) * sizeof(cplx<T>);
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(kLogRows) k_hqr_apply_log(int n, cplx<T>* Z, const unsigned char* logbuf,
+                                                             int64_t log_bytes, int64_t boff) {
+  extern __shared__ __align__(32) unsigned char dyn[];
+  HqrRot<T>* stage = reinterpret_cast<HqrRot<T>*>(dyn);  // [2][kLogChunk]
+  cplx<T>* rows = reinterpret_cast<cplx<T>*>(dyn + 2 * kLogChunk * sizeof(HqrRot<T>));
+  const int lds = n | 1;
+  const int64_t b = blockIdx.y + boff;
+  const HqrLog<T> L = hqr_log_view<T>(const_cast<unsigned char*>(logbuf) + b * log_bytes, log_bytes, n);
+  const int nsw = L.head[0], nrot = L.head[1];
+  if (nsw <= 0) return;
+  const int lane = threadIdx.x;
+  const int r0 = blockIdx.x * kLogRows;
+  const int nr = min(kLogRows, n - r0);
+  cplx<T>* Zb = Z + b * (int64_t)n * n;
+  for (int i = 0; i < nr; ++i)
+    for (int j = lane; j < n; j += kLogRows) rows[i * lds + j] = Zb[(int64_t)(r0 + i) * n + j];
+  // stage chunk c of the rotations into buffer c % 2 (16-byte pieces; past the end: not copied)
+  constexpr int kPieces = (int)sizeof(HqrRot<T>) / 16;
+  auto load_chunk = [&](int c) {
+    const int q0 = c * kLogChunk;
+    const int cnt = min(kLogChunk, nrot - q0);
+    HqrRot<T>* dst = stage + (c & 1) * kLogChunk;
+    for (int e = lane; e < cnt * kPieces; e += kLogRows)
+      cp_async16(reinterpret_cast<char*>(dst) + 16 * (size_t)e, reinterpret_cast<const char*>(L.rot + q0) + 16 * (size_t)e);
+    cp_async_commit();
+  };
+  const int nchunks = (nrot + kLogChunk - 1) / kLogChunk;
+  load_chunk(0);
+  if (nchunks > 1) load_chunk(1);
+  else cp_async_commit();  // an empty group keeps the wait counts below uniform
+  cp_async_wait<1>();
+  __syncwarp();
+  cplx<T>* row = rows + lane * lds;  // lanes past the last row roll a copy they never store
+  int chunk = 0, q = 0, qend = min(kLogChunk, nrot);
+  const HqrRot<T>* cur = stage;
+  int nlo = L.sweeps[0], nhi = L.sweeps[1];
+  for (int sw = 0; sw < nsw; ++sw) {
+    const int lo = nlo, hi = nhi;
+    if (sw + 1 < nsw) {  // the next sweep's bounds load while this one rolls
+      nlo = L.sweeps[2 * sw + 2];
+      nhi = L.sweeps[2 * sw + 3];
+    }
+    cplx<T> a = row[lo];
+    int k = lo;
+    while (k < hi) {
+      if (q == qend) {  // next chunk: refill this buffer with chunk + 2, wait for chunk + 1
+        __syncwarp();
+        if (chunk + 2 < nchunks) load_chunk(chunk + 2);
+        else cp_async_commit();
+        ++chunk;
+        cp_async_wait<1>();
+        __syncwarp();
+        cur = stage + (chunk & 1) * kLogChunk;
+        qend = min(q + kLogChunk, nrot);
+      }
+      const int take = min(hi - k, qend - q);
+      const HqrRot<T>* g = cur + (q - chunk * kLogChunk);
+#pragma unroll 4
+      for (int u = 0; u < take; ++u) {
+        const HqrRot<T> r = g[u];
+        const cplx<T> s = mk(r.sre, r.sim);
+        const cplx<T> bb = row[k + u + 1];
+        row[k + u] = r.c * a + mul_conj(bb, s);
+        a = r.c * bb - s * a;
+      }
+      k += take;
+      q += take;
+    }
+    row[hi] = a;
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+  for (int i = 0; i < nr; ++i)
+    for (int j = lane; j < n; j += kLogRows) Zb[(int64_t)(r0 + i) * n + j] = rows[i * lds + j];
 }
 
 // Scale every column of W to unit 2-norm (thread per column, coalesced along rows).
@@ -676,7 +782,8 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
 
 template <typename T>
 int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
-                int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s) {
+                int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s, void* logbuf,
+                int64_t log_bytes) {
   if (batch <= 0) return KHP_OK;
   // blocked reduction when panels pay off and their scratch fits in shared memory
   const size_t scratch = sizeof(cplx<T>) * (size_t)gehrd_blocked_scratch(n);
@@ -688,10 +795,28 @@ int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx
     return KHP_ERR_CUDA;
   const int threads = eig_threads(n);
   k_gehrd<T><<<(unsigned)batch, threads, smem, s>>>(n, A, lda, bsA, Z, blocked);
-  k_geev_schur<T><<<(unsigned)batch, threads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info);
+  // Z through the rotation log when the region holds at least one full sweep per matrix
+  unsigned char* lg = nullptr;
+  if (logbuf && log_bytes % 32 == 0 && reinterpret_cast<uintptr_t>(logbuf) % 32 == 0 &&
+      hqr_log_view<T>(logbuf, log_bytes, n).cap_rot >= n - 1)
+    lg = static_cast<unsigned char*>(logbuf);
+  k_geev_schur<T><<<(unsigned)batch, threads, 0, s>>>(n, A, lda, bsA, Z, lam, bsLam, info, lg, log_bytes);
   count_launches(2);
   int st = cuda_status();
   if (st) return st;
+  if (lg) {
+    const size_t lsm = apply_log_smem<T>(n);
+    if (lsm > 48 * 1024 &&
+        cudaFuncSetAttribute(k_hqr_apply_log<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm) != cudaSuccess)
+      return KHP_ERR_CUDA;
+    for (int64_t off = 0; off < batch; off += kMaxGridY) {
+      const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
+      k_hqr_apply_log<T><<<dim3((n + kLogRows - 1) / kLogRows, nb), kLogRows, lsm, s>>>(n, Z, lg, log_bytes, off);
+      count_launches(1);
+    }
+    st = cuda_status();
+    if (st) return st;
+  }
   // W = Z X (X unit upper triangular, stored in A) and unit columns
   st = launch_gemm<T>(batch, n, n, n, mk(T(1)), Z, n, (int64_t)n * n, A, lda, bsA, mk(T(0)), W, ldw, bsW, s);
   if (st) return st;
@@ -906,7 +1031,7 @@ int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_
                               int64_t, int64_t, cplx<T>, cplx<T>*, int64_t, int64_t, cudaStream_t, const int*, \
                               const int*, cplx<T>);                                                             \
   template int launch_geev<T>(int64_t, int, cplx<T>*, int64_t, int64_t, cplx<T>*, cplx<T>*, int64_t, int64_t,  \
-                              cplx<T>*, int64_t, int*, cudaStream_t);                                           \
+                              cplx<T>*, int64_t, int*, cudaStream_t, void*, int64_t);                           \
   template int launch_copy<T>(int64_t, int, int, const cplx<T>*, int64_t, int64_t, cplx<T>*, int64_t, int64_t,  \
                               cudaStream_t);                                                                    \
   template int launch_identity<T>(int64_t, int, int, cplx<T>*, int64_t, int64_t, cplx<T>, cudaStream_t);        \

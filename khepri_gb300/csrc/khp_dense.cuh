@@ -678,18 +678,94 @@ KHP_HD int team_hqr(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, in
   return sh->bi[3];
 }
 
+// ------------------------------------------------------------------------------------------
+// Rotation log of the QR sweeps.  Z does not feed back into the iteration, so its updates can
+// wait: each sweep's rotations are appended to a log and applied to Z later, each row of Z
+// rolled through all logged sweeps while it sits in fast memory (k_hqr_apply_log), instead of
+// streaming all of Z through DRAM once per sweep.  Every element of Z still receives the same
+// rotations in the same order.
+//
+// Layout of one matrix's log (hqr_log_view): a header of two ints (sweeps, rotations logged,
+// written when the QR ends), the (lo, hi) of every sweep (room for the iteration cap's number of
+// sweeps), then the rotations of all sweeps in order, sweep s holding the hi - lo rotations
+// k = lo .. hi - 1.  When a sweep does not fit in the rotations left, the team applies the log so
+// far to Z itself (hqr_log_flush) and starts the log again.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+struct alignas(4 * sizeof(T)) HqrRot {
+  T c, sre, sim, pad;  // G = [[c, s], [-conj(s), c]], s = sre + i sim
+};
+
+template <typename T>
+struct HqrLog {
+  int* head;        // [0] sweeps, [1] rotations in the log
+  int* sweeps;      // 2 per sweep: lo, hi
+  HqrRot<T>* rot;   // rotations in order of application
+  int cap_rot;      // rotations the log holds
+};
+
+// Upper bound on the sweeps team_hqr_win makes on an n x n matrix (its iteration cap).
+KHP_HD int hqr_max_sweeps(int n) { return 30 * n + 61; }
+
+KHP_HD int64_t hqr_log_rot_offset(int n) { return (8 + 8 * (int64_t)hqr_max_sweeps(n) + 31) / 32 * 32; }
+
+// View of a matrix's log in `bytes` bytes at base (32-byte aligned).  cap_rot < n - 1 means the
+// region cannot hold one full sweep: the caller then updates Z eagerly.
+template <typename T>
+KHP_HD HqrLog<T> hqr_log_view(void* base, int64_t bytes, int n) {
+  char* p = static_cast<char*>(base);
+  HqrLog<T> L;
+  L.head = reinterpret_cast<int*>(p);
+  L.sweeps = reinterpret_cast<int*>(p + 8);
+  const int64_t off = hqr_log_rot_offset(n);
+  L.rot = reinterpret_cast<HqrRot<T>*>(p + off);
+  const int64_t cap = bytes > off ? (bytes - off) / (int64_t)sizeof(HqrRot<T>) : 0;
+  L.cap_rot = cap > 0x3fffffff ? 0x3fffffff : (int)cap;
+  return L;
+}
+
+// One row of Z through logged sweeps (right rotations, the arithmetic of the eager update).
+template <typename T>
+KHP_HD void hqr_roll_row(cplx<T>* row, const int* sweeps, const HqrRot<T>* rot, int nsw) {
+  int q = 0;
+  for (int sw = 0; sw < nsw; ++sw) {
+    const int lo = sweeps[2 * sw], hi = sweeps[2 * sw + 1];
+    cplx<T> a = row[lo];
+    for (int k = lo; k < hi; ++k, ++q) {
+      const HqrRot<T> g = rot[q];
+      const T c = g.c;
+      const cplx<T> s = mk(g.sre, g.sim);
+      const cplx<T> b = row[k + 1];
+      row[k] = c * a + mul_conj(b, s);
+      a = c * b - s * a;
+    }
+    row[hi] = a;
+  }
+}
+
+// The team applies the first nsw logged sweeps to Z (thread per row, in place).
+template <class Team, typename T>
+KHP_HD void hqr_log_flush(const Team& t, const HqrLog<T>& log, int nsw, cplx<T>* Z, int64_t ldz, int n) {
+  t.sync();  // the log entries written by every thread are visible
+  for (int i = t.tid(); i < n; i += t.size()) hqr_roll_row(Z + (int64_t)i * ldz, log.sweeps, log.rot, nsw);
+  t.sync();
+}
+
 // Windowed form of the same single-shift QR sweep.  The bulge is chased through a window of
 // at most KHP_HQR_WIN rotations held in shared memory (win: (KHP_HQR_WIN + 2)^2 complex), the
 // rotations are recorded (rc, rs), and only then applied to the parts of H and Z outside the
 // window in one rolling pass per row or column (two live values per thread).  Same rotations,
 // same order of application per element as team_hqr; per-step work touches shared memory only.
+// With a log, Z is left alone and the rotations go to log->rot from index qbase (the sweep's
+// first rotation) on.
 #ifndef KHP_HQR_WIN
 #define KHP_HQR_WIN 32
 #endif
 
 template <class Team, typename T>
 KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, int lo, int hi,
-                             cplx<T> mu, cplx<T>* win, T* rc, cplx<T>* rs, TeamShared* sh) {
+                             cplx<T> mu, cplx<T>* win, T* rc, cplx<T>* rs, TeamShared* sh,
+                             const HqrLog<T>* log = nullptr, int qbase = 0) {
   constexpr int WS = KHP_HQR_WIN + 2;
   int k0 = lo;
   while (k0 < hi) {
@@ -754,6 +830,16 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
       H[(int64_t)(r0 + i) * ld + c0 + j] = win[i * WS + j];
     }
     const int nrot = k1 - k0;
+    if (log) {
+      for (int u = t.tid(); u < nrot; u += t.size()) {
+        HqrRot<T> g;
+        g.c = rc[u];
+        g.sre = rs[u].re;
+        g.sim = rs[u].im;
+        g.pad = T(0);
+        log->rot[qbase + (k0 - lo) + u] = g;
+      }
+    }
     // Each thread's strip is rotated in chunks of RB elements: the chunk's loads are issued
     // together (one memory latency per chunk instead of one per rotation), the running element
     // `a` is carried from chunk to chunk.
@@ -782,8 +868,10 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
       }
       H[(int64_t)k1 * ld + j] = a;
     }
-    // rows above the window (columns k0..k1) and every row of Z: right rotations, rolling along the row
-    for (int i = t.tid(); i < r0 + n; i += t.size()) {
+    // rows above the window (columns k0..k1) and every row of Z (unless logged): right
+    // rotations, rolling along the row
+    const int rows_end = log ? r0 : r0 + n;
+    for (int i = t.tid(); i < rows_end; i += t.size()) {
       cplx<T>* row = (i < r0) ? H + (int64_t)i * ld : Z + (int64_t)(i - r0) * ldz;
       cplx<T> a = row[k0];
       for (int q0 = 0; q0 < nrot; q0 += RB) {
@@ -812,9 +900,12 @@ KHP_HD void hqr_window_sweep(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<
   }
 }
 
+// With a log (log != nullptr, log->cap_rot >= n - 1) Z is updated through the log: the sweeps
+// still in the log when the QR ends are left for the caller to apply (hqr_roll_row on every row
+// of Z, k_hqr_apply_log on the GPU), their counts in log->head.
 template <class Team, typename T>
 KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z, int64_t ldz, cplx<T>* win, T* rc,
-                        cplx<T>* rs, TeamShared* sh) {
+                        cplx<T>* rs, TeamShared* sh, const HqrLog<T>* log = nullptr) {
   const T smlnum = Eps<T>::safemin * (T(n) / Eps<T>::ulp);
   const int cap = 30 * n + 60;
   int its = 0, total = 0;  // iteration counters, thread 0 only
@@ -823,6 +914,11 @@ KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z
     sh->bi[3] = 0;      // status
     sh->bi[4] = 0;      // sweeps done (diagnostic)
     sh->bi[5] = 0;      // rotations done (diagnostic)
+    sh->bi[6] = 0;      // log: flush before this sweep
+    sh->bi[7] = 0;      // log: sweeps in the log
+    sh->bi[8] = 0;      // log: rotations in the log
+    sh->bi[9] = 0;      // log: index of this sweep's first rotation
+    sh->bi[10] = 0;     // log: sweeps to apply at a flush
   }
   t.sync();
   while (true) {
@@ -860,13 +956,44 @@ KHP_HD int team_hqr_win(const Team& t, cplx<T>* H, int64_t ld, int n, cplx<T>* Z
           sh->bi[1] = l;
           sh->bd[0] = (double)mu.re;
           sh->bd[1] = (double)mu.im;
+          if (log) {
+            if (sh->bi[8] + (hi - l) > log->cap_rot) {
+              // no room for this sweep's hi - l rotations: the team applies the bi[7] sweeps
+              // logged so far, then this sweep starts a new log (recorded after the flush)
+              sh->bi[6] = 1;
+              sh->bi[10] = sh->bi[7];
+              sh->bi[7] = 1;
+              sh->bi[8] = 0;
+            } else {
+              sh->bi[6] = 0;
+              log->sweeps[2 * sh->bi[7]] = l;
+              log->sweeps[2 * sh->bi[7] + 1] = hi;
+              sh->bi[7] += 1;
+            }
+            sh->bi[9] = sh->bi[8];
+            sh->bi[8] += hi - l;
+          }
         }
       }
     }
     t.sync();
     if (sh->bi[0] != 0) continue;
-    hqr_window_sweep(t, H, ld, n, Z, ldz, sh->bi[1], hi, mk((T)sh->bd[0], (T)sh->bd[1]), win, rc, rs, sh);
+    const int lo = sh->bi[1];
+    if (log && sh->bi[6]) {
+      hqr_log_flush(t, *log, sh->bi[10], Z, ldz, n);  // ends with a team barrier
+      if (t.tid() == 0) {
+        log->sweeps[0] = lo;
+        log->sweeps[1] = hi;
+      }
+    }
+    hqr_window_sweep(t, H, ld, n, Z, ldz, lo, hi, mk((T)sh->bd[0], (T)sh->bd[1]), win, rc, rs, sh, log,
+                     log ? sh->bi[9] : 0);
   }
+  if (log && t.tid() == 0) {
+    log->head[0] = sh->bi[7];
+    log->head[1] = sh->bi[8];
+  }
+  t.sync();
   return sh->bi[3];
 }
 

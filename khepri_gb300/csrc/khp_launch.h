@@ -26,9 +26,12 @@ int launch_gemm(int64_t batch, int n, int m, int k, cplx<T> alpha, const cplx<T>
                 cudaStream_t s, const int* aidx = nullptr, const int* bidx = nullptr, cplx<T> bshift = cplx<T>{});
 
 // Eigen-decomposition A W = W diag(lam); A destroyed; Z: batch x n x n scratch (ld n).
+// logbuf (optional, log_bytes per matrix, both multiples of 32): scratch for the QR's rotation
+// log, which defers the updates of Z (used when it holds at least one full sweep).
 template <typename T>
 int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* Z, cplx<T>* W, int64_t ldw,
-                int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s);
+                int64_t bsW, cplx<T>* lam, int64_t bsLam, int* info, cudaStream_t s, void* logbuf = nullptr,
+                int64_t log_bytes = 0);
 
 // Element-wise helpers on batches of n x m matrices.
 template <typename T>

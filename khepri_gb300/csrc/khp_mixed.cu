@@ -1008,8 +1008,9 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
   p.Z32 = a.take<cf>(bm * nn);
   p.E32 = a.take<cf>(bm * nn);
   p.lu32 = a.take<cf>(bm * nn);
-  p.M64 = a.take<cd>(bm * nn);
-  p.MW64 = a.take<cd>(bm * nn);
+  // M64 and MW64 are one block: free while the eigensolver runs, it holds its rotation logs
+  p.M64 = a.take<cd>(2 * bm * nn);
+  p.MW64 = p.M64 ? p.M64 + bm * nn : nullptr;
   p.CW64 = a.take<cd>(bm * nn);
   p.Ct64 = nullptr;
   p.mu64 = a.take<cd>(bm * n);
@@ -1276,7 +1277,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
             midx + (int64_t)m * batch, sx + (int64_t)m * batch);
     MX_TRY(launch_assemble_pq<float>(bm, nh, Cm, HX, HY, midx, gx, gy, kpx, k0x, p.M32, s));
     stage_begin(KHP_STAGE_EIGENSOLVE, s);
-    MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s));
+    MX_TRY(launch_geev<float>(bm, n, p.M32, n, nn, p.Z32, W32, n, nn, lam32, n, sx, s, p.M64,
+                              (int64_t)(2 * nn * sizeof(cd))));
     stage_end(KHP_STAGE_EIGENSOLVE, s);
     // Refinement steps: R = M W - W mu in FP64, E = W^-1 R (FP32 inverse of the current W, held
     // in Wi until the final inverse), mu += diag(E), W += W F.

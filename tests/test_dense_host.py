@@ -27,6 +27,8 @@ def lib(tmp_path_factory):
     L.host_geev.argtypes = [I, P, P, P]
     L.host_geev_f32.argtypes = [I, P, P, P]
     L.host_gesv.argtypes = [I, I, P, P]
+    L.host_geev_log.argtypes = [I, P, P, P, I]
+    L.host_geev_log_f32.argtypes = [I, P, P, P, I]
     return L
 
 
@@ -86,6 +88,23 @@ def test_geev_fp32(lib):
     assert lib.host_geev_f32(n, _p(A.copy()), _p(W), _p(lam)) == 0
     A64, W64 = A.astype(np.complex128), W.astype(np.complex128)
     assert np.abs(A64 @ W64 - W64 * lam).max() / (np.abs(A).max() * n * np.abs(W).max()) < 1e-5
+
+
+@pytest.mark.parametrize("n", [5, 33, 70, 150])
+def test_geev_rotation_log_is_exact(lib, n):
+    # Z updated through the rotation log (deferred, and flushed by the team whenever the log is
+    # full) receives the same rotations in the same order as the eager update: identical results
+    for dtype, fn, fn_log in ((np.complex128, lib.host_geev, lib.host_geev_log),
+                              (np.complex64, lib.host_geev_f32, lib.host_geev_log_f32)):
+        A = _rand(n, 300 + n, dtype)
+        W0, lam0 = np.zeros_like(A), np.zeros(n, dtype)
+        assert fn(n, _p(A.copy()), _p(W0), _p(lam0)) == 0
+        # room for every sweep; room for about three sweeps (many flushes); room for one sweep
+        for cap in (100 * n * n, 3 * n, max(n - 1, 1)):
+            W, lam = np.zeros_like(A), np.zeros(n, dtype)
+            assert fn_log(n, _p(A.copy()), _p(W), _p(lam), cap) == 0
+            assert np.array_equal(lam, lam0), (dtype, cap)
+            assert np.array_equal(W, W0), (dtype, cap, np.abs(W - W0).max())
 
 
 def test_geev_repeated_and_real_spectrum(lib):
