@@ -93,6 +93,9 @@ def parse():
                     help="problems per call (456 = 3 x 152 SMs: three eigensolver CTAs per SM)")
     ap.add_argument("--eig-threads", type=int, default=0,
                     help="eigensolver threads per CTA for the sweep's 242 x 242 matrices (khp_tune; 0 = default)")
+    ap.add_argument("--mode-digits", type=int, default=0, choices=[0, 6, 8],
+                    help="7-bit digits per operand of the eigen-refinement steps' M W products (khp_tune; 0 = "
+                         "library default)")
     ap.add_argument("--tf32-min-n", type=int, default=-1,
                     help="smallest n whose recursion products run as 3xTF32 on the tensor cores (khp_tune; 0 = "
                          "never; -1 = the library default)")
@@ -438,6 +441,8 @@ def run_gpu(args):
         _capi.check(lib.khp_tune(1, N_MAT, args.eig_threads), "khp_tune")
     if args.tf32_min_n >= 0:
         _capi.check(lib.khp_tune(2, 1, args.tf32_min_n), "khp_tune")
+    if args.mode_digits:
+        _capi.check(lib.khp_tune(3, 1, args.mode_digits), "khp_tune")
     st = workloads.batched_structure(0)
     wl_all, kp_all = workloads.batched_problems()
     P = wl_all.shape[0]

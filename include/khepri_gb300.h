@@ -54,9 +54,13 @@ const char* khp_status_string(int code);
  * param KHP_TUNE_TF32_MIN_N (n ignored): the mixed solve's FP32 recursion products of size
  * n >= value run as 3xTF32 on the tensor cores (khp_cgemm_tf32x3's method), smaller ones on the
  * FP32 pipe; 0 = never (default 128).
+ * param KHP_TUNE_MODE_DIGITS (n ignored): 7-bit digits per operand of the tensor-core products
+ * M W inside the mixed solve's eigen-refinement steps: 8 (default; operands cut at 2^-56 of their
+ * row / column maximum) or 6 (2^-42).  The final residual test and the products C W stay at 8.
  */
 #define KHP_TUNE_EIG_THREADS 1
 #define KHP_TUNE_TF32_MIN_N 2
+#define KHP_TUNE_MODE_DIGITS 3
 int khp_tune(int32_t param, int32_t n, int32_t value);
 
 /*

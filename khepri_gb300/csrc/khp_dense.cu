@@ -31,6 +31,10 @@ int eig_threads(int n) {
 int g_tf32_min_n = 128;
 bool use_tf32_products(int n) { return g_tf32_min_n > 0 && n >= g_tf32_min_n; }
 
+// Digits per operand of the eigen-refinement steps' M W products (khp_tune KHP_TUNE_MODE_DIGITS).
+int g_mode_digits = 8;
+int mode_step_digits() { return g_mode_digits; }
+
 namespace {
 
 template <typename T>
@@ -1057,6 +1061,11 @@ int khp_tune(int32_t param, int32_t n, int32_t value) {
   if (param == KHP_TUNE_TF32_MIN_N) {
     if (value < 0) return KHP_ERR_INVALID_ARG;
     g_tf32_min_n = value;
+    return KHP_OK;
+  }
+  if (param == KHP_TUNE_MODE_DIGITS) {
+    if (value != 6 && value != 8) return KHP_ERR_INVALID_ARG;
+    g_mode_digits = value;
     return KHP_OK;
   }
   if (param != KHP_TUNE_EIG_THREADS || n < 1 || n > kTuneMaxN) return KHP_ERR_INVALID_ARG;

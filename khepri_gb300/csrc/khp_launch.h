@@ -82,12 +82,14 @@ size_t ozaki_b_elems(int k, int n);  // per problem
 int ozaki_rows_padded(int m);
 int64_t ozaki_chunk(int64_t batch);  // problems per chunk for a batch (even split, <= kOzakiMaxChunk)
 // C[b] = A[aidx ? aidx[b] : b] B[b] (complex FP64; A m x k, B k x n; aidx optional, device).
+// digits = 8: FP64-accurate (operands cut at 2^-56 of their row / column maximum); digits = 6:
+// operands cut at 2^-42 (error ~2^-42 2k |A row| |B column|, for residuals that need ~1e-12).
 int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64_t lda, int64_t bsA, const int* aidx,
                 const cplx<double>* B, int64_t ldb, int64_t bsB, cplx<double>* C, int64_t ldc, int64_t bsC,
-                const OzakiWs& w, cudaStream_t s);
+                const OzakiWs& w, cudaStream_t s, int digits = 8);
 
-// The same exact digit products on tcgen05 with TMEM accumulators (7-bit digits, ND = 8 for an
-// FP64 result, 4 for FP32): C = alpha A B + beta C, A[aidx[b]] and B[bidx[b]] optional gathers.
+// The same exact digit products on tcgen05 with TMEM accumulators (7-bit digits, ND = 8 or 6 for
+// an FP64 result, 4 for FP32): C = alpha A B + beta C, A[aidx[b]] and B[bidx[b]] optional gathers.
 // Valid while 2k rounded up to 64 is at most tc_max_k2p(ND); digit arrays in OzakiWs sized by
 // tc_a_elems / tc_b_elems (per problem), exponents by tc_rows_padded(m) and n.
 int tc_max_k2p(int nd);
@@ -121,6 +123,8 @@ int tf32x3_from_planes(int64_t batch, int m, int n, int k, const float* Aplanes,
 
 // Whether the mixed solve's n x n FP32 products take the 3xTF32 tensor-core path (khp_tune).
 bool use_tf32_products(int n);
+// Digits per operand of the mixed solve's eigen-refinement products (khp_tune).
+int mode_step_digits();
 
 inline int cuda_status() { return cudaGetLastError() == cudaSuccess ? KHP_OK : KHP_ERR_CUDA; }
 

@@ -1301,7 +1301,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
         MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
         MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
       }
-      MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s));
+      MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s,
+                         mode_step_digits()));
       MX_PP(k_eig_residual, bm, nn, n, p.MW64, W64, mu_a, p.E32);
       MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
       k_clusters<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.Z32, p.pair, p.nearest, p.csz, p.memb, p.xc, mu_b);

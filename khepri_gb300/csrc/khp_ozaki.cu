@@ -407,15 +407,19 @@ int64_t ozaki_chunk(int64_t batch) {
 
 int ozaki_zgemm(int64_t batch, int m, int n, int k, const cplx<double>* A, int64_t lda, int64_t bsA, const int* aidx,
                 const cplx<double>* B, int64_t ldb, int64_t bsB, cplx<double>* C, int64_t ldc, int64_t bsC,
-                const OzakiWs& w, cudaStream_t s) {
+                const OzakiWs& w, cudaStream_t s, int digits) {
   if (batch <= 0 || m <= 0 || n <= 0) return KHP_OK;
   // the int32 level sums stay below 2.25 * 2^16 * K2p, under 2^31 for k <= 4096
   if (k <= 0 || k > 4096) return KHP_ERR_INVALID_ARG;
   // tcgen05 with TMEM level accumulators where its exactness bound and the scratch allow
   if (w.err && up64(2 * k) <= tc_max_k2p(8) && w.ad_elems >= tc_a_elems(8, m, k) &&
-      w.bd_elems >= tc_b_elems(8, k, n) && w.ea_n >= (size_t)tc_rows_padded(m) && w.eb_n >= (size_t)n)
+      w.bd_elems >= tc_b_elems(8, k, n) && w.ea_n >= (size_t)tc_rows_padded(m) && w.eb_n >= (size_t)n) {
+    if (digits == 6)
+      return tc_product<6, double, double>(batch, m, n, k, A, lda, bsA, aidx, B, ldb, bsB, nullptr, mk(1.0), mk(0.0),
+                                           C, ldc, bsC, w, s);
     return tc_product<8, double, double>(batch, m, n, k, A, lda, bsA, aidx, B, ldb, bsB, nullptr, mk(1.0), mk(0.0), C,
                                          ldc, bsC, w, s);
+  }
   const int64_t per_a = (int64_t)kDig * up64(m) * up64(2 * k), per_b = (int64_t)kDig * up64(2 * n) * up64(2 * k);
   const int64_t cap = std::min(std::min<int64_t>((int64_t)(w.ad_elems / per_a), (int64_t)(w.ea_n / up64(m))),
                                std::min<int64_t>((int64_t)(w.bd_elems / per_b), (int64_t)(w.eb_n / n)));

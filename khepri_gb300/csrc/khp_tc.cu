@@ -12,6 +12,7 @@
 // weigh 2^-35 and less and their rounding stays below 2^-59 of the result.  The epilogue
 // combines the levels in 64-bit integers and converts once:
 //   ND = 8 (FP64 result): sum_l L_l 2^-7(l+2) = hi 2^-35 + lo 2^-63 with hi, lo four levels each;
+//   ND = 6 (FP64 result, 42-bit operands): the same with lo from levels 4 and 5;
 //   ND = 4 (FP32 result): sum_l L_l 2^-7(l+2) = hi 2^-35, rounded once to FP32.
 //
 // Kernel: one CTA of 4 warps per 128 x NT tile of one problem's real output; one thread streams the
@@ -47,6 +48,10 @@ struct TcCfg;
 template <>
 struct TcCfg<8> {
   static constexpr int NT = 64;  // 8 levels x 64 columns = 512 TMEM columns
+};
+template <>
+struct TcCfg<6> {
+  static constexpr int NT = 64;  // 6 levels x 64 columns (of the 512 allocated)
 };
 template <>
 struct TcCfg<4> {
@@ -401,10 +406,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int l = 0; l < 4; ++l)
             hi += (long long)__float2int_rn(__uint_as_float(v[l][q + p])) * (1ll << (7 * (3 - l)));
-          if constexpr (ND == 8) {
+          if constexpr (ND > 4) {
             long long lo = 0;
 #pragma unroll
-            for (int l = 4; l < 8; ++l)
+            for (int l = 4; l < ND; ++l)
               lo += (long long)__float2int_rn(__uint_as_float(v[l][q + p])) * (1ll << (7 * (7 - l)));
             out[p] = (TO)scaled_sum(hi, lo, ex);
           } else {
@@ -699,11 +704,11 @@ bool encode_planes_map(CUtensorMap* map, const float* base, int Kp, int rows, in
 }  // namespace
 
 // Largest inner size (2k padded to 64) for which the levels that matter stay exact.
-int tc_max_k2p(int nd) { return nd == 8 ? 576 : 640; }
+int tc_max_k2p(int nd) { return nd > 4 ? 576 : 640; }
 
 size_t tc_a_elems(int nd, int m, int k) { return (size_t)nd * up_to(m, kM) * up_to(2 * k, kK); }
 size_t tc_b_elems(int nd, int k, int n) {
-  const int nt = nd == 8 ? TcCfg<8>::NT : TcCfg<4>::NT;
+  const int nt = nd > 4 ? TcCfg<8>::NT : TcCfg<4>::NT;
   return (size_t)nd * up_to(2 * n, nt) * up_to(2 * k, kK);
 }
 int tc_rows_padded(int m) { return up_to(m, kM); }
@@ -812,6 +817,10 @@ int tf32x3_from_planes(int64_t batch, int m, int n, int k, const float* Aplanes,
 }
 
 template int tc_product<8, double, double>(int64_t, int, int, int, const cplx<double>*, int64_t, int64_t, const int*,
+                                           const cplx<double>*, int64_t, int64_t, const int*, cplx<double>,
+                                           cplx<double>, cplx<double>*, int64_t, int64_t, const OzakiWs&,
+                                           cudaStream_t);
+template int tc_product<6, double, double>(int64_t, int, int, int, const cplx<double>*, int64_t, int64_t, const int*,
                                            const cplx<double>*, int64_t, int64_t, const int*, cplx<double>,
                                            cplx<double>, cplx<double>*, int64_t, int64_t, const OzakiWs&,
                                            cudaStream_t);
