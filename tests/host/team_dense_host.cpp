@@ -12,7 +12,7 @@ namespace {
 // log_cap > 0: Z updated through a rotation log of log_cap rotations (flushed by the team when
 // full), the sweeps left in it applied to every row of Z afterwards, as the GPU does.
 template <typename T>
-int geev_host(int n, const T* a, T* w, T* lam, int log_cap = 0) {
+int geev_host(int n, const T* a, T* w, T* lam, int log_cap = 0, bool unwindowed = false) {
   std::vector<cplx<T>> A(n * n), Z(n * n), v(3 * n), win((KHP_HQR_WIN + 2) * (KHP_HQR_WIN + 2)), rs(KHP_HQR_WIN);
   std::vector<cplx<T>> scratch(gehrd_blocked_scratch(n));
   std::vector<T> rc(KHP_HQR_WIN);
@@ -23,7 +23,9 @@ int geev_host(int n, const T* a, T* w, T* lam, int log_cap = 0) {
   if (n >= 64) team_gehrd_blocked(t, A.data(), n, n, Z.data(), n, scratch.data(), &sh);
   else team_gehrd(t, A.data(), n, n, Z.data(), n, v.data(), &sh);
   int st;
-  if (log_cap > 0) {
+  if (unwindowed) {
+    st = team_hqr(t, A.data(), n, n, Z.data(), n, &sh);
+  } else if (log_cap > 0) {
     const int64_t bytes = hqr_log_rot_offset(n) + (int64_t)log_cap * sizeof(HqrRot<T>);
     std::vector<HqrRot<T>> store((bytes + sizeof(HqrRot<T>) - 1) / sizeof(HqrRot<T>));
     const HqrLog<T> L = hqr_log_view<T>(store.data(), bytes, n);
@@ -59,6 +61,13 @@ int host_gehrd(int n, double* a, double* z, int blocked) {
 // Eigenvalues lam [n] and eigenvectors w [n x n] (columns), FP64 / FP32; returns the QR status.
 int host_geev(int n, const double* a, double* w, double* lam) { return geev_host<double>(n, a, w, lam); }
 int host_geev_f32(int n, const float* a, float* w, float* lam) { return geev_host<float>(n, a, w, lam); }
+// The same by the unwindowed sweep (one rotation at a time over all of H and Z).
+int host_geev_unwindowed(int n, const double* a, double* w, double* lam) {
+  return geev_host<double>(n, a, w, lam, 0, true);
+}
+int host_geev_unwindowed_f32(int n, const float* a, float* w, float* lam) {
+  return geev_host<float>(n, a, w, lam, 0, true);
+}
 // The same with Z updated through a rotation log of log_cap rotations.
 int host_geev_log(int n, const double* a, double* w, double* lam, int log_cap) {
   return geev_host<double>(n, a, w, lam, log_cap);

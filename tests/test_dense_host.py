@@ -28,6 +28,8 @@ def lib(tmp_path_factory):
     L.host_geev_f32.argtypes = [I, P, P, P]
     L.host_gesv.argtypes = [I, I, P, P]
     L.host_geev_log.argtypes = [I, P, P, P, I]
+    L.host_geev_unwindowed.argtypes = [I, P, P, P]
+    L.host_geev_unwindowed_f32.argtypes = [I, P, P, P]
     L.host_geev_log_f32.argtypes = [I, P, P, P, I]
     return L
 
@@ -88,6 +90,22 @@ def test_geev_fp32(lib):
     assert lib.host_geev_f32(n, _p(A.copy()), _p(W), _p(lam)) == 0
     A64, W64 = A.astype(np.complex128), W.astype(np.complex128)
     assert np.abs(A64 @ W64 - W64 * lam).max() / (np.abs(A).max() * n * np.abs(W).max()) < 1e-5
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 33, 34, 70, 150])
+def test_windowed_qr_matches_unwindowed(lib, n):
+    # the windowed sweep (bulge chased inside a shared-memory window, the rows and columns outside
+    # it updated afterwards) applies the same rotations in the same order to every element as the
+    # one-rotation-at-a-time sweep: identical results
+    for dtype, fn, fn_ref in ((np.complex128, lib.host_geev, lib.host_geev_unwindowed),
+                              (np.complex64, lib.host_geev_f32, lib.host_geev_unwindowed_f32)):
+        A = _rand(n, 500 + n, dtype)
+        W0, lam0 = np.zeros_like(A), np.zeros(n, dtype)
+        W, lam = np.zeros_like(A), np.zeros(n, dtype)
+        assert fn_ref(n, _p(A.copy()), _p(W0), _p(lam0)) == 0
+        assert fn(n, _p(A.copy()), _p(W), _p(lam)) == 0
+        assert np.array_equal(lam, lam0), (dtype, np.abs(lam - lam0).max())
+        assert np.array_equal(W, W0), (dtype, np.abs(W - W0).max())
 
 
 @pytest.mark.parametrize("n", [5, 33, 70, 150])
