@@ -147,3 +147,42 @@ def test_lu_solve(lib, n, m):
     assert lib.host_gesv(n, m, _p(A.copy()), _p(X)) == 0
     ref = np.linalg.solve(A, B)
     assert np.abs(X - ref).max() / np.abs(ref).max() < 1e-11
+
+
+def _sweep_pq(i):
+    """P Q of the 11x11 sweep structure's patterned layer at sweep problem i (the eigenproblem of
+    alternative.py:158-178), built by the oracle's formulas."""
+    import sys
+    sys.path.insert(0, ROOT)
+    from khepri_gb300 import workloads
+    from oracle import khepri_oracle as ko
+
+    st = workloads.batched_structure(0)
+    wl, kp = workloads.batched_problems()
+    eps = [v for v in st.layers.values() if v[0] == "pixmap"][0][1]
+    conv = ko.convolution_matrix(eps, st.pw)
+    kx, ky, _ = ko.k_vectors(ko.g_vectors(st.pw, ko.lattice_vectors("square")), kp[i], wl[i])
+    eye = np.eye(len(kx))
+    ic_kx, ic_ky = np.linalg.solve(conv, np.diag(kx)), np.linalg.solve(conv, np.diag(ky))
+    dkx, dky = np.diag(kx), np.diag(ky)
+    p = np.block([[dkx @ ic_ky, eye - dkx @ ic_kx], [dky @ ic_ky - eye, -dky @ ic_kx]])
+    q = np.block([[dkx @ dky, conv - dkx @ dkx], [dky @ dky - conv, -dky @ dkx]])
+    return p @ q
+
+
+@pytest.mark.parametrize("i", [0, 2])
+def test_windowed_qr_matches_unwindowed_sweep_matrices(lib, i):
+    # the sweep's 242 x 242 P Q matrices split in the middle during the FP32 QR (the active block's
+    # first row moves, and with it every later window), which random matrices rarely do: the
+    # windowed sweep must stay identical to the unwindowed one there too
+    M = _sweep_pq(i)
+    n = M.shape[0]
+    for dtype, fn, fn_ref in ((np.complex64, lib.host_geev_f32, lib.host_geev_unwindowed_f32),
+                              (np.complex128, lib.host_geev, lib.host_geev_unwindowed)):
+        A = M.astype(dtype)
+        W0, lam0 = np.zeros_like(A), np.zeros(n, dtype)
+        W, lam = np.zeros_like(A), np.zeros(n, dtype)
+        assert fn_ref(n, _p(A.copy()), _p(W0), _p(lam0)) == 0
+        assert fn(n, _p(A.copy()), _p(W), _p(lam)) == 0
+        assert np.array_equal(lam, lam0), (dtype, np.abs(lam - lam0).max())
+        assert np.array_equal(W, W0), (dtype, np.abs(W - W0).max())
