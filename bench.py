@@ -65,9 +65,10 @@ TC_PAIRS = 36
 TC_FLOPS_PER_MATRIX = TC_PAIRS * 2 * (2 * _up128(N_MAT) * _up64(2 * N_MAT) * _up64(2 * N_MAT)
                                       + 2 * _up128(N_MAT // 2) * _up64(2 * N_MAT) * _up64(N_MAT))
 BF16_PEAK = 1935.4  # TFLOP/s, MEASURED_PEAKS.json bf16_tflops (burst)
-# DRAM bytes per matrix of the FP32 eigensolver (read + write of k_gehrd and k_geev_schur) at
-# 456 matrices per launch, from one ncu capture of the bench's eigensolver launches
-GEEV_TRAFFIC_PER_MATRIX = (23328427776 + 9063487744 + 90695730432 + 99780031744) / 456
+# DRAM bytes per matrix of the FP32 eigensolver (read + write of k_gehrd, k_geev_schur and
+# k_hqr_apply_log) at 912 matrices per launch and 128-thread teams, from one ncu capture of the
+# bench's eigensolver launches (dram__bytes_read.sum + dram__bytes_write.sum, one pass)
+GEEV_TRAFFIC_PER_MATRIX = (70947202816 + 18853817088 + 80481979392 + 95487486208 + 1118951936 + 392237056) / 912
 
 
 def solve_mixed_flops(n, nmaps, npattern, nhomog):
@@ -89,10 +90,11 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=456,
-                    help="problems per call (456 = 3 x 152 SMs: three eigensolver CTAs per SM)")
-    ap.add_argument("--eig-threads", type=int, default=0,
-                    help="eigensolver threads per CTA for the sweep's 242 x 242 matrices (khp_tune; 0 = default)")
+    ap.add_argument("--batch", type=int, default=912,
+                    help="problems per call (912 = 6 x 152 SMs: six 128-thread eigensolver CTAs per SM)")
+    ap.add_argument("--eig-threads", type=int, default=128,
+                    help="eigensolver threads per CTA for the sweep's 242 x 242 matrices (khp_tune; 0 = the "
+                         "library default, 256)")
     ap.add_argument("--mode-digits", type=int, default=0, choices=[0, 6, 8],
                     help="7-bit digits per operand of the eigen-refinement steps' M W products (khp_tune; 0 = "
                          "library default)")
@@ -535,12 +537,13 @@ def run_gpu(args):
         achieved = eig_flops / (eig_ms / eig_calls * 1e-3) / 1e12
         stages = {k: {"ms_per_call": v[0] / args.steps, "share": round(v[0] / ms, 4)}
                   for k, v in stage_ms.items() if v[1] > 0}
-        roof = {"bound": "fp32", "kernel": "k_gehrd<float> + k_geev_schur<float> (eigensolve stage of khp_solve_batched_mixed)",
+        roof = {"bound": "fp32", "kernel": "k_gehrd<float> + k_geev_schur<float> + k_hqr_apply_log<float> (eigensolve "
+                         "stage of khp_solve_batched_mixed)",
                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak > 0 else None,
                 "traffic": GEEV_TRAFFIC_PER_MATRIX * mats if GEEV_TRAFFIC_PER_MATRIX else None,
-                "traffic_source": "DRAM read + write per matrix from one ncu capture at 456 matrices per launch, "
-                                  "scaled by the matrices of this launch",
+                "traffic_source": "DRAM read + write per matrix from one ncu capture at 912 matrices per launch "
+                                  "(128-thread teams), scaled by the matrices of this launch",
                 "peak_source": "FP32 FMA pipe measured in this run (khp_probe_fp32_tflops); MEASURED_PEAKS.json "
                                "lists only HBM and bf16",
                 "note": "latency-bound (one CTA per matrix; barriers and dependent loads inside each QR "

@@ -427,56 +427,72 @@ def convmat_bwd(struct, dconv, nx, ny):
     return deps
 
 
-def _group_chunks(structures, which, chunk, lattice, device):
-    """Yield (struct, idx, plan, pmap, pdepth, maps) for every chunk of every shape group:
-    ``maps`` lists the (structure, slot) of each prepared map, ``plan`` carries C, C^-1, Hx, Hy."""
+def _group_plan(structures, which, chunk):
+    """The shape groups of the problems (host only): a list of (key, [problem index arrays, one
+    per chunk]) and the per-structure map digests."""
     keys, digests = [], []
     for pw, layers, stack in structures:
         k, d = _shape_key(layers, stack)
         keys.append((tuple(pw),) + k)
         digests.append(d)
-    lat = engine.lattice_vectors(lattice)
     groups = {}
     for p in range(len(which)):
         groups.setdefault(keys[which[p]], []).append(p)
+    out = []
     for key, members in groups.items():
-        pw, kinds, slots, eps = key[0], key[1], key[2], key[3]
-        struct = engine.StructureGPU(pw, lat, device)
+        pw, kinds, slots = key[0], key[1], key[2]
         members = np.asarray(members)
-        L = len(kinds)
         nslots = len({s for k, s in zip(kinds, slots) if k == 1}) or 1
         step = chunk if chunk else autotune.chunk_for(2 * pw[0] * pw[1], nslots)
-        for s in range(0, len(members), step):
-            idx = members[s:s + step]
-            B = len(idx)
-            mpos, eps_maps = {}, []
-            for sid in dict.fromkeys(which[idx].tolist()):
-                _, layers, stack = structures[sid]
-                for name in stack:
-                    kind, e, _ = layers[name]
-                    if kind != "pixmap":
-                        continue
-                    slot = digests[sid].index(engine._digest(e))
-                    if (sid, slot) not in mpos:
-                        mpos[(sid, slot)] = len(eps_maps)
-                        eps_maps.append(np.asarray(e))
-            conv = ic = hx = hy = None
-            if eps_maps:
-                conv, ic, hx, hy = prepare_maps(struct, np.stack(eps_maps))
-            pm = np.zeros((L, B), dtype=np.int32)
-            pd = np.zeros((L, B), dtype=np.float64)
-            for j, p in enumerate(idx):
-                sid = which[p]
-                _, layers, stack = structures[sid]
-                for l, name in enumerate(stack):
-                    pd[l, j] = layers[name][2]
-                    if kinds[l] == 1:
-                        pm[l, j] = mpos[(sid, slots[l])]
-            plan = _ChunkPlan(kinds, slots, eps, conv, hx, hy)
-            plan.ic = ic
-            maps = sorted(mpos, key=mpos.get)
-            yield (struct, idx, plan, torch.tensor(pm, device=struct.device), torch.tensor(pd, device=struct.device),
-                   maps, eps_maps)
+        out.append((key, [members[s:s + step] for s in range(0, len(members), step)]))
+    return out, digests
+
+
+def _chunk_item(structures, which, digests, key, idx, struct):
+    """(struct, idx, plan, pmap, pdepth, maps, eps_maps) of one chunk: the chunk's pixmaps prepared
+    on the device (C, C^-1, Hx, Hy), per-problem map indices and depths."""
+    kinds, slots, eps = key[1], key[2], key[3]
+    L = len(kinds)
+    B = len(idx)
+    mpos, eps_maps = {}, []
+    for sid in dict.fromkeys(which[idx].tolist()):
+        _, layers, stack = structures[sid]
+        for name in stack:
+            kind, e, _ = layers[name]
+            if kind != "pixmap":
+                continue
+            slot = digests[sid].index(engine._digest(e))
+            if (sid, slot) not in mpos:
+                mpos[(sid, slot)] = len(eps_maps)
+                eps_maps.append(np.asarray(e))
+    conv = ic = hx = hy = None
+    if eps_maps:
+        conv, ic, hx, hy = prepare_maps(struct, np.stack(eps_maps))
+    pm = np.zeros((L, B), dtype=np.int32)
+    pd = np.zeros((L, B), dtype=np.float64)
+    for j, p in enumerate(idx):
+        sid = which[p]
+        _, layers, stack = structures[sid]
+        for l, name in enumerate(stack):
+            pd[l, j] = layers[name][2]
+            if kinds[l] == 1:
+                pm[l, j] = mpos[(sid, slots[l])]
+    plan = _ChunkPlan(kinds, slots, eps, conv, hx, hy)
+    plan.ic = ic
+    maps = sorted(mpos, key=mpos.get)
+    return (struct, idx, plan, torch.tensor(pm, device=struct.device), torch.tensor(pd, device=struct.device),
+            maps, eps_maps)
+
+
+def _group_chunks(structures, which, chunk, lattice, device):
+    """Yield (struct, idx, plan, pmap, pdepth, maps, eps_maps) for every chunk of every shape group:
+    ``maps`` lists the (structure, slot) of each prepared map, ``plan`` carries C, C^-1, Hx, Hy."""
+    groups, digests = _group_plan(structures, which, chunk)
+    lat = engine.lattice_vectors(lattice)
+    for key, chunks in groups:
+        struct = engine.StructureGPU(key[0], lat, device)
+        for idx in chunks:
+            yield _chunk_item(structures, which, digests, key, idx, struct)
 
 
 def _prep_args(wavelengths, kp, which, te, tm):
@@ -490,7 +506,8 @@ def _prep_args(wavelengths, kp, which, te, tm):
 
 
 def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, lattice="square", epsi=1.0,
-                     epse=1.0, chunk=None, both_pols=False, method="mixed", refine=2, strict=True, device="cuda"):
+                     epse=1.0, chunk=None, both_pols=False, method="mixed", refine=2, strict=True, device="cuda",
+                     streams=4):
     """R and T of problems spread over many structures, batched across structures.
 
     structures: list of (pw, layers, stack) (``layers`` as in solve_rt); which: [P] structure of
@@ -500,6 +517,10 @@ def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, la
     prepared in one batched launch).  chunk: problems per call (None: the autotuned number of
     mode matrices per call for the group's size, divided by its maps per problem).
     method: "mixed" (default) or "gamma" (FP64).
+    streams: CUDA streams the shape groups are dealt to in turn, each stream with its own
+    workspaces; a group's chunks stay on its stream.  Many small groups (structures of uneven
+    sizes) then fill the GPU together instead of one after the other; a chunk's flags are read
+    (and its flagged problems re-solved) only when its stream takes its next chunk.
     Returns R, T ([P] or [P, 2] with ``both_pols``) and status [P].
     """
     _capi.require_cuda()
@@ -508,21 +529,58 @@ def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, la
     R = np.empty((P, 2) if both_pols else P)
     T = np.empty((P, 2) if both_pols else P)
     st_all = np.zeros(P, dtype=np.int32)
-    for struct, idx, plan, pmap, pdepth, _, _ in _group_chunks(structures, which, chunk, lattice, device):
-        B = len(idx)
-        prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], struct.device)
-        status = torch.zeros(B, dtype=torch.int32, device=struct.device)
-        # the autotuned chunk comes with its tuned eigensolver team size
-        with (autotune.tuned_team(struct.n) if chunk is None else contextlib.nullcontext()):
-            if both_pols:
-                tt, tmm = both_pol_weights(B, struct.device)
-                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, tt, tmm, prec, refine, pmap, pdepth)
-            else:
-                r, t = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine,
-                                         pmap=pmap, pdepth=pdepth)
-        R[idx] = r.cpu().numpy()
-        T[idx] = t.cpu().numpy()
-        st_all[idx] = status.cpu().numpy()
+    dev = torch.device(device)
+    if dev.type == "cuda" and dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    main = torch.cuda.current_stream(dev)
+    K = max(1, int(streams))
+    ss = [main] + [torch.cuda.Stream(device=dev) for _ in range(K - 1)]
+    for s in ss[1:]:
+        s.wait_stream(main)  # the caller's earlier work on the inputs comes first
+    pending = [None] * K
+
+    def finish(k):
+        """Repairs and results of the chunk in flight on stream k (on that stream)."""
+        if pending[k] is None:
+            return
+        idx, r, t, status, fix, keep = pending[k]
+        pending[k] = None
+        with torch.cuda.stream(ss[k]):
+            fix()
+            R[idx] = r.cpu().numpy()
+            T[idx] = t.cpu().numpy()
+            st_all[idx] = status.cpu().numpy()
+
+    # a shape group's chunks run on one stream (they share the group's device data); groups are
+    # dealt to the streams in turn
+    groups, digests = _group_plan(structures, which, chunk)
+    lat = engine.lattice_vectors(lattice)
+    for gi, (key, chunk_idx) in enumerate(groups):
+        k = gi % K
+        struct_k = None
+        for idx in chunk_idx:
+            finish(k)  # the stream's workspaces are reused by its next chunk
+            with torch.cuda.stream(ss[k]):
+                if struct_k is None:
+                    struct_k = engine.StructureGPU(key[0], lat, dev)
+                _, _, plan, pmap, pdepth, _, _ = _chunk_item(structures, which, digests, key, idx, struct_k)
+                B = len(idx)
+                prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], dev)
+                status = torch.zeros(B, dtype=torch.int32, device=dev)
+                # the autotuned chunk comes with its tuned eigensolver team size
+                with (autotune.tuned_team(struct_k.n) if chunk is None else contextlib.nullcontext()):
+                    if both_pols:
+                        tt, tmm = both_pol_weights(B, dev)
+                        r, t, fix = solve_chunk_gamma(struct_k, plan, prob, status, epsi, epse, tt, tmm, prec, refine,
+                                                      pmap, pdepth, defer_repair=True)
+                    else:
+                        r, t, fix = solve_chunk_gamma(struct_k, plan, prob, status, epsi, epse, precision=prec,
+                                                      refine=refine, pmap=pmap, pdepth=pdepth, defer_repair=True)
+                pending[k] = (idx, r, t, status, fix, (struct_k, plan, prob, pmap, pdepth))
+    for k in range(K):
+        finish(k)
+    for s in ss[1:]:
+        main.wait_stream(s)
     if strict and st_all.any():
         bad = int(np.flatnonzero(st_all)[0])
         raise _capi.KhpError(f"problem {bad}: {_capi.decode_status(int(st_all[bad]))}")

@@ -133,11 +133,15 @@ _WS = {}
 
 
 def workspace(nbytes, device, slot=0):
-    """A reusable device byte buffer of at least ``nbytes`` per device and slot (grown, never
-    shrunk).  Calls whose workspaces must coexist use different slots: a mixed-precision solve
-    keeps its refined modes in its workspace until its flagged problems are re-solved, and a
-    pipelined caller alternates two slots between consecutive chunks."""
-    key = (str(device), int(slot))
+    """A reusable device byte buffer of at least ``nbytes`` per device, slot and current stream
+    (grown, never shrunk).  Calls whose workspaces must coexist use different slots: a
+    mixed-precision solve keeps its refined modes in its workspace until its flagged problems are
+    re-solved, and a pipelined caller alternates two slots between consecutive chunks.  Work
+    enqueued on different streams gets different buffers, so concurrent streams never share
+    scratch (work on one stream runs in order, so its calls may share a buffer)."""
+    dev = torch.device(device)
+    stream = torch.cuda.current_stream(dev).cuda_stream if dev.type == "cuda" else 0
+    key = (str(device), int(slot), stream)
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
         _WS[key] = buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
