@@ -525,7 +525,8 @@ def run_gpu(args):
         return
 
     # roofline of the dominant kernels: the FP32 eigensolver of the modes stage (k_gehrd +
-    # k_geev_schur, ~32 % of the step in the launch list), timed live by the library's stage events
+    # k_geev_schur + k_hqr_apply_log, ~31 % of the step in the launch list), timed live by the
+    # library's stage events
     scratch = torch.empty(2048 * 1024, dtype=torch.float64, device=dev)
     fp64_peak = lib.khp_probe_fp64_tflops(_capi.ptr(scratch), scratch.numel(), _capi.stream_ptr())
     fp32_peak = lib.khp_probe_fp32_tflops(_capi.ptr(scratch), 2 * scratch.numel(), _capi.stream_ptr())
