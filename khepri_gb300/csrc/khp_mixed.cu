@@ -1060,8 +1060,9 @@ MixedPlan plan_mixed(Arena& a, int64_t batch, int nh, int L, const int* kinds, i
     p.tfa = tf32x3_a_elems((int)n, (int)n);
     p.tfb = tf32x3_b_elems((int)n, (int)n);
     p.tfAc = a.take<float>((size_t)4 * S * batch * p.tfa);
-    p.tfA = a.take<float>(batch * p.tfa);
-    p.tfB = a.take<float>(batch * p.tfb);
+    // the recursion's per-product planes, first used by the modes stage's S * batch products
+    p.tfA = a.take<float>((size_t)S * batch * p.tfa);
+    p.tfB = a.take<float>((size_t)S * batch * p.tfb);
     p.tferr = a.take<int>(1);
   }
   p.gam = a.take<cf>((size_t)(L + 1) * batch * nn);
@@ -1289,6 +1290,14 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
     cd* mu_a = p.mu64;
     cd* mu_b = p.mu64b;
+    // the refinement steps' FP32 products (E = W^-1 R, W F): 3xTF32 on the tensor cores when the
+    // recursion's products are (their planes are free until the recursion), else the tiled product
+    auto mode_prod = [&](const cf* A, const cf* B, cf* C) -> int {
+      if (!p.tfA) return launch_gemm<float>(bm, n, n, n, one, A, n, nn, B, n, nn, zero, C, n, nn, s);
+      int st = tf32x3_split_a(bm, n, n, A, n, nn, nullptr, p.tfA, s);
+      if (!st) st = tf32x3_split_b(bm, n, n, B, n, nn, nullptr, zero, p.tfB, s);
+      return st ? st : tf32x3_from_planes(bm, n, n, n, p.tfA, p.tfB, one, zero, C, n, nn, p.tferr, s);
+    };
     // M W in FP64 (tensor-core digit products) at every step.  Updating it in FP32 instead
     // (M W += round(M W) F) is only FP32-accurate where F is large: next to a nearly defective
     // cluster that error enters the next step's residual and the refinement stalls at ~1e-8.
@@ -1304,12 +1313,12 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
       MX_TRY(ozaki_zgemm(bm, n, n, n, p.M64, n, nn, nullptr, W64, n, nn, p.MW64, n, nn, p.oz, s,
                          mode_step_digits()));
       MX_PP(k_eig_residual, bm, nn, n, p.MW64, W64, mu_a, p.E32);
-      MX_TRY(launch_gemm<float>(bm, n, n, n, one, Wi, n, nn, p.E32, n, nn, zero, p.Z32, n, nn, s));  // E
+      MX_TRY(mode_prod(Wi, p.E32, p.Z32));  // E
       k_clusters<<<(unsigned)bm, 256, 0, s>>>(n, mu_a, p.Z32, p.pair, p.nearest, p.csz, p.memb, p.xc, mu_b);
       count_launches(1);
       MX_TRY(cuda_status());
       MX_PP(k_eig_update, bm, nn, n, mu_a, p.Z32, p.M32, p.pair, p.nearest, p.csz, p.memb, p.xc);  // M32 <- F
-      MX_TRY(launch_gemm<float>(bm, n, n, n, one, W32, n, nn, p.M32, n, nn, zero, p.Z32, n, nn, s));
+      MX_TRY(mode_prod(W32, p.M32, p.Z32));
       MX_EW(k_add_correction, bm * nn, bm * nn, W64, p.Z32, W32);
       std::swap(mu_a, mu_b);
     }
