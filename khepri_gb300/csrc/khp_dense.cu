@@ -503,6 +503,43 @@ __global__ void k_perm_matrix(int n, const int* __restrict__ piv, cplx<T>* B, in
   }
 }
 
+// X <- X P, P the permutation matrix of the row interchanges piv[0:n) (one CTA per matrix): the
+// permutation and its inverse are resolved in shared memory, then the rows pass through a
+// shared-memory buffer R at a time and come back with their columns gathered, X[i][c] =
+// X[i][pinv[c]] (coalesced reads and writes).
+template <typename T>
+__global__ void k_col_perm(int n, int R, const int* __restrict__ piv, cplx<T>* X, int64_t ldx, int64_t bsX) {
+  extern __shared__ __align__(16) unsigned char dyn_cp[];
+  int* perm = reinterpret_cast<int*>(dyn_cp);
+  int* pinv = perm + n;
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(dyn_cp + ((2 * sizeof(int) * (size_t)n + 15) & ~size_t(15)));
+  const int64_t b = blockIdx.x;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) perm[r] = r;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < n; ++k) {
+      const int p = piv[b * n + k];
+      if (p != k) {
+        const int t = perm[k];
+        perm[k] = perm[p];
+        perm[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int r = threadIdx.x; r < n; r += blockDim.x) pinv[perm[r]] = r;
+  cplx<T>* Xb = X + b * bsX;
+  for (int r0 = 0; r0 < n; r0 += R) {
+    const int rows = min(R, n - r0);
+    __syncthreads();  // pinv ready; the previous rows written back
+    for (int e = threadIdx.x; e < rows * n; e += blockDim.x) buf[e] = Xb[(int64_t)(r0 + e / n) * ldx + e % n];
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+      const int i = e / n, c = e % n;
+      Xb[(int64_t)(r0 + i) * ldx + c] = buf[i * n + pinv[c]];
+    }
+  }
+}
+
 // Apply the row interchanges piv[k0:k1] to columns [c0, c1) of A (thread per column, in order).
 template <typename T>
 __global__ void k_laswp(int64_t batch, int n, int k0, int k1, int c0, int c1, cplx<T>* A, int64_t lda, int64_t bsA,
@@ -941,9 +978,12 @@ int launch_getrf_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t 
 // Block forward and backward substitution with launch_getrf_blocked's L and U (B already
 // permuted): for 128 or more right-hand sides each block row is one fused product + solve
 // (k_block_solve), for fewer a tiled product sized to m followed by the block solve.
+// tri_rhs: B is lower triangular (the identity, for an inverse), so L Y = B keeps Y lower
+// triangular and the forward sweep's block row kb only computes its first kb + w columns (the
+// rest stay 0): a third of the forward work instead of all of it.
 template <typename T>
 int getrs_blocked_tri(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64_t bsA, cplx<T>* B, int64_t ldb,
-                      int64_t bsB, int m, cudaStream_t s) {
+                      int64_t bsB, int m, cudaStream_t s, bool tri_rhs = false) {
   if (m < kBsBN) {
     // few right-hand sides: tiled product sized to m, then the block solve
     auto trsm = [&](int kb, int w, int lower) {
@@ -980,19 +1020,22 @@ int getrs_blocked_tri(int64_t batch, int n, const cplx<T>* A, int64_t lda, int64
   constexpr size_t smem = block_solve_smem<T>();
   if (cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
-  auto block = [&](int kb, int w, int k0, int K, int lower) {
+  auto block = [&](int kb, int w, int k0, int K, int lower, int mc) {
     for (int64_t off = 0; off < batch; off += kMaxGridY) {
       const unsigned nb = (unsigned)std::min<int64_t>(batch - off, kMaxGridY);
-      k_block_solve<T><<<dim3((m + kBsBN - 1) / kBsBN, nb), 256, smem, s>>>(w, kb, k0, K, m, A + off * bsA, lda, bsA,
-                                                                           B + off * bsB, ldb, bsB, lower);
+      k_block_solve<T><<<dim3((mc + kBsBN - 1) / kBsBN, nb), 256, smem, s>>>(w, kb, k0, K, mc, A + off * bsA, lda,
+                                                                            bsA, B + off * bsB, ldb, bsB, lower);
       count_launches(1);
     }
   };
-  for (int kb = 0; kb < n; kb += KHP_NB) block(kb, std::min(KHP_NB, n - kb), 0, kb, 1);  // L Y = B
+  for (int kb = 0; kb < n; kb += KHP_NB) {  // L Y = B
+    const int w = std::min(KHP_NB, n - kb);
+    block(kb, w, 0, kb, 1, tri_rhs ? std::min(m, kb + w) : m);
+  }
   const int last = ((n - 1) / KHP_NB) * KHP_NB;
   for (int kb = last; kb >= 0; kb -= KHP_NB) {  // U X = Y
     const int w = std::min(KHP_NB, n - kb);
-    block(kb, w, kb + w, n - kb - w, 0);
+    block(kb, w, kb + w, n - kb - w, 0, m);
   }
   return cuda_status();
 }
@@ -1020,11 +1063,25 @@ int launch_inverse_blocked(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_
     if (st) return st;
     return launch_getrs_blocked<T>(batch, n, A, lda, bsA, piv, Ainv, ldi, bsI, n, s);
   }
-  k_perm_matrix<T><<<(unsigned)batch, 256, psmem, s>>>(n, piv, Ainv, ldi, bsI);
-  count_launches(1);
-  st = cuda_status();
+  // A^-1 = U^-1 L^-1 P: the substitutions on the identity (lower triangular, so the forward sweep
+  // skips the zero columns), then the columns permuted; for few columns the permutation matrix
+  // itself is the right-hand side
+  const size_t head = (2 * sizeof(int) * (size_t)n + 15) & ~size_t(15);
+  const size_t row_bytes = sizeof(cplx<T>) * (size_t)n;
+  if (n < kBsBN || head + row_bytes > 48 * 1024) {
+    k_perm_matrix<T><<<(unsigned)batch, 256, psmem, s>>>(n, piv, Ainv, ldi, bsI);
+    count_launches(1);
+    st = cuda_status();
+    if (st) return st;
+    return getrs_blocked_tri<T>(batch, n, A, lda, bsA, Ainv, ldi, bsI, n, s);
+  }
+  st = launch_identity<T>(batch, n, n, Ainv, ldi, bsI, mk(T(1)), s);
+  if (!st) st = getrs_blocked_tri<T>(batch, n, A, lda, bsA, Ainv, ldi, bsI, n, s, true);
   if (st) return st;
-  return getrs_blocked_tri<T>(batch, n, A, lda, bsA, Ainv, ldi, bsI, n, s);
+  const int R = (int)std::min<size_t>(16, (48 * 1024 - head) / row_bytes);
+  k_col_perm<T><<<(unsigned)batch, 256, head + row_bytes * R, s>>>(n, R, piv, Ainv, ldi, bsI);
+  count_launches(1);
+  return cuda_status();
 }
 
 #define KHP_INSTANTIATE(T)                                                                                       \
