@@ -272,9 +272,61 @@ def _no_repair():
     return None
 
 
+class ChunkGraph:
+    """One full-size chunk of the batched recursion (khp_solve_batched(_mixed), one or both
+    polarisations) captured as a CUDA graph: the ~1000 launches of a chunk are replayed as one
+    graph launch, with the next chunk's problems copied into the graph's input buffers first.
+
+    The capture follows one eager call that sizes the workspace, so nothing is allocated while
+    capturing; outputs (R, T, status) live in the graph's memory and are overwritten by the next
+    replay.  The deferred re-solve of flagged problems (mixed path) runs eagerly after a replay.
+    Library stage timing (khp_stage_timing) must be off while a graph is captured or replayed."""
+
+    def __init__(self, struct, plan, B, precision, refine, epsi, epse, both_pols, ws_slot, prob0):
+        self.B = B
+        dev = struct.device
+        self.prob = engine.Problems(k0=prob0.k0.clone(), kp=prob0.kp.clone(), te=prob0.te.clone(),
+                                    tm=prob0.tm.clone())
+        self.status = torch.zeros(B, dtype=torch.int32, device=dev)
+        kw = dict(ws_slot=ws_slot, defer_repair=precision == "mixed", repair=False)
+
+        def call():
+            if both_pols:
+                return solve_chunk_gamma_both_pols(struct, plan, self.prob, self.status, epsi, epse, precision,
+                                                   refine, **kw)
+            return solve_chunk_gamma(struct, plan, self.prob, self.status, epsi, epse, precision=precision,
+                                     refine=refine, **kw)
+
+        # the eager call solves prob0 (its results are first()'s) and sizes the workspaces and sets
+        # the kernel attributes, so nothing is allocated or configured while capturing
+        out = call()
+        # (the status buffer is shared with the graph: a replay clears it, so the caller reads these
+        # results before the next replay)
+        self._first = (out[0], out[1], self.status, out[2] if len(out) > 2 else _no_repair)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
+            out = call()
+        self.R, self.T = out[0], out[1]
+        self.fix = out[2] if len(out) > 2 else _no_repair
+
+    def first(self):
+        """R, T, status and deferred re-solve of the eager call that preceded the capture."""
+        return self._first
+
+    def replay(self, prob):
+        """Solve ``prob`` (B problems): returns R, T, status and the deferred re-solve."""
+        for dst, src in ((self.prob.k0, prob.k0), (self.prob.kp, prob.kp), (self.prob.te, prob.te),
+                         (self.prob.tm, prob.tm)):
+            dst.copy_(src)
+        self.status.zero_()
+        self.graph.replay()
+        return self.R, self.T, self.status, self.fix
+
+
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
              chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False, method="gamma",
-             refine=2):
+             refine=2, graphs=False):
     """R and T of every problem (host numpy arrays); problems share ``layers``/``stack``.
 
     layers: name -> ("pixmap", eps_map, depth) | ("uniform", eps, depth); stack: layer names
@@ -285,7 +337,9 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     "mixed" (the same recursion in FP32 with FP64 eigen-refinement and ``refine`` rounds of FP64
     iterative refinement, khp_solve_batched_mixed) or "chain" (layer S-matrices and the
     star-product chain, as the reference; needed for per-order powers).  With ``strict`` a
-    non-zero per-problem status raises KhpError.
+    non-zero per-problem status raises KhpError.  ``graphs=True`` (methods "gamma" and "mixed"):
+    every full-size chunk after the first replays a CUDA graph of the chunk solve (ChunkGraph, one
+    per workspace slot) instead of enqueueing its launches one by one; the results are the same.
     """
     if orders:
         method = "chain"
@@ -321,13 +375,26 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     # chunk c + 1 is enqueued, so the device never waits for the host's look at the flags; the two
     # chunks in flight use alternate workspace slots.
     pending = None
+    cgraphs = {}
+    use_graphs = graphs and method in ("gamma", "mixed")
     for c, s in enumerate(range(0, P, chunk)):
         e = min(P, s + chunk)
         prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
         status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
         r_o = t_o = None
         fix = _no_repair
-        if method in ("gamma", "mixed"):
+        if use_graphs and e - s == chunk and c > 0:
+            g = cgraphs.get(c % 2)
+            if g is None:
+                if pending is not None:  # the capture waits for the device anyway
+                    finish(pending)
+                    pending = None
+                g = cgraphs[c % 2] = ChunkGraph(struct, plan, chunk, prec, refine, epsi, epse, both_pols, c % 2,
+                                                prob)
+                r, t, status, fix = g.first()
+            else:
+                r, t, status, fix = g.replay(prob)
+        elif method in ("gamma", "mixed"):
             kw = dict(ws_slot=c % 2, defer_repair=prec == "mixed")
             if both_pols:
                 out = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine, **kw)
