@@ -124,6 +124,8 @@ def parse():
     ap.add_argument("--tf32-product", type=int, default=0,
                     help="only time khp_cgemm_tf32x3 (3xTF32 tensor-core complex product) on this many random "
                          "242 x 242 complex64 problems against torch's complex64 matmul (kernel profiling)")
+    ap.add_argument("--graphs-check", type=int, default=1,
+                    help="time the 5x5 sweep in small chunks with and without CUDA-graph replay (0 = skip)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -381,6 +383,26 @@ def bench_uneven(args):
                           f"({t_cpu:.1f} s)"}
 
 
+def bench_graphs(args):
+    """Chunk solves replayed as CUDA graphs against enqueued launch by launch (batch.solve_rt,
+    graphs=False / True), host wall clock through the public API: the 5x5 drop-in structure's 151
+    frequencies, eight times over, in chunks of 16 (small chunks, where launch overhead counts)."""
+    if args.graphs_check <= 0:
+        return None
+    from khepri_gb300 import batch, workloads
+    out = {}
+    sw = workloads.plain_sweep()
+    wl = np.tile(sw.wavelengths, 8)
+    kp = np.tile(np.asarray(sw.kp).reshape(-1, 2), (8, 1))
+    for g in (False, True):
+        batch.solve_rt((5, 5), sw.structure.layers, sw.structure.stack, wl[:64], kp[:64], chunk=16, method="mixed",
+                       graphs=g)
+        _, t = _timed(lambda: batch.solve_rt((5, 5), sw.structure.layers, sw.structure.stack, wl, kp, chunk=16,
+                                             method="mixed", graphs=g))
+        out.setdefault("plain_5x5_chunk16", {})["graphs" if g else "eager"] = len(wl) / t
+    return out
+
+
 def bench_twisted(args):
     """Twisted bilayers at 5x5 base harmonics (product expansion of 625 orders, n = 1250): a disc
     grating (eps 12 in 1, 128x128 map, depth 0.3) on each side of a gap (d 0.3), twist 13 deg,
@@ -630,8 +652,9 @@ def run_gpu(args):
                "one_thread": {"value": one, "unit": UNIT, "cores": 1,
                               "sample": "the same problems, BLAS and OpenMP pinned to one thread"}}
 
-    grad_info = uneven_info = twisted_info = twisted7_info = None
+    grad_info = uneven_info = twisted_info = twisted7_info = graphs_info = None
     if rank == 0:
+        graphs_info = bench_graphs(args)
         grad_info = bench_grad(args, struct, st, wl_all, kp_all)
         uneven_info = bench_uneven(args)
         twisted_info = bench_twisted(args)
@@ -660,7 +683,7 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}", "problems_with_status": bad,
                        "repairs": repairs,
                        "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info,
-                       "twisted_7x7": twisted7_info},
+                       "twisted_7x7": twisted7_info, "graphs": graphs_info},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": world * len(e2e_idx) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.steps, "repairs": e2e_repairs,
