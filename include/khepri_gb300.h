@@ -182,7 +182,8 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
  * layers).  Every O(n^3) step runs in FP32; FP64 is used for three eigen-refinement steps per
  * patterned-layer eigensolve (residual M W - W mu) and for the residual of the whole stack's
  * interface equations, which refine_iters rounds of iterative refinement drive to FP64
- * accuracy through the FP32 factors (0 = FP32 answer only; 2 is the default of the Python API).
+ * accuracy through the FP32 factors (0 = FP32 answer only, at most 64; 2 is the default of the
+ * Python API).
  * A problem whose refinement has not converged (estimated error of its reflected or
  * transmitted amplitudes above 1e-9, e.g. an ill-conditioned system next to a Wood anomaly)
  * gets status bit 8; its R, T must then be recomputed with khp_solve_batched (the Python API
@@ -237,7 +238,9 @@ int khp_solve_batched_mixed_repair(int64_t batch, int32_t px, int32_t py, int32_
  *   ic: device complex [nmaps][nh][nh] = C^-1 (khp_structure_prep);
  *   dR, dT: device real [batch][npol][nh] (NULL = 0);  R_orders, T_orders: device real
  *   [batch][npol][nh] out (NULL = not written);  dconv: device complex [nmaps][nh][nh] out, in
- *   the convention dL = Re sum(dconv o dC) (summed over the problems using each map);
+ *   the convention dL = Re sum(dconv o dC) (summed over the problems using each map; a problem
+ *   returned with status bit 8 adds nothing to it: solve it again with more refine_iters and add
+ *   its share, as the Python API does);
  *   refine_iters >= 1.  A problem whose forward refinement did not converge keeps status bit 8
  *   (no FP64 re-solve here).
  */

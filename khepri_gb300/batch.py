@@ -182,7 +182,11 @@ MODES_BIT = 32
 # Problems re-solved after the mixed path flagged them: "refine_repairs" (status bit 8, the stack
 # refinement did not converge) are re-solved in FP64 from the mixed path's refined modes;
 # "fp64_repairs" (status bit 32, a refined mode missed its residual test) by the full FP64 path.
-STATS = {"refine_repairs": 0, "fp64_repairs": 0}
+STATS = {"refine_repairs": 0, "fp64_repairs": 0, "grad_repairs": 0}
+# Rounds of stack refinement for the gradient call's second pass over problems whose refinement
+# did not converge in the first (status bit 8; typically next to a Wood anomaly, where the FP32
+# factors make each round gain only a factor ~0.3)
+GRAD_REPAIR_ROUNDS = 40
 REPAIR_WS_SLOT = 7  # workspace slot of the re-solves (the flagged call's own slot must stay intact)
 
 
@@ -663,7 +667,10 @@ def solve_structures_grad(structures, wavelengths, kp, which=None, dR=None, dT=N
     harmonic count.  Returns R [P], T [P], R_orders [P, nh], T_orders [P, nh], grads, status:
     grads[s][name] = dL/d(eps map) of structure s's pixmap layer ``name`` as a complex [nx, ny]
     array in the convention dL = Re sum(grad * d eps) (for a real map, dL/deps = grad.real);
-    layers sharing one pixmap get the total gradient with respect to that pixmap.
+    layers sharing one pixmap get the total gradient with respect to that pixmap.  A problem whose
+    stack refinement does not converge adds nothing to the first call's gradients; it is solved
+    again with more refinement rounds and its share added (``STATS["grad_repairs"]``); what stays
+    unconverged keeps status bit 8.
     """
     _capi.require_cuda()
     wl, P, kpa, which, te, tm = _prep_args(wavelengths, kp, which, te, tm)
@@ -679,28 +686,52 @@ def solve_structures_grad(structures, wavelengths, kp, which=None, dR=None, dT=N
             Ro, To = np.empty((P, nh)), np.empty((P, nh))
         dev = struct.device
         prob = engine.Problems.make(wl[idx], kpa[idx], te[idx], tm[idx], dev)
-        status = torch.zeros(B, dtype=torch.int32, device=dev)
-        te_d, tm_d = prob.te.reshape(B, 1).contiguous(), prob.tm.reshape(B, 1).contiguous()
         wr = None if dR is None else torch.tensor(np.asarray(dR, dtype=float)[idx].reshape(B, 1, nh), device=dev)
         wt = None if dT is None else torch.tensor(np.asarray(dT, dtype=float)[idx].reshape(B, 1, nh), device=dev)
-        r = torch.empty((B, 1), dtype=torch.float64, device=dev)
-        t = torch.empty((B, 1), dtype=torch.float64, device=dev)
-        ro = torch.empty((B, 1, nh), dtype=torch.float64, device=dev)
-        to = torch.empty((B, 1, nh), dtype=torch.float64, device=dev)
         L = len(plan.kinds)
-        dconv = torch.empty((plan.nmaps, nh, nh), dtype=torch.complex128, device=dev)
-        ws = engine.workspace(lib.khp_solve_batched_mixed_grad_workspace(B, nh, L, _host(plan.kinds),
-                                                                         _host(plan.maps), plan.nmaps), dev)
         ei, ee = complex(epsi), complex(epse)
-        with engine._stage("khp_solve_batched_mixed_grad"):
-            code = lib.khp_solve_batched_mixed_grad(
-                B, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
-                _host(plan.depth), _capi.ptr(pmap), _capi.ptr(pdepth), plan.nmaps, _capi.ptr(plan.conv),
-                _capi.ptr(plan.ic), _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx), _capi.ptr(struct.gy),
-                ei.real, ei.imag, ee.real, ee.imag, _capi.ptr(prob.kp), _capi.ptr(prob.k0), 1, _capi.ptr(te_d),
-                _capi.ptr(tm_d), int(refine), _capi.ptr(wr), _capi.ptr(wt), _capi.ptr(r), _capi.ptr(t), _capi.ptr(ro),
-                _capi.ptr(to), _capi.ptr(dconv), _capi.ptr(status), _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
-        _capi.check(code, "khp_solve_batched_mixed_grad")
+
+        def run(sel, rounds):
+            """The gradient call on the chunk's problems at device indices ``sel`` (None: all)."""
+            pb = prob if sel is None else prob.subset(sel)
+            K = pb.batch
+            pm = pmap if sel is None else pmap[:, sel].contiguous()
+            pd = pdepth if sel is None else pdepth[:, sel].contiguous()
+            ted, tmd = pb.te.reshape(K, 1).contiguous(), pb.tm.reshape(K, 1).contiguous()
+            wrs = None if wr is None else (wr if sel is None else wr[sel].contiguous())
+            wts = None if wt is None else (wt if sel is None else wt[sel].contiguous())
+            st_k = torch.zeros(K, dtype=torch.int32, device=dev)
+            r_k = torch.empty((K, 1), dtype=torch.float64, device=dev)
+            t_k = torch.empty((K, 1), dtype=torch.float64, device=dev)
+            ro_k = torch.empty((K, 1, nh), dtype=torch.float64, device=dev)
+            to_k = torch.empty((K, 1, nh), dtype=torch.float64, device=dev)
+            dconv_k = torch.empty((plan.nmaps, nh, nh), dtype=torch.complex128, device=dev)
+            ws = engine.workspace(lib.khp_solve_batched_mixed_grad_workspace(K, nh, L, _host(plan.kinds),
+                                                                             _host(plan.maps), plan.nmaps), dev)
+            with engine._stage("khp_solve_batched_mixed_grad"):
+                code = lib.khp_solve_batched_mixed_grad(
+                    K, struct.pw[0], struct.pw[1], L, _host(plan.kinds), _host(plan.maps), _host(plan.eps),
+                    _host(plan.depth), _capi.ptr(pm), _capi.ptr(pd), plan.nmaps, _capi.ptr(plan.conv),
+                    _capi.ptr(plan.ic), _capi.ptr(plan.hx), _capi.ptr(plan.hy), _capi.ptr(struct.gx),
+                    _capi.ptr(struct.gy), ei.real, ei.imag, ee.real, ee.imag, _capi.ptr(pb.kp), _capi.ptr(pb.k0), 1,
+                    _capi.ptr(ted), _capi.ptr(tmd), int(rounds), _capi.ptr(wrs), _capi.ptr(wts), _capi.ptr(r_k),
+                    _capi.ptr(t_k), _capi.ptr(ro_k), _capi.ptr(to_k), _capi.ptr(dconv_k), _capi.ptr(st_k),
+                    _capi.ptr(ws), ws.numel(), _capi.stream_ptr())
+            _capi.check(code, "khp_solve_batched_mixed_grad")
+            return r_k, t_k, ro_k, to_k, dconv_k, st_k
+
+        r, t, ro, to, dconv, status = run(None, refine)
+        # A problem whose stack refinement did not converge (status bit 8; the modes are good)
+        # adds nothing to the call's map gradients; it is solved again with GRAD_REPAIR_ROUNDS
+        # rounds and its share added.
+        flagged = (status & REFINE_BIT) != 0
+        if bool(flagged.any()):
+            sel = torch.nonzero(flagged).flatten()
+            r2, t2, ro2, to2, dconv_new, st2 = run(sel, max(int(refine), GRAD_REPAIR_ROUNDS))
+            dconv = dconv + dconv_new
+            r[sel], t[sel], ro[sel], to[sel] = r2, t2, ro2, to2
+            status[sel] = (status[sel] & ~REFINE_BIT) | st2
+            STATS["grad_repairs"] += int(sel.numel())
         R[idx] = r[:, 0].cpu().numpy()
         T[idx] = t[:, 0].cpu().numpy()
         Ro[idx] = ro[:, 0].cpu().numpy()

@@ -835,7 +835,10 @@ int launch_geev(int64_t batch, int n, cplx<T>* A, int64_t lda, int64_t bsA, cplx
       cudaFuncSetAttribute(k_gehrd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return KHP_ERR_CUDA;
   const int threads = eig_threads(n);
-  k_gehrd<T><<<(unsigned)batch, threads, smem, s>>>(n, A, lda, bsA, Z, blocked);
+  // the blocked reduction keeps full 256-thread teams (its panel updates are parallel work; three
+  // teams per SM already cover the SM), whatever team size suits the QR's serial window chase
+  const int gthreads = blocked ? kTeamThreads : threads;
+  k_gehrd<T><<<(unsigned)batch, gthreads, smem, s>>>(n, A, lda, bsA, Z, blocked);
   // Z through the rotation log when the region holds at least one full sweep per matrix
   unsigned char* lg = nullptr;
   if (logbuf && log_bytes % 32 == 0 && reinterpret_cast<uintptr_t>(logbuf) % 32 == 0 &&

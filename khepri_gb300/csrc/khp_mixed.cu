@@ -43,6 +43,8 @@ constexpr int kMaxLayers = 16;
 constexpr int kEigSteps = 3;
 // Refinement rounds beyond the requested ones, run only for problems not yet converged.
 constexpr int kExtraRounds = 12;
+// Largest refine_iters the entry points accept (every round is one residual and one sweep launch).
+constexpr int kMaxRefine = 64;
 
 // ------------------------------------------------------------------------------------------
 // Eigen-refinement kernels
@@ -367,6 +369,18 @@ __global__ void k_or_status(int64_t batch, int S, const int* __restrict__ statx,
     int w = 0;
     for (int m = 0; m < S; ++m) w |= statx[(int64_t)m * batch + b];
     status[b] |= w;
+  }
+}
+
+// The loss seeds of problems whose stack refinement did not converge (status bit 8) cleared, so
+// that they add nothing to the map gradients (GR, GT: [batch][2n]); the caller solves them again
+// with more rounds and adds their share.
+__global__ void k_drop_unconverged_seeds(int64_t batch, int n2, const int* __restrict__ status, cd* GR, cd* GT) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < batch * n2; e += (int64_t)gridDim.x * blockDim.x) {
+    if (status[e / n2] & KHP_BIT_REFINE) {
+      GR[e] = mk(0.0);
+      GT[e] = mk(0.0);
+    }
   }
 }
 
@@ -1152,7 +1166,7 @@ int grad_mixed(const Table& tb, MixedPlan& p, GradPlan& g, const GradArgs& ga, i
                const int* kinds, const std::vector<int>& slot, const std::vector<int>& used, DepthOf depth_of,
                int64_t nmaps, const double* conv, const double* gx, const double* gy, const double* kp,
                const double* k0, int npol, const double* te, const double* tm, cd epsi, cd epse, int refine, double* R,
-               double* Tt, cudaStream_t s) {
+               double* Tt, const int* status, cudaStream_t s) {
   const int n = 2 * nh;
   const int64_t nn = (int64_t)n * n, hh = (int64_t)nh * nh;
   const cf one = mk(1.f), zero = mk(0.f);
@@ -1162,6 +1176,7 @@ int grad_mixed(const Table& tb, MixedPlan& p, GradPlan& g, const GradArgs& ga, i
                                               epse, ga.wR, ga.wT, R, Tt, ga.Ro, ga.To, g.GR, g.GT);
   count_launches(1);
   MX_TRY(cuda_status());
+  MX_EW(k_drop_unconverged_seeds, batch * 2 * n, batch, 2 * n, status, g.GR, g.GT);
   // ---- adjoint: F^T y = g ----
   if (cudaMemsetAsync(g.Y, 0, sizeof(cd) * batch * (size_t)(L + 2) * 4 * 2 * n, s) != cudaSuccess)
     return KHP_ERR_CUDA;
@@ -1482,7 +1497,7 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   }
   stage_end(KHP_STAGE_REFINE, s);
   return grad_mixed(tb, p, gp, *grad, batch, nh, L, kinds, slot, used, depth_of, nmaps, conv, gx, gy, kp, k0, npol,
-                    te, tm, epsi, epse, refine, R, Tt, s);
+                    te, tm, epsi, epse, refine, R, Tt, status, s);
 }
 
 }  // namespace
@@ -1531,8 +1546,8 @@ int khp_solve_batched_mixed(int64_t batch, int32_t px, int32_t py, int32_t nlaye
                             const double* kp, const double* k0, int32_t npol, const double* te, const double* tm,
                             int32_t refine_iters, double* R, double* T, int32_t* status, void* workspace,
                             size_t ws_bytes, void* stream) {
-  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 0 || refine_iters > 8 || !gx || !gy ||
-      !kp || !k0 || !te || !tm || !R || !T || !status)
+  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 0 || refine_iters > kMaxRefine ||
+      !gx || !gy || !kp || !k0 || !te || !tm || !R || !T || !status)
     return KHP_ERR_INVALID_ARG;
   if (nlayers > kMaxLayers) return KHP_ERR_TOO_LARGE;
   if (nlayers > 0 && (!layer_kind || !layer_map || !layer_eps || !layer_depth)) return KHP_ERR_INVALID_ARG;
@@ -1567,8 +1582,8 @@ int khp_solve_batched_mixed_grad(int64_t batch, int32_t px, int32_t py, int32_t 
                                  const double* tm, int32_t refine_iters, const double* dR, const double* dT, double* R,
                                  double* T, double* R_orders, double* T_orders, double* dconv, int32_t* status,
                                  void* workspace, size_t ws_bytes, void* stream) {
-  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 1 || refine_iters > 8 || !gx ||
-      !gy || !kp || !k0 || !te || !tm || !R || !T || !status || !dconv || !ic || nmaps < 1)
+  if (batch < 0 || px < 1 || py < 1 || nlayers < 0 || npol < 1 || refine_iters < 1 || refine_iters > kMaxRefine ||
+      !gx || !gy || !kp || !k0 || !te || !tm || !R || !T || !status || !dconv || !ic || nmaps < 1)
     return KHP_ERR_INVALID_ARG;
   if (nlayers > kMaxLayers) return KHP_ERR_TOO_LARGE;
   if (nlayers > 0 && (!layer_kind || !layer_map || !layer_eps || !layer_depth)) return KHP_ERR_INVALID_ARG;
