@@ -384,6 +384,66 @@ __global__ void k_drop_unconverged_seeds(int64_t batch, int n2, const int* __res
   }
 }
 
+// ---- double-float arithmetic for the stack residual's FP64 products ----------------------
+// A double d is carried as hi + lo, hi = fl32(d), lo = fl32(d - hi): about 48 significant bits
+// (the accumulation keeps ~1e-12 of the sum).  That is enough for the refinement rounds before
+// its convergence test, which only have to bring the next correction within reach; the tested
+// rounds take their products in FP64, since an ill-conditioned stack (next to a Wood anomaly)
+// only converges to 1e-9 on an FP64 residual.  Products and sums follow Dekker / Knuth
+// error-free transformations on the FP32 pipe, which on this GPU has ~60x the FP64 pipe's
+// throughput; the rounded intrinsics keep the compiler from contracting the error terms.
+__global__ void k_split_df(int64_t count, const cd* __restrict__ in, float4* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const cd v = in[e];
+    const float hr = (float)v.re, hi_ = (float)v.im;
+    out[e] = make_float4(hr, hi_, (float)(v.re - (double)hr), (float)(v.im - (double)hi_));
+  }
+}
+
+// (sh, sl) += (ah + al) (xh + xl), dropping al xl (relative 2^-48).
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float xh, float xl) {
+  const float p = __fmul_rn(ah, xh);
+  float e = fmaf(ah, xh, -p);  // ah xh = p + e exactly
+  e = fmaf(ah, xl, e);
+  e = fmaf(al, xh, e);
+  const float t = __fadd_rn(sh, p);  // two-sum: sh + p = t + err exactly
+  const float bb = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  sh = t;
+  sl += err + e;
+}
+
+// y = A x for two columns, A row-major n x n as double-float pairs, x [n][2] as double-float
+// pairs, y [n][2] FP64 (hi + lo of each accumulator).  A thread per row; x is read by every
+// thread in the same order (broadcast loads).
+__device__ void team_mv2_df(const TeamCta& t, const float4* __restrict__ A, int n, const float4* __restrict__ x,
+                            cd* y) {
+  for (int i = t.tid(); i < n; i += t.size()) {
+    float r0h = 0.f, r0l = 0.f, i0h = 0.f, i0l = 0.f, r1h = 0.f, r1l = 0.f, i1h = 0.f, i1l = 0.f;
+    const float4* row = A + (int64_t)i * n;
+    for (int j = 0; j < n; ++j) {
+      const float4 a = row[j];
+      const float4 u = x[2 * j], v = x[2 * j + 1];
+      // (a.x + i a.y) + (a.z + i a.w) times (u.x + i u.y) + (u.z + i u.w), column 0
+      df_mac(r0h, r0l, a.x, a.z, u.x, u.z);
+      df_mac(r0h, r0l, -a.y, -a.w, u.y, u.w);
+      df_mac(i0h, i0l, a.x, a.z, u.y, u.w);
+      df_mac(i0h, i0l, a.y, a.w, u.x, u.z);
+      df_mac(r1h, r1l, a.x, a.z, v.x, v.z);
+      df_mac(r1h, r1l, -a.y, -a.w, v.y, v.w);
+      df_mac(i1h, i1l, a.x, a.z, v.y, v.w);
+      df_mac(i1h, i1l, a.y, a.w, v.x, v.z);
+    }
+    y[2 * i] = mk((double)r0h + (double)r0l, (double)i0h + (double)i0l);
+    y[2 * i + 1] = mk((double)r1h + (double)r1l, (double)i1h + (double)i1l);
+  }
+}
+
+__device__ __forceinline__ float4 df_of(cd v) {
+  const float hr = (float)v.re, hi_ = (float)v.im;
+  return make_float4(hr, hi_, (float)(v.re - (double)hr), (float)(v.im - (double)hi_));
+}
+
 __global__ void k_round(int64_t count, const cd* __restrict__ in, cf* out) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = mk((float)in[e].re, (float)in[e].im);
@@ -411,6 +471,8 @@ struct MapPtrs {
   const cf* lam32;
   const cf* Wi;
   const cf* Vi;
+  const float4* W2;  // W64 and V64 as double-float pairs {hi.re, hi.im, lo.re, lo.im} (k_split_df)
+  const float4* V2;
 };
 
 struct Table {
@@ -495,7 +557,8 @@ __device__ __forceinline__ cd xprop(const cd* lam64, int i, double dk) { return 
 __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* gx, const double* gy,
                                                         const double* kp, const double* k0v, const cd* __restrict__ X,
                                                         const cd* __restrict__ XA, const cd* __restrict__ RT,
-                                                        cd* RES, cd* scratch, const int* active, int x_zero) {
+                                                        cd* RES, cd* scratch, const int* active, int x_zero,
+                                                        int use_df) {
   TeamCta t;
   const int64_t b = blockIdx.x;
   if (active && !active[b]) return;
@@ -559,23 +622,45 @@ __global__ void __launch_bounds__(256) k_stack_residual(Table tb, const double* 
     const double dk = E.dep.at(b) * k0;
     const cd* ap = xa + (2 * pl) * 2 * n;
     const cd* am = xa + (2 * pl + 1) * 2 * n;
-    // w1 = a+ + X a-, w2 = X a- - a+, w3 = X a+ + a-, w4 = a- - X a+
-    for (int e = t.tid(); e < 2 * n; e += t.size()) {
-      const cd xi = xprop(lam, e / 2, dk);
-      w1[e] = ap[e] + xi * am[e];
-      w2[e] = xi * am[e] - ap[e];
-      w3[e] = xi * ap[e] + am[e];
-      w4[e] = am[e] - xi * ap[e];
-    }
-    t.sync();
     cd* r1 = rs;
     cd* r2 = rs + 2 * n;
     cd* r3 = rs + 4 * n;
     cd* r4 = rs + 6 * n;
-    team_mv2(t, W, n, w1, r1);
-    team_mv2(t, V, n, w2, r2);
-    team_mv2(t, W, n, w3, r3);
-    team_mv2(t, V, n, w4, r4);
+    // w1 = a+ + X a-, w2 = X a- - a+, w3 = X a+ + a-, w4 = a- - X a+
+    if (use_df && M.W2) {
+      // the products W w, V w in double-float on the FP32 pipe (w1..w4 as pairs in the scratch)
+      float4* f1 = reinterpret_cast<float4*>(w1);
+      float4* f2 = f1 + 2 * n;
+      float4* f3 = f2 + 2 * n;
+      float4* f4 = f3 + 2 * n;
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const cd xi = xprop(lam, e / 2, dk);
+        f1[e] = df_of(ap[e] + xi * am[e]);
+        f2[e] = df_of(xi * am[e] - ap[e]);
+        f3[e] = df_of(xi * ap[e] + am[e]);
+        f4[e] = df_of(am[e] - xi * ap[e]);
+      }
+      t.sync();
+      const float4* W2 = M.W2 + b * nn;
+      const float4* V2 = M.V2 + b * nn;
+      team_mv2_df(t, W2, n, f1, r1);
+      team_mv2_df(t, V2, n, f2, r2);
+      team_mv2_df(t, W2, n, f3, r3);
+      team_mv2_df(t, V2, n, f4, r4);
+    } else {
+      for (int e = t.tid(); e < 2 * n; e += t.size()) {
+        const cd xi = xprop(lam, e / 2, dk);
+        w1[e] = ap[e] + xi * am[e];
+        w2[e] = xi * am[e] - ap[e];
+        w3[e] = xi * ap[e] + am[e];
+        w4[e] = am[e] - xi * ap[e];
+      }
+      t.sync();
+      team_mv2(t, W, n, w1, r1);
+      team_mv2(t, V, n, w2, r2);
+      team_mv2(t, W, n, w3, r3);
+      team_mv2(t, V, n, w4, r4);
+    }
     t.sync();
     for (int e = t.tid(); e < 2 * n; e += t.size()) {
       const int i = e / 2, c = e % 2;
@@ -1350,6 +1435,9 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     MX_TRY(ozaki_zgemm(bm, nh, n, nh, Cm, nh, hh, midx, W64 + hn, n, nn, CWb, n, nn, p.oz, s));
     MX_TRY(launch_modes_v<double>(bm, nh, gx, gy, kpx, k0x, W64, CWt, CWb, nn, lam64, V64, sx, s));
     MX_EW(k_round, bm * nn, bm * nn, V64, V32);
+    // W and V as double-float pairs for the stack residual, in the M, M W block (free from here on)
+    MX_EW(k_split_df, bm * nn, bm * nn, W64, reinterpret_cast<float4*>(p.M64));
+    MX_EW(k_split_df, bm * nn, bm * nn, V64, reinterpret_cast<float4*>(p.MW64));
     // FP32 inverses and V0 products
     MX_TRY(launch_copy<float>(bm, n, n, W32, n, nn, p.lu32, n, nn, s));
     MX_TRY(launch_inverse_blocked<float>(bm, n, p.lu32, n, nn, Wi, n, nn, p.piv, sx, s));
@@ -1460,6 +1548,8 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
     M.lam32 = p.lam32[m];
     M.Wi = p.Wi[m];
     M.Vi = p.Vi[m];
+    M.W2 = p.M64 ? reinterpret_cast<const float4*>(p.M64) + m * (size_t)batch * nn : nullptr;
+    M.V2 = p.MW64 ? reinterpret_cast<const float4*>(p.MW64) + m * (size_t)batch * nn : nullptr;
   }
   const size_t xbytes = sizeof(cd) * batch * (size_t)(2 * (L + 1)) * 2 * n;
   if (cudaMemsetAsync(p.X, 0, xbytes, s) != cudaSuccess) return KHP_ERR_CUDA;
@@ -1472,8 +1562,11 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   const int total = refine >= 1 ? refine + kExtraRounds : 0;
   for (int it = 0; it <= total; ++it) {
     const int* act = it > refine ? p.active : nullptr;
+    // rounds before the convergence test take the products in double-float (their residual
+    // only has to be good enough for the next correction); the tested rounds, and the extra
+    // rounds of slow problems next to Wood anomalies, in FP64
     k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr, act,
-                                                      it == 0 ? 1 : 0);
+                                                      it == 0 ? 1 : 0, it < refine ? 1 : 0);
     count_launches(1);
     MX_TRY(cuda_status());
     k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW,
