@@ -186,10 +186,11 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
  * Python API).
  * A problem whose refinement has not converged (estimated error of its reflected or
  * transmitted amplitudes above 1e-9, e.g. an ill-conditioned system next to a Wood anomaly)
- * gets status bit 8; its R, T must then be recomputed with khp_solve_batched (the Python API
- * does this).  After the eigen-refinement every mode is checked in FP64: a problem with a mode
- * whose relative residual |M w - mu w| / (max|mu| |w|) exceeds 1e-8 gets status bit 32 and must
- * be recomputed the same way.
+ * gets status bit 8; its R, T must then be recomputed, by khp_solve_batched_mixed_repair from
+ * this call's refined modes (the Python API does this) or by khp_solve_batched.  After the
+ * eigen-refinement every mode is checked in FP64: a problem with a mode whose relative residual
+ * |M w - mu w| / (max|mu| |w|) exceeds 1e-8 gets status bit 32 and must be recomputed by
+ * khp_solve_batched (its own FP64 eigensolve).
  */
 size_t khp_solve_batched_mixed_workspace(int64_t batch, int32_t nh, int32_t nlayers, const int32_t* layer_kind,
                                          const int32_t* layer_map);
