@@ -386,10 +386,10 @@ __global__ void k_drop_unconverged_seeds(int64_t batch, int n2, const int* __res
 
 // ---- double-float arithmetic for the stack residual's FP64 products ----------------------
 // A double d is carried as hi + lo, hi = fl32(d), lo = fl32(d - hi): about 48 significant bits
-// (the accumulation keeps ~1e-12 of the sum).  That is enough for the refinement rounds before
-// its convergence test, which only have to bring the next correction within reach; the tested
-// rounds take their products in FP64, since an ill-conditioned stack (next to a Wood anomaly)
-// only converges to 1e-9 on an FP64 residual.  Products and sums follow Dekker / Knuth
+// (the accumulation keeps ~1e-12 of the sum).  That is enough for the refinement rounds every
+// problem runs: a well-conditioned stack converges on them; an ill-conditioned one (next to a
+// Wood anomaly) stalls at that floor and only converges to 1e-9 on an FP64 residual, so its
+// extra rounds take their products in FP64.  Products and sums follow Dekker / Knuth
 // error-free transformations on the FP32 pipe, which on this GPU has ~60x the FP64 pipe's
 // throughput; the rounded intrinsics keep the compiler from contracting the error terms.
 __global__ void k_split_df(int64_t count, const cd* __restrict__ in, float4* __restrict__ out) {
@@ -1562,11 +1562,11 @@ int solve_mixed(int64_t batch, int px, int py, int L, const int* kinds, const in
   const int total = refine >= 1 ? refine + kExtraRounds : 0;
   for (int it = 0; it <= total; ++it) {
     const int* act = it > refine ? p.active : nullptr;
-    // rounds before the convergence test take the products in double-float (their residual
-    // only has to be good enough for the next correction); the tested rounds, and the extra
-    // rounds of slow problems next to Wood anomalies, in FP64
+    // the refine rounds every problem runs take the products in double-float; the extra rounds
+    // of the problems that have not converged by then (an ill-conditioned stack next to a Wood
+    // anomaly, whose corrections stall at the double-float floor) take them in FP64
     k_stack_residual<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.X, p.XA, p.RT, p.RES, p.scr, act,
-                                                      it == 0 ? 1 : 0, it < refine ? 1 : 0);
+                                                      it == 0 ? 1 : 0, it <= refine ? 1 : 0);
     count_launches(1);
     MX_TRY(cuda_status());
     k_stack_sweep<<<(unsigned)batch, 256, 0, s>>>(tb, gx, gy, kp, k0, p.RES, p.X, p.XA, p.RT, p.SW,
