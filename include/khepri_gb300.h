@@ -181,9 +181,10 @@ int khp_solve_batched(int64_t batch, int32_t px, int32_t py, int32_t nlayers, co
  * Mixed-precision form of khp_solve_batched (same arguments plus refine_iters; at most 16
  * layers).  Every O(n^3) step runs in FP32; FP64 is used for three eigen-refinement steps per
  * patterned-layer eigensolve (residual M W - W mu) and for the residual of the whole stack's
- * interface equations, which refine_iters rounds of iterative refinement drive to FP64
+ * interface equations, which refine_iters rounds of iterative refinement drive to near-FP64
  * accuracy through the FP32 factors (0 = FP32 answer only, at most 64; 2 is the default of the
- * Python API).
+ * Python API).  The residual's products run in double-float (FP32 pairs) in those rounds and in
+ * FP64 in the up to 12 extra rounds of problems that have not converged by then.
  * A problem whose refinement has not converged (estimated error of its reflected or
  * transmitted amplitudes above 1e-9, e.g. an ill-conditioned system next to a Wood anomaly)
  * gets status bit 8; its R, T must then be recomputed, by khp_solve_batched_mixed_repair from
