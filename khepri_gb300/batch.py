@@ -276,15 +276,28 @@ def _no_repair():
     return None
 
 
+_CAPTURE_STREAMS = {}
+
+
+def _capture_stream(device):
+    """The side stream ChunkGraph captures on (one per device, so that every capture, and the
+    eager call before it, find the same workspaces in engine.workspace's per-stream cache)."""
+    key = str(device)
+    if key not in _CAPTURE_STREAMS:
+        _CAPTURE_STREAMS[key] = torch.cuda.Stream(device=device)
+    return _CAPTURE_STREAMS[key]
+
+
 class ChunkGraph:
     """One full-size chunk of the batched recursion (khp_solve_batched(_mixed), one or both
     polarisations) captured as a CUDA graph: the ~1000 launches of a chunk are replayed as one
     graph launch, with the next chunk's problems copied into the graph's input buffers first.
 
-    The capture follows one eager call that sizes the workspace, so nothing is allocated while
-    capturing; outputs (R, T, status) live in the graph's memory and are overwritten by the next
-    replay.  The deferred re-solve of flagged problems (mixed path) runs eagerly after a replay.
-    Library stage timing (khp_stage_timing) must be off while a graph is captured or replayed."""
+    The capture follows one eager call of the same chunk on the same side stream, which sizes
+    the workspace (the graph then uses that buffer) and sets the kernels' attributes; outputs (R,
+    T, status) live in the graph's memory and are overwritten by the next replay.  The deferred
+    re-solve of flagged problems (mixed path) runs eagerly after a replay.  Library stage timing
+    (khp_stage_timing) must be off while a graph is captured or replayed."""
 
     def __init__(self, struct, plan, B, precision, refine, epsi, epse, both_pols, ws_slot, prob0):
         self.B = B
@@ -301,15 +314,18 @@ class ChunkGraph:
             return solve_chunk_gamma(struct, plan, self.prob, self.status, epsi, epse, precision=precision,
                                      refine=refine, **kw)
 
-        # the eager call solves prob0 (its results are first()'s) and sizes the workspaces and sets
-        # the kernel attributes, so nothing is allocated or configured while capturing
-        out = call()
+        # the eager call solves prob0 (its results are first()'s), sizes the side stream's workspace
+        # and sets the kernel attributes, so the capture allocates and configures nothing
+        cap = _capture_stream(dev)
+        cap.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(cap):
+            out = call()
         # (the status buffer is shared with the graph: a replay clears it, so the caller reads these
         # results before the next replay)
         self._first = (out[0], out[1], self.status, out[2] if len(out) > 2 else _no_repair)
         torch.cuda.synchronize(dev)
         self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
+        with torch.cuda.graph(self.graph, stream=cap, capture_error_mode="relaxed"):
             out = call()
         self.R, self.T = out[0], out[1]
         self.fix = out[2] if len(out) > 2 else _no_repair
