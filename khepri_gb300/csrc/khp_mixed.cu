@@ -392,12 +392,14 @@ __global__ void k_drop_unconverged_seeds(int64_t batch, int n2, const int* __res
 // extra rounds take their products in FP64.  Products and sums follow Dekker / Knuth
 // error-free transformations on the FP32 pipe, which on this GPU has ~60x the FP64 pipe's
 // throughput; the rounded intrinsics keep the compiler from contracting the error terms.
+__device__ __forceinline__ float4 df_of(cd v) {
+  const float hr = (float)v.re, hi_ = (float)v.im;
+  return make_float4(hr, hi_, (float)(v.re - (double)hr), (float)(v.im - (double)hi_));
+}
+
 __global__ void k_split_df(int64_t count, const cd* __restrict__ in, float4* __restrict__ out) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
-    const cd v = in[e];
-    const float hr = (float)v.re, hi_ = (float)v.im;
-    out[e] = make_float4(hr, hi_, (float)(v.re - (double)hr), (float)(v.im - (double)hi_));
-  }
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = df_of(in[e]);
 }
 
 // (sh, sl) += (ah + al) (xh + xl), dropping al xl (relative 2^-48).
@@ -437,11 +439,6 @@ __device__ void team_mv2_df(const TeamCta& t, const float4* __restrict__ A, int 
     y[2 * i] = mk((double)r0h + (double)r0l, (double)i0h + (double)i0l);
     y[2 * i + 1] = mk((double)r1h + (double)r1l, (double)i1h + (double)i1l);
   }
-}
-
-__device__ __forceinline__ float4 df_of(cd v) {
-  const float hr = (float)v.re, hi_ = (float)v.im;
-  return make_float4(hr, hi_, (float)(v.re - (double)hr), (float)(v.im - (double)hi_));
 }
 
 __global__ void k_round(int64_t count, const cd* __restrict__ in, cf* out) {
