@@ -126,6 +126,9 @@ def parse():
                          "242 x 242 complex64 problems against torch's complex64 matmul (kernel profiling)")
     ap.add_argument("--graphs-check", type=int, default=1,
                     help="time the 5x5 sweep in small chunks with and without CUDA-graph replay (0 = skip)")
+    ap.add_argument("--streams", type=int, default=2,
+                    help="CUDA streams the chunks are dealt to in turn (chunk k on stream k mod S, each with its "
+                         "own workspace), so that one chunk's stages run beside the next one's (1 = one stream)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="run only the warm-up and timed steps and print the line (for kernel profiling)")
     return ap.parse_args()
@@ -491,24 +494,41 @@ def run_gpu(args):
     FLOPS_PER_CALL["khp_solve_batched_mixed"] = solve_mixed_flops(N_MAT, plan.nmaps, npat, len(plan.kinds) - npat)
     prec = args.precision
 
-    def step(k):
-        """Enqueue chunk k; returns the chunk's deferred repair (its flags are read only after the
-        next chunk is enqueued, so the device never idles while the host looks at them)."""
-        out = batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k], precision=prec,
-                                                refine=args.refine, ws_slot=k % 2, defer_repair=prec == "mixed")
-        return out[2] if prec == "mixed" else (lambda: None)
+    # chunk k on stream k mod S with workspace slot k mod max(2, S); its deferred repair (the flags
+    # read, flagged problems re-solved) runs after the next max(1, S - 1) chunks are enqueued, so
+    # the device never idles while the host looks at them, and before the next chunk that reuses
+    # its stream and slot (the same schedule as batch.solve_rt)
+    nstreams = max(1, args.streams)
+    streams = [torch.cuda.Stream(dev) for _ in range(nstreams)] if nstreams > 1 else None
+    nslots, lag = max(2, nstreams), max(1, nstreams - 1)
 
-    def run_steps(ks, between=None):
-        pending = None
-        for k in ks:
+    def step(k, between=None):
+        """Enqueue chunk k (after ``between``, on the chunk's stream); returns its deferred repair."""
+        s = streams[k % nstreams] if streams else torch.cuda.current_stream(dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(s):
             if between is not None:
                 between()
-            fix = step(k)
-            if pending is not None:
-                pending()
-            pending = fix
-        if pending is not None:
-            pending()
+            out = batch.solve_chunk_gamma_both_pols(struct, plan, probs[k], statuses[k], precision=prec,
+                                                    refine=args.refine, ws_slot=k % nslots,
+                                                    defer_repair=prec == "mixed")
+        fix = out[2] if prec == "mixed" else (lambda: None)
+
+        def on_stream():
+            with torch.cuda.stream(s):
+                fix()
+        return on_stream
+
+    def run_steps(ks, between=None):
+        pending = []
+        for k in ks:
+            pending.append(step(k, between))
+            while len(pending) > lag:
+                pending.pop(0)()
+        while pending:
+            pending.pop(0)()
+        for s in streams or ():
+            torch.cuda.current_stream(dev).wait_stream(s)
 
     run_steps(range(args.warmup))
     torch.cuda.synchronize()
@@ -633,7 +653,8 @@ def run_gpu(args):
     rep_e0 = dict(batch.STATS)
     t0 = time.perf_counter()
     batch.solve_rt(st.pw, st.layers, st.stack, wl_all[e2e_idx], kp_all[e2e_idx], chunk=B, struct=struct,
-                   strict=False, both_pols=True, method="mixed" if prec == "mixed" else "gamma", refine=args.refine)
+                   strict=False, both_pols=True, method="mixed" if prec == "mixed" else "gamma", refine=args.refine,
+                   streams=nstreams)
     torch.cuda.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0

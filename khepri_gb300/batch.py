@@ -277,6 +277,17 @@ def _no_repair():
 
 
 _CAPTURE_STREAMS = {}
+_CHUNK_STREAMS = {}
+
+
+def _chunk_streams(device, count):
+    """``count`` side streams of ``device`` that solve_rt deals its chunks to; the same streams on
+    every call, so that engine.workspace's per-stream cache finds their workspaces again."""
+    key = str(device)
+    have = _CHUNK_STREAMS.setdefault(key, [])
+    while len(have) < count:
+        have.append(torch.cuda.Stream(device=device))
+    return have[:count]
 
 
 def _capture_stream(device):
@@ -346,7 +357,7 @@ class ChunkGraph:
 
 def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square", epsi=1.0, epse=1.0,
              chunk=256, orders=False, device="cuda", struct=None, strict=True, both_pols=False, method="gamma",
-             refine=2, graphs=False):
+             refine=2, graphs=False, streams=2):
     """R and T of every problem (host numpy arrays); problems share ``layers``/``stack``.
 
     layers: name -> ("pixmap", eps_map, depth) | ("uniform", eps, depth); stack: layer names
@@ -360,6 +371,9 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     non-zero per-problem status raises KhpError.  ``graphs=True`` (methods "gamma" and "mixed"):
     every full-size chunk after the first replays a CUDA graph of the chunk solve (ChunkGraph, one
     per workspace slot) instead of enqueueing its launches one by one; the results are the same.
+    ``streams`` (methods "gamma" and "mixed" without graphs): chunk c is enqueued on side stream
+    c mod ``streams``, so that one chunk's stages run beside the next one's on the device; each
+    stream has its own workspaces, and the results do not depend on it.
     """
     if orders:
         method = "chain"
@@ -381,57 +395,70 @@ def solve_rt(pw, layers, stack, wavelengths, kp, te=1.0, tm=0.0, lattice="square
     st = np.zeros(P, dtype=np.int32)
 
     def finish(job):
-        # the chunk's deferred re-solve of flagged problems, then its results to the host
-        s, e, r, t, r_o, t_o, status, fix = job
-        fix()
-        R[s:e] = r.cpu().numpy()
-        T[s:e] = t.cpu().numpy()
-        if orders:
-            ro[s:e] = r_o.cpu().numpy()
-            to[s:e] = t_o.cpu().numpy()
-        st[s:e] = status.cpu().numpy()
+        # the chunk's deferred re-solve of flagged problems, then its results to the host (on the
+        # chunk's stream, which orders the copies after its work)
+        sc, s, e, r, t, r_o, t_o, status, fix = job
+        with torch.cuda.stream(sc):
+            fix()
+            R[s:e] = r.cpu().numpy()
+            T[s:e] = t.cpu().numpy()
+            if orders:
+                ro[s:e] = r_o.cpu().numpy()
+                to[s:e] = t_o.cpu().numpy()
+            st[s:e] = status.cpu().numpy()
 
     # Chunk c is finished (flags read, flagged problems re-solved, results copied back) only after
-    # chunk c + 1 is enqueued, so the device never waits for the host's look at the flags; the two
-    # chunks in flight use alternate workspace slots.
-    pending = None
-    cgraphs = {}
+    # the next max(1, S - 1) chunks are enqueued (S streams), so the device never waits for the
+    # host's look at the flags.  The chunks in flight use distinct workspace slots; the next chunk
+    # on a stream reuses a slot only after the chunk that held it was finished.
     use_graphs = graphs and method in ("gamma", "mixed")
+    nstreams = max(1, int(streams)) if method in ("gamma", "mixed") and not use_graphs else 1
+    cur = torch.cuda.current_stream(struct.device)
+    side = _chunk_streams(struct.device, nstreams) if nstreams > 1 else None
+    nslots, lag = max(2, nstreams), max(1, nstreams - 1)
+    pending = []
+    cgraphs = {}
     for c, s in enumerate(range(0, P, chunk)):
         e = min(P, s + chunk)
-        prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
-        status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
-        r_o = t_o = None
-        fix = _no_repair
-        if use_graphs and e - s == chunk and c > 0:
-            g = cgraphs.get(c % 2)
-            if g is None:
-                if pending is not None:  # the capture waits for the device anyway
-                    finish(pending)
-                    pending = None
-                g = cgraphs[c % 2] = ChunkGraph(struct, plan, chunk, prec, refine, epsi, epse, both_pols, c % 2,
-                                                prob)
-                r, t, status, fix = g.first()
+        sc = side[c % nstreams] if side else cur
+        if side:
+            sc.wait_stream(cur)
+        with torch.cuda.stream(sc):
+            prob = engine.Problems.make(wl[s:e], kpa[s:e], te[s:e], tm[s:e], struct.device)
+            status = torch.zeros(e - s, dtype=torch.int32, device=struct.device)
+            r_o = t_o = None
+            fix = _no_repair
+            if use_graphs and e - s == chunk and c > 0:
+                g = cgraphs.get(c % 2)
+                if g is None:
+                    while pending:  # the capture waits for the device anyway
+                        finish(pending.pop(0))
+                    g = cgraphs[c % 2] = ChunkGraph(struct, plan, chunk, prec, refine, epsi, epse, both_pols,
+                                                    c % 2, prob)
+                    r, t, status, fix = g.first()
+                else:
+                    r, t, status, fix = g.replay(prob)
+            elif method in ("gamma", "mixed"):
+                kw = dict(ws_slot=c % nslots, defer_repair=prec == "mixed")
+                if both_pols:
+                    out = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine, **kw)
+                else:
+                    out = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine,
+                                            **kw)
+                r, t = out[0], out[1]
+                if prec == "mixed":
+                    fix = out[2]
+            elif both_pols:
+                r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
             else:
-                r, t, status, fix = g.replay(prob)
-        elif method in ("gamma", "mixed"):
-            kw = dict(ws_slot=c % 2, defer_repair=prec == "mixed")
-            if both_pols:
-                out = solve_chunk_gamma_both_pols(struct, plan, prob, status, epsi, epse, prec, refine, **kw)
-            else:
-                out = solve_chunk_gamma(struct, plan, prob, status, epsi, epse, precision=prec, refine=refine, **kw)
-            r, t = out[0], out[1]
-            if prec == "mixed":
-                fix = out[2]
-        elif both_pols:
-            r, t = solve_chunk_both_pols(struct, specs, stack, prob, status, epsi, epse)
-        else:
-            r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
-        if pending is not None:
-            finish(pending)
-        pending = (s, e, r, t, r_o, t_o, status, fix)
-    if pending is not None:
-        finish(pending)
+                r, t, r_o, t_o = solve_chunk(struct, specs, stack, prob, status, orders, epsi, epse)
+        pending.append((sc, s, e, r, t, r_o, t_o, status, fix))
+        while len(pending) > lag:
+            finish(pending.pop(0))
+    while pending:
+        finish(pending.pop(0))
+    for sc in side or ():
+        cur.wait_stream(sc)
     if strict and st.any():
         bad = int(np.flatnonzero(st)[0])
         raise _capi.KhpError(f"problem {bad}: {_capi.decode_status(int(st[bad]))}")
