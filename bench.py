@@ -387,9 +387,10 @@ def bench_uneven(args):
 
 
 def bench_graphs(args):
-    """Chunk solves replayed as CUDA graphs against enqueued launch by launch (batch.solve_rt,
-    graphs=False / True), host wall clock through the public API: the 5x5 drop-in structure's 151
-    frequencies, eight times over, in chunks of 16 (small chunks, where launch overhead counts)."""
+    """Chunk solves replayed as CUDA graphs (one stream) against enqueued launch by launch on one
+    and on two streams (batch.solve_rt: graphs=True; graphs=False with streams=1, 2), host wall
+    clock through the public API: the 5x5 drop-in structure's 151 frequencies, eight times over,
+    in chunks of 16 (small chunks, where launch overhead counts)."""
     if args.graphs_check <= 0:
         return None
     from khepri_gb300 import batch, workloads
@@ -397,12 +398,12 @@ def bench_graphs(args):
     sw = workloads.plain_sweep()
     wl = np.tile(sw.wavelengths, 8)
     kp = np.tile(np.asarray(sw.kp).reshape(-1, 2), (8, 1))
-    for g in (False, True):
+    for name, g, ns in (("eager", False, 1), ("eager_2_streams", False, 2), ("graphs", True, 1)):
         batch.solve_rt((5, 5), sw.structure.layers, sw.structure.stack, wl[:64], kp[:64], chunk=16, method="mixed",
-                       graphs=g)
+                       graphs=g, streams=ns)
         _, t = _timed(lambda: batch.solve_rt((5, 5), sw.structure.layers, sw.structure.stack, wl, kp, chunk=16,
-                                             method="mixed", graphs=g))
-        out.setdefault("plain_5x5_chunk16", {})["graphs" if g else "eager"] = len(wl) / t
+                                             method="mixed", graphs=g, streams=ns))
+        out.setdefault("plain_5x5_chunk16", {})[name] = len(wl) / t
     return out
 
 
@@ -590,7 +591,8 @@ def run_gpu(args):
                 "peak_source": "FP32 FMA pipe measured in this run (khp_probe_fp32_tflops); MEASURED_PEAKS.json "
                                "lists only HBM and bf16",
                 "note": "latency-bound (one CTA per matrix; barriers and dependent loads inside each QR "
-                        "window), not pipe-bound",
+                        "window), not pipe-bound; with chunks on %d streams a stage's events span the share of "
+                        "the SMs the other stream's kernels take meanwhile, so stage times overlap" % nstreams,
                 "flops_per_launch": eig_flops, "launch_ms": eig_ms / eig_calls, "stages": stages,
                 "fp64_peak_tflops": fp64_peak}
         tc_ms, tc_calls = stage_ms["tc_product"]
@@ -701,7 +703,8 @@ def run_gpu(args):
                        "method": "reflection-matrix recursion (khp_solve_batched%s), one eigensolve per problem"
                                  % ("_mixed" if prec == "mixed" else ""),
                        "l2": "256 MB buffer written between steps (> 129 MB L2)",
-                       "parallelism": f"replicas x{world}", "problems_with_status": bad,
+                       "parallelism": f"replicas x{world}", "streams": nstreams,
+                       "problems_with_status": bad,
                        "repairs": repairs,
                        "solve_grad": grad_info, "uneven": uneven_info, "twisted_5x5": twisted_info,
                        "twisted_7x7": twisted7_info, "graphs": graphs_info},
