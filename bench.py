@@ -4,7 +4,8 @@ Workload (the batched sweep): one seed of the 11x11 structure — a 256x256 bina
 of 1-4 periodic discs, eps 12 in eps 1) shared by 3 patterned layers, 2 uniform layers, depths
 U(0.2, 1.0) — over 64 frequencies 0.3-0.7 c/a x a 32x32 Bloch grid (65,536 problems), both
 polarisations from one S-matrix per problem.  A step solves one chunk of ``--batch`` problems
-(successive chunks of the sweep).  Synthetic seeded inputs: no dataset is involved.
+(successive chunks of the sweep, dealt to two CUDA streams in turn so that two chunks are in
+flight).  Synthetic seeded inputs: no dataset is involved.
 
 * value: problems (S-matrix solves) per second with the problem arrays resident in HBM,
   timed with CUDA events over exactly K steps (barrier + synchronize on both sides).
