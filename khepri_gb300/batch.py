@@ -281,8 +281,9 @@ _CHUNK_STREAMS = {}
 
 
 def _chunk_streams(device, count):
-    """``count`` side streams of ``device`` that solve_rt deals its chunks to; the same streams on
-    every call, so that engine.workspace's per-stream cache finds their workspaces again."""
+    """``count`` side streams of ``device`` that solve_rt deals its chunks (and solve_structures
+    its shape groups) to; the same streams on every call, so that engine.workspace's per-stream
+    cache finds their workspaces again."""
     key = str(device)
     have = _CHUNK_STREAMS.setdefault(key, [])
     while len(have) < count:
@@ -648,7 +649,9 @@ def solve_structures(structures, wavelengths, kp, which=None, te=1.0, tm=0.0, la
         dev = torch.device("cuda", torch.cuda.current_device())
     main = torch.cuda.current_stream(dev)
     K = max(1, int(streams))
-    ss = [main] + [torch.cuda.Stream(device=dev) for _ in range(K - 1)]
+    # the same side streams on every call: engine.workspace keys its buffers by stream, so fresh
+    # streams (torch cycles through a pool of 32) would leave a workspace behind for each
+    ss = [main] + _chunk_streams(dev, K - 1)
     for s in ss[1:]:
         s.wait_stream(main)  # the caller's earlier work on the inputs comes first
     pending = [None] * K

@@ -47,3 +47,26 @@ def test_streams_with_deferred_resolves(khp):
         R, T, n = results[S]
         assert n == n1
         assert np.abs(R - R1).max() < 1e-12 and np.abs(T - T1).max() < 1e-12
+
+
+def test_repeated_calls_reuse_stream_workspaces(khp):
+    """solve_structures and solve_rt take their side streams from one persistent set, so calling
+    them again adds no workspace (engine.workspace keys its buffers by stream)."""
+    from khepri_gb300 import batch, engine, workloads
+    structs = workloads.uneven_structures(12, seed=3, n_pix=32, max_pw=5, max_layers=2)
+    entries = [(st.pw, st.layers, st.stack) for st, _, _ in structs]
+    wl = np.array([w for _, w, _ in structs])
+    kp = np.array([k for _, _, k in structs])
+    sw = workloads.plain_sweep(nfreq=40)
+    rt_args = ((5, 5), sw.structure.layers, sw.structure.stack, sw.wavelengths, sw.kp)
+    first = None
+    for _ in range(3):
+        R, T, s = batch.solve_structures(entries, wl, kp, chunk=4, streams=4, strict=False)
+        R2, T2, s2 = batch.solve_rt(*rt_args, chunk=8, method="mixed", streams=2)
+        assert not s2.any()
+        if first is None:
+            first = (len(engine._WS), R, T, R2, T2)
+        else:
+            assert len(engine._WS) == first[0]
+            assert np.array_equal(R, first[1], equal_nan=True) and np.array_equal(T, first[2], equal_nan=True)
+            assert np.array_equal(R2, first[3]) and np.array_equal(T2, first[4])
