@@ -15,7 +15,11 @@
  *     device arrays and are never turned into traps.
  *   - No call allocates device memory: scratch comes from the caller through `workspace`
  *     (size from the matching *_workspace function, 256-byte aligned base).
- *   - Calls are reentrant per stream and hold no host-global state.
+ *   - Calls are reentrant per stream and hold no host-global state.  Calls on different
+ *     streams may run concurrently on the device when each has its own workspace (kernels
+ *     share no device globals; khp_star_product_noalloc's fixed scratch is the one exception):
+ *     two chunks of a sweep in flight on two streams fill the SMs that one chunk's latency-
+ *     bound stages leave idle.
  *
  * The reference (Kaeryv/Khepri) is a numpy library; each entry point below replaces the
  * reference function named beside it (file:line in that project).
